@@ -1,0 +1,341 @@
+#!/usr/bin/env python
+"""Benchmark of the 2D GPE RK4 stepper (grid-point-steps/s).
+
+Workload (default): 1024^2 periodic box, plain FP64, i dpsi/dt = -1/2 lap psi
++ g|psi|^2 psi - mu psi (g = rho0 = mu = 1), 64 seeded vortices with minimum
+separation 4*sqrt(2)*dx, RK4 at dt = 5e-4.  One bench step = SUBSTEPS RK4 steps
+(vk_gpe_rk4(ctx, SUBSTEPS)); metric = N^2 * RK4 steps / second.
+
+  python bench.py [--gpus N --steps K --warmup W] [--impl reference]
+
+With N > 1 (torchrun) every rank steps its own independent field (replicas:
+a single field does not shard), value = all ranks' grid-point-steps / the
+slowest rank's time.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "RK4 grid-pt-steps/s at 1024^2"
+UNIT = "grid-pt-steps/s"
+PEAKS_FILE = os.path.join(ROOT, "MEASURED_PEAKS.json")
+FALLBACK_HBM_GBS = 6800.0
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--n", type=int, default=1024)
+    ap.add_argument("--substeps", type=int, default=20)
+    ap.add_argument("--no-fp32", action="store_true")
+    ap.add_argument("--cpu-seconds", type=float, default=12.0)
+    return ap.parse_args()
+
+
+def workload(n, seed):
+    from quantumvortices_gb300 import vk
+    dx = 2 * math.pi / n
+    psi0, _ = vk.ic_vortices(n, n, 64, seed=seed, min_sep=4 * math.sqrt(2) * dx)
+    return psi0
+
+
+def hbm_peak():
+    try:
+        with open(PEAKS_FILE) as f:
+            return float(json.load(f)["hbm_gbs"]), "measured"
+    except Exception:
+        return FALLBACK_HBM_GBS, "fallback"
+
+
+# ------------------------------------------------------------- clocks --
+
+class ClockSampler:
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        fd, self.path = tempfile.mkstemp(suffix=".csv")
+        os.close(fd)
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+        time.sleep(0.3)
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        sm, smax, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in open(self.path):
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                smax = float(f[2])
+            except ValueError:
+                continue
+            for nm, v in zip(names, f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        os.unlink(self.path)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": smax,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+# ---------------------------------------------------- per-kernel bytes --
+
+def kernel_bytes(tag, n, K, e, disk, stage=None):
+    """Bytes one launch of `tag` must move (its own loads + stores) at grid n^2,
+    element size e, K = largest kept |k|, disk = # modes with k^2 <= k2max."""
+    rows_half, rows_full = K + 1, 2 * K + 1
+    if tag == "k_x1":      # Ta (kept columns) in, psi out, rho x-spectrum (kx <= K) out
+        return e * (n * rows_full + n * n + n * rows_half)
+    if tag == "k_y1":      # Tb in, Tc out
+        return e * (2 * n * rows_half)
+    if tag == "k_x2":      # Tc in, psi in, Td (kept columns) out
+        return e * (n * rows_half + n * n + n * rows_full)
+    if tag == "k_y2_rk4":  # Td in; kpsi,str1,str2 in (disk); kpsi out (rows), str2 out (disk), Ta out
+        return e * (n * rows_full + 3 * disk + n * rows_full + disk + n * rows_full)
+    if tag == "k_xinv":
+        return e * (n * rows_full + n * n)
+    return None
+
+
+def count_disk(n):
+    ka2 = (n / 3.0) ** 2          # IF (ksqr .GE. kalias**2), src/gpe.f90:571
+    k2 = int(math.floor(ka2)) + 1
+    while float(k2) >= ka2:
+        k2 -= 1
+    k = np.array([i if i < n // 2 else i - n for i in range(n)])
+    ks = k[:, None] ** 2 + k[None, :] ** 2
+    return int((ks <= k2).sum()), int(math.isqrt(k2))
+
+
+# ---------------------------------------------------------- our arm --
+
+def run_ours(args, rank, world, local_rank):
+    import torch
+    from quantumvortices_gb300 import vk
+
+    torch.cuda.set_device(local_rank)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local_rank))
+
+    def barrier():
+        if dist is not None:
+            dist.barrier()
+        torch.cuda.synchronize()
+
+    n, S, K, W = args.n, args.substeps, args.steps, args.warmup
+    p = vk.params_for(n, dt=5e-4, precision=vk.VK_PREC_FP64)
+    psi0 = workload(n, seed=1 + rank)
+    flush = torch.empty(512 * 1024 * 1024, dtype=torch.uint8, device="cuda")
+
+    def timed_loop(solver, K, W):
+        ext = torch.cuda.ExternalStream(solver.stream)
+        for _ in range(W):
+            solver.gpe_rk4(S)
+        barrier()
+        ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(K)]
+        l0 = solver.launches
+        for i in range(K):
+            with torch.cuda.stream(ext):
+                flush.zero_()          # L2 flush between timed iterations (outside the events)
+            ev[i][0].record(ext)
+            solver.gpe_rk4(S)
+            ev[i][1].record(ext)
+        torch.cuda.synchronize()
+        launches = solver.launches - l0
+        ms = sum(a.elapsed_time(b) for a, b in ev)
+        barrier()
+        return ms, launches
+
+    s = vk.GPESolver(p)
+    s.set_psi(psi0)
+    sampler = ClockSampler(local_rank)
+    sampler.start()
+    ms, launches = timed_loop(s, K, W)
+    clocks = sampler.stop()
+    t = torch.tensor([ms], device="cuda", dtype=torch.float64)
+    if dist is not None:
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    ms_max = float(t.item())
+    value = world * n * n * S * K / (ms_max * 1e-3)
+
+    # per-kernel times (events around every launch, separate pass)
+    s.timing_begin()
+    s.gpe_rk4(S)
+    per = s.timing_end()
+
+    # end to end through the public API with host buffers
+    host_in = np.ascontiguousarray(psi0)
+    host_out = np.empty_like(host_in)
+    e2e_times = []
+    for i in range(3):
+        t0 = time.perf_counter()
+        s.set_psi(host_in)
+        s.gpe_rk4(S)
+        s.get_psi(host_out)
+        e2e_times.append(time.perf_counter() - t0)
+    e2e_t = statistics.median(e2e_times)
+    s.close()
+
+    # FP32 bulk path: throughput and error against the FP64 path after S steps
+    fp32 = None
+    if not args.no_fp32:
+        p32 = vk.params_for(n, dt=5e-4, precision=vk.VK_PREC_FP32)
+        s32 = vk.GPESolver(p32)
+        s32.set_psi(psi0)
+        ms32, l32 = timed_loop(s32, K, W)
+        s32.set_psi(psi0)
+        s32.gpe_rk4(100)
+        a = s32.get_psi()
+        s64 = vk.GPESolver(p)
+        s64.set_psi(psi0)
+        s64.gpe_rk4(100)
+        b = s64.get_psi()
+        s32.timing_begin()
+        s32.gpe_rk4(S)
+        per32 = s32.timing_end()
+        s32.close()
+        s64.close()
+        fp32 = {"value": world * n * n * S * K / (ms32 * 1e-3), "unit": UNIT, "ms_per_step": ms32 / K,
+                "rel_l2_psi_vs_fp64_after_100_steps": float(np.linalg.norm(a - b) / np.linalg.norm(b)),
+                "kernel_ms": {k: round(v[0] / v[1], 5) for k, v in per32.items()}}
+
+    if rank != 0:
+        return
+    disk, Kk = count_disk(n)
+    e = 16
+    # dominant kernel of the FP64 step
+    tag, (tot, cnt) = max(per.items(), key=lambda kv: kv[1][0])
+    per_launch_ms = tot / cnt
+    nbytes = kernel_bytes(tag, n, Kk, e, disk)
+    peak, peak_kind = hbm_peak()
+    achieved = nbytes / (per_launch_ms * 1e-3) / 1e9 if nbytes else None
+    step_ms = ms_max / (K * S)
+    canonical = 1344.0 * n * n / (step_ms * 1e-3) / 1e9  # SURVEY 8(d) model: 84 field transfers
+    out = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": K, "warmup": W,
+        "ms_per_step": ms_max / K, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f64", "data": "synthetic (seeded 64-vortex state)",
+        "config": {"workload": f"RK4 {n}^2 plain FP64, 64 vortices, dt=5e-4", "grid": n,
+                   "rk4_steps_per_step": S, "parallelism": "replicas" if world > 1 else "single",
+                   "l2": "flushed between timed steps (512 MiB write)"},
+        "clocks": clocks, "gpu_launches": launches,
+        "roofline": {"bound": "hbm", "kernel": tag, "achieved": achieved, "peak": peak,
+                     "peak_source": peak_kind, "unit": "GB/s",
+                     "frac": achieved / peak if achieved else None, "traffic": None,
+                     "algorithmic_bytes_per_launch": nbytes, "launch_ms": per_launch_ms,
+                     "step_canonical_gbs": canonical, "step_canonical_frac": canonical / peak,
+                     "fp64_dfma_bound_note": "GB300 FP64 issues ~1.9 DFMA/clk/SM (1.19 TFLOP/s measured)"},
+        "kernel_ms": {k: round(v[0] / v[1], 5) for k, v in per.items()},
+        "e2e": {"value": n * n * S / e2e_t, "unit": UNIT, "h2d_bytes_per_step": n * n * 16,
+                "d2h_bytes_per_step": n * n * 16},
+        "fp32": fp32,
+    }
+    out["cpu_baseline"] = cpu_baseline(n, psi0, args.cpu_seconds)
+    print(json.dumps(out))
+
+
+def cpu_baseline(n, psi0, seconds):
+    """The CPU FP64 oracle (restatement of src/gpe.f90 on the host cores)."""
+    from quantumvortices_gb300 import vk
+    from oracle.oracle import Oracle
+    cores = os.cpu_count() or 1
+    p = vk.params_for(n, dt=5e-4)
+    o = Oracle.from_vk_params(p, threads=cores)
+    o.set_psi(psi0)
+    t0 = time.perf_counter()
+    o.gpe_rk4(1)
+    t1 = time.perf_counter() - t0
+    steps = max(1, min(200, int(seconds / max(t1, 1e-6))))
+    t0 = time.perf_counter()
+    o.gpe_rk4(steps)
+    dt = time.perf_counter() - t0
+    return {"value": n * n * steps / dt, "unit": UNIT, "cores": cores, "kind": "port",
+            "sample": f"{steps} RK4 steps at {n}^2 FP64 (oracle restatement, OpenMP over rows)"}
+
+
+# ----------------------------------------------------- reference arm --
+
+def run_reference(args, rank):
+    if rank != 0:
+        return
+    from quantumvortices_gb300 import vk
+    from oracle.oracle import Oracle
+    n = args.n
+    cores = os.cpu_count() or 1
+    p = vk.params_for(n, dt=5e-4)
+    psi0 = workload(n, seed=1)
+    o = Oracle.from_vk_params(p, threads=cores)
+    o.set_psi(psi0)
+    for _ in range(args.warmup):
+        o.gpe_rk4(1)
+    times = []
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        o.gpe_rk4(1)
+        times.append(time.perf_counter() - t0)
+    tot = sum(times)
+    value = n * n * args.steps / tot
+    out = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
+           "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * tot / args.steps,
+           "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+           "data": "synthetic (seeded 64-vortex state)",
+           "config": {"workload": f"RK4 {n}^2 plain FP64, 64 vortices, dt=5e-4", "grid": n,
+                      "rk4_steps_per_step": 1},
+           "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port",
+                            "sample": f"1 RK4 step at {n}^2 per bench step; the Fortran+FFTW+MPI "
+                                      "reference cannot be built here (no gfortran, MPI or FFTW), so the "
+                                      "oracle restatement runs on all host cores"},
+           "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(out))
+
+
+def main():
+    args = parse()
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local_rank = int(os.environ.get("LOCAL_RANK", "0"))
+    if args.impl == "reference":
+        run_reference(args, rank)
+        return
+    run_ours(args, rank, world, local_rank)
+
+
+if __name__ == "__main__":
+    main()

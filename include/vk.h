@@ -1,0 +1,172 @@
+/*
+ * vk.h -- C ABI of the GB300-native VIKSHOBHA 2D GPE stepper (libvk.so).
+ *
+ * Drop-in boundary for the reference's Fortran hot path: the Fortran driver
+ * (src/driver.f90) keeps reading parameter.txt / parameter_gpe.txt, writing
+ * the wf / energy / spectra files and running the solve loop
+ * (src/solve.f90); the routines it calls for the state update and the
+ * diagnostics reductions come from here through ISO_C_BINDING.
+ *
+ * Conventions
+ *  - Every entry point returns int status: VK_OK (0) or a negative VK_E_*
+ *    code; vk_last_error() returns a message for the calling thread.
+ *  - All array arguments are HOST pointers owned by the caller.
+ *  - Complex arrays are interleaved (re, im) doubles, i.e. Fortran
+ *    COMPLEX(C_DOUBLE_COMPLEX).
+ *  - Physical layout psi(i1=x, i2=y), x fastest: element (x, y) at y*nx + x.
+ *    Fourier layout kpsi(i2=ky, i1=kx), ky fastest: element (kx, ky) at
+ *    kx*ny + ky -- the FFTW_MPI_TRANSPOSED_OUT layout of
+ *    src/mod_fft.f90:143-146.
+ *  - One context = one GPU state = one CUDA stream; a context is used from
+ *    one host thread at a time.
+ */
+#ifndef VK_H
+#define VK_H
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define VK_OK 0
+#define VK_E_INVALID (-1)   /* bad argument or parameter value          */
+#define VK_E_CUDA (-2)      /* a CUDA runtime call failed               */
+#define VK_E_NOMEM (-3)     /* device or host allocation failed          */
+#define VK_E_IO (-4)        /* file missing, truncated or malformed     */
+#define VK_E_STATE (-5)     /* call out of order (e.g. no psi set yet)  */
+#define VK_E_NUMERIC (-6)   /* NaN/Inf or norm blow-up detected          */
+
+#define VK_PREC_FP64 0      /* plain FP64 everywhere                       */
+#define VK_PREC_FP32 1      /* FP32 bulk, FP64 twiddles and reductions     */
+
+/* Solver parameters.  Field names follow the Fortran module globals
+ * (src/mod_grid.f90, src/mod_2dHD.f90, src/mod_gpparticles.f90) holding the
+ * values AFTER set_grid (src/mod_grid.f90:63-101) and the derived-physics
+ * block (src/driver.f90:360-396).  vk_params_derive() computes them from
+ * the raw namelist values. */
+typedef struct vk_params {
+  int32_t nx, ny;            /* &resolution Nx, Ny (powers of two, 16..4096) */
+  int32_t precision;         /* VK_PREC_FP64 or VK_PREC_FP32                 */
+  int32_t otoc;              /* -DGPOTOC: ic_OTOC_gpe after vk_set_psi        */
+  double dt;                 /* dt (= dt_fix)                                */
+  double alpha;              /* alpha = csound*xi*sqrt(rho_avg/2)            */
+  double gstrength;          /* g = csound^2/(2 alpha)                       */
+  double omega_chem;         /* Omega (= g without SGLE)                     */
+  double disp_factor;        /* &gpparam disp_factor                         */
+  double xi;                 /* xi after xi*dx                               */
+  double k_otoc_gp;          /* &gpotoc k_otoc_gp                            */
+  double eps_otoc_gp;        /* &gpotoc eps_otoc_gp                          */
+  int32_t n_particles;       /* &gpparticle gp_N_obj (0 = -DGPPART off)      */
+  int32_t argle_renorm;      /* ARGLE renormalisation to Nparticle (new)     */
+  double ppot_v0;            /* ppotV0 after *gstrength                      */
+  double ppot_d;             /* ppotd  after *xi                             */
+  double gp_mass_part;       /* &gpparticle gp_mass_part                     */
+  int32_t reserved[8];
+} vk_params;
+
+/* Raw namelist values (src/driver.f90:52-79) -> vk_params, restating
+ * set_grid (src/mod_grid.f90:63-101) and src/driver.f90:360-396. */
+typedef struct vk_namelist {
+  int32_t nx, ny;
+  double dt_fix;
+  double xi, csound, rho_avg, disp_factor;   /* &gpparam */
+  double k_otoc_gp, eps_otoc_gp;            /* &gpotoc  */
+  int32_t gp_n_obj;                         /* &gpparticle */
+  double gp_mass_part, ppotd, ppotv0, ppotthick;
+  int32_t maxiter, fsteps, ssteps, gsteps;  /* &tparam */
+  int32_t nrst, sprst;                      /* &ckprst */
+} vk_namelist;
+
+/* Replaces: the namelist reads + MPI_BCAST block (src/driver.f90:147-334).
+ * Parses parameter.txt and parameter_gpe.txt (either path may be NULL). */
+int vk_read_namelists(const char* parameter_txt, const char* parameter_gpe_txt, vk_namelist* out);
+/* Replaces: set_grid + derived GPE parameters (src/mod_grid.f90:63-101,
+ * src/driver.f90:360-396). */
+int vk_params_derive(const vk_namelist* nl, int32_t precision, int32_t otoc, vk_params* out);
+/* nshell = int(1.414*Nx/2.0d0)+1 (src/mod_grid.f90:77). */
+int32_t vk_nshell(int32_t nx);
+
+/* Replaces: mpi_localsize_estimate + create_state_variables +
+ * create_global_array + initialize_fft + global_array
+ * (src/mod_fft.f90:122-428, src/mod_2dHD.f90:62-76, src/pspectral.f90:1-35).
+ * Allocates the device state on the current CUDA device. */
+int vk_init(const vk_params* p, void** ctx);
+/* Replaces: clear_fft + free_state_variables + dealloc_global_array
+ * (src/mod_fft.f90:201-228,433-465, src/mod_2dHD.f90:78-92). */
+int vk_finalize(void* ctx);
+
+/* Replaces: restart_from_argle_data(0) + ic_OTOC_gpe
+ * (src/initial_config.f90:630-771, :295-368): psi <- psi_phys,
+ * kpsi <- F[psi]; with p->otoc the kpsi modes outside the 2/3 disk are
+ * zeroed and psi <- F^-1[kpsi]. */
+int vk_set_psi(void* ctx, const double* psi_phys);
+/* Sets kpsi directly (transposed Fourier layout); psi <- F^-1[kpsi]. */
+int vk_set_kpsi(void* ctx, const double* kpsi);
+/* Copies back psi (physical) / kpsi (transposed Fourier). */
+int vk_get_psi(void* ctx, double* psi_phys);
+int vk_get_kpsi(void* ctx, double* kpsi);
+
+/* Replaces: gpe_rk4 (src/gpe.f90:310-494) with gpe_rhs (:498-671) and, with
+ * particles, gp_particle_motion_rk4 (src/gpe_particle.f90:429-531);
+ * nsteps consecutive steps.  psi is current on return. */
+int vk_gpe_rk4(void* ctx, int32_t nsteps);
+/* Replaces: ARGLE(time) (src/gpe.f90:5-224), nsteps consecutive steps.
+ * As in the reference, psi on return is the field at the START of the last
+ * step.  residual_out (may be NULL) receives the new convergence measure
+ * ||kpsi_new-kpsi_old||_2 / (dt ||kpsi_old||_2) of the last step. */
+int vk_argle(void* ctx, int32_t nsteps, double* residual_out);
+
+/* Replaces: diagnostics_gpe (src/diagnostics.f90:4-571) reductions.
+ * scalars[10] = momx, momy, egrad, echem, eintr, etot, norm, eppot,
+ *               eobj_kin, esrep (reference scalings, :105-239).
+ * spec[(nshell+1)*6] in Fortran order spec_gp(0:nshell,1:6) (:394-399).
+ * nvort[2] (may be NULL) = (# of +1, # of -1) plaquette windings (new). */
+int vk_diagnostics(void* ctx, double* scalars, double* spec, int32_t* nvort);
+
+/* Particle state, Fortran (1:2,1:P) order: [p][d] (src/mod_gpparticles.f90:24-30).
+ * vk_particles_set also runs particle_potential (src/gpe_particle.f90:3-90). */
+int vk_particles_set(void* ctx, const double* pos, const double* vel, const double* f0ext);
+/* frc = gp_frc_obj as diagnostics_gpe leaves it (src/diagnostics.f90:528-533). */
+int vk_particles_get(void* ctx, double* pos, double* vel, double* frc);
+
+/* The context's CUDA stream (cudaStream_t), for callers that time or order
+ * work against it. */
+int vk_get_stream(void* ctx, void** stream);
+/* Number of kernels this context has launched so far. */
+int vk_kernel_launches(void* ctx, int64_t* count);
+
+/* Per-kernel timing.  Between vk_timing_begin and vk_timing_end every kernel
+ * this context launches is bracketed by CUDA events on the context's stream;
+ * vk_timing_end synchronises and returns, per kernel tag (NUL-terminated,
+ * 24 bytes each), the summed elapsed milliseconds and the launch count.
+ * Timing adds one event record per launch; time production runs without it. */
+int vk_timing_begin(void* ctx);
+int vk_timing_end(void* ctx, int32_t cap, char* tags, double* total_ms, int64_t* counts, int32_t* ntags);
+
+/* Thread-local message for the last failing call on this thread. */
+const char* vk_last_error(void);
+
+/* ---- host-side I/O in the reference's file formats (no GPU needed) ---- */
+
+/* io_fields (src/io_fields.f90:1-66, -DIOEVERYPROC, one rank): Fortran
+ * sequential-unformatted file: record (int32 iopoint, real64 time, real64 dt),
+ * then ny records of nx complex128 (x fastest). */
+int vk_write_wf(const char* path, int32_t iopoint, double time, double dt,
+                int32_t nx, int32_t ny, const double* psi_phys);
+/* Reads the same layout (restart_from_argle_data, src/initial_config.f90:727-741). */
+int vk_read_wf(const char* path, int32_t nx, int32_t ny, int32_t* iopoint,
+               double* time, double* dt, double* psi_phys);
+
+/* New (no reference counterpart): seeded N-vortex initial state.
+ * Positions from SplitMix64(seed), uniform on [0,2pi)^2 with periodic
+ * minimum separation min_sep; charges +1 for the first n_vort/2, -1 after.
+ * psi = prod_j A(r_j) * exp(i theta), A(r) = (r/xi0)/sqrt(2+(r/xi0)^2),
+ * theta the doubly periodic phase of the neutral set.  pos_out[2*n_vort]
+ * (may be NULL) receives the positions. */
+int vk_ic_vortices(int32_t nx, int32_t ny, int32_t n_vort, uint64_t seed,
+                   double xi0, double min_sep, double* psi_phys, double* pos_out);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* VK_H */

@@ -1,0 +1,75 @@
+"""In-tree build of libvk.so (CUDA for sm_103a + host C++).
+
+Each translation unit compiles in its own process (in parallel); objects go
+to quantumvortices_gb300/_build/, the library to quantumvortices_gb300/libvk.so.
+"""
+from __future__ import annotations
+
+import os
+import shutil
+import subprocess
+from concurrent.futures import ThreadPoolExecutor
+
+PKG = os.path.dirname(os.path.abspath(__file__))
+CSRC = os.path.join(PKG, "csrc")
+OUT_DIR = os.path.join(PKG, "_build")
+LIB = os.path.join(PKG, "libvk.so")
+
+CU_SRCS = ["vk_f64.cu", "vk_f32.cu", "vk_common.cu"]
+CPP_SRCS = ["vk_api.cpp", "vk_host.cpp"]
+ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+NVCC_FLAGS = ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC,-fopenmp",
+                     "--expt-relaxed-constexpr"]
+CXX_FLAGS = ["-O2", "-std=c++17", "-fPIC", "-fopenmp", "-fno-fast-math"]
+
+
+def _nvcc() -> str:
+    for cand in (shutil.which("nvcc"), "/usr/local/cuda/bin/nvcc"):
+        if cand and os.path.exists(cand):
+            return cand
+    raise RuntimeError("nvcc not found")
+
+
+def _run(cmd: list[str]) -> None:
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError("build failed:\n" + " ".join(cmd) + "\n" + r.stdout + r.stderr)
+
+
+def _stale(obj: str, src: str) -> bool:
+    if not os.path.exists(obj):
+        return True
+    deps = [src] + [os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith((".cuh", ".h"))]
+    deps.append(os.path.join(PKG, "..", "include", "vk.h"))
+    t = os.path.getmtime(obj)
+    return any(os.path.getmtime(d) > t for d in deps if os.path.exists(d))
+
+
+def build(verbose: bool = False, jobs: int | None = None) -> str:
+    """Compile every source that changed and link libvk.so; returns its path."""
+    os.makedirs(OUT_DIR, exist_ok=True)
+    nvcc = _nvcc()
+    cxx = os.environ.get("CXX", "g++")
+    cmds, objs = [], []
+    for s in CU_SRCS:
+        src, obj = os.path.join(CSRC, s), os.path.join(OUT_DIR, s + ".o")
+        objs.append(obj)
+        if _stale(obj, src):
+            cmds.append([nvcc, *NVCC_FLAGS, "-c", src, "-o", obj])
+    for s in CPP_SRCS:
+        src, obj = os.path.join(CSRC, s), os.path.join(OUT_DIR, s + ".o")
+        objs.append(obj)
+        if _stale(obj, src):
+            cmds.append([cxx, *CXX_FLAGS, "-c", src, "-o", obj])
+    if cmds:
+        with ThreadPoolExecutor(max_workers=jobs or min(8, len(cmds))) as ex:
+            list(ex.map(_run, cmds))
+    if cmds or not os.path.exists(LIB):
+        _run([nvcc, *ARCH, "-shared", "-o", LIB, *objs, "-Xcompiler", "-fopenmp", "-lgomp"])
+    if verbose:
+        print("built", LIB)
+    return LIB
+
+
+if __name__ == "__main__":
+    build(verbose=True)

@@ -1,0 +1,202 @@
+// vk_fft.cuh -- row FFT engine for sm_103a.
+//
+// A CTA holds R rows of L complex points in shared memory (row pitch
+// LP = L + L/16: one pad slot per 16 points keeps the strided Stockham stores
+// free of bank conflicts for 8- and 16-byte elements).  The transform is a
+// mixed-radix Stockham auto-sort FFT: every stage reads RAD points at stride
+// L/RAD, multiplies by table twiddles, runs a radix-RAD codelet in registers
+// and writes RAD points at stride NS, so the output comes out in natural
+// order.  Twiddles come from a per-length table W_L[k] = exp(-2 pi i k/L)
+// generated on the host in FP64 (and rounded once for FP32).
+//
+// FP64 on GB300 issues about two DFMA per clock per SM, so the codelets are
+// written for the fewest floating-point instructions: radix-16/8/4 butterflies
+// with +-i rotations as register swaps, W8 rotations as add+mul, and table
+// twiddles as 2 MUL + 2 FMA.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace vk {
+
+template <typename T> struct cvec;
+template <> struct cvec<double> { using type = double2; };
+template <> struct cvec<float> { using type = float2; };
+template <typename T> using cplx = typename cvec<T>::type;
+
+template <typename T> __device__ __forceinline__ cplx<T> mkc(T x, T y) { cplx<T> r; r.x = x; r.y = y; return r; }
+template <typename C> __device__ __forceinline__ C cadd(C a, C b) { a.x += b.x; a.y += b.y; return a; }
+template <typename C> __device__ __forceinline__ C csub(C a, C b) { a.x -= b.x; a.y -= b.y; return a; }
+template <typename C> __device__ __forceinline__ C cmul(C a, C b) {
+  C r;
+  r.x = a.x * b.x - a.y * b.y;
+  r.y = a.x * b.y + a.y * b.x;
+  return r;
+}
+template <typename C> __device__ __forceinline__ C cconj(C a) { a.y = -a.y; return a; }
+template <typename C, typename S> __device__ __forceinline__ C cscale(C a, S s) { a.x *= s; a.y *= s; return a; }
+
+// Multiply by exp(DIR * i*pi/2): -i for the forward (DIR<0), +i for inverse.
+template <int DIR, typename C> __device__ __forceinline__ C rot90(C a) {
+  C r;
+  if (DIR < 0) { r.x = a.y; r.y = -a.x; } else { r.x = -a.y; r.y = a.x; }
+  return r;
+}
+// Multiply by exp(DIR * i*pi/4) = (1 + DIR*i)/sqrt(2).
+template <int DIR, typename C> __device__ __forceinline__ C rot45(C a) {
+  typedef decltype(a.x) T;
+  const T r = T(0.70710678118654752440084436210484903928);
+  C o;
+  if (DIR < 0) { o.x = (a.x + a.y) * r; o.y = (a.y - a.x) * r; }
+  else { o.x = (a.x - a.y) * r; o.y = (a.x + a.y) * r; }
+  return o;
+}
+// Multiply by exp(DIR * i*3pi/4).
+template <int DIR, typename C> __device__ __forceinline__ C rot135(C a) { return rot90<DIR>(rot45<DIR>(a)); }
+// Multiply by the constant (c, DIR*s): exp(DIR*i*theta) with c = cos, s = sin.
+template <int DIR, typename C, typename T> __device__ __forceinline__ C rotc(C a, T c, T s) {
+  C o;
+  if (DIR < 0) { o.x = a.x * c + a.y * s; o.y = a.y * c - a.x * s; }
+  else { o.x = a.x * c - a.y * s; o.y = a.y * c + a.x * s; }
+  return o;
+}
+
+// ---- radix codelets: v[k] <- sum_m v[m] exp(DIR*2*pi*i*m*k/RAD) ----------
+
+template <int DIR, typename C> __device__ __forceinline__ void dft2(C& a, C& b) {
+  C t = a;
+  a = cadd(t, b);
+  b = csub(t, b);
+}
+
+template <int DIR, typename C> __device__ __forceinline__ void dft4(C& a0, C& a1, C& a2, C& a3) {
+  C t0 = cadd(a0, a2), t1 = csub(a0, a2);
+  C t2 = cadd(a1, a3), t3 = rot90<DIR>(csub(a1, a3));
+  a0 = cadd(t0, t2);
+  a2 = csub(t0, t2);
+  a1 = cadd(t1, t3);
+  a3 = csub(t1, t3);
+}
+
+template <int DIR, typename C> __device__ __forceinline__ void dft8(C* v) {
+  // even / odd DFT4 then one radix-2 layer with W8 rotations.
+  C e0 = v[0], e1 = v[2], e2 = v[4], e3 = v[6];
+  C o0 = v[1], o1 = v[3], o2 = v[5], o3 = v[7];
+  dft4<DIR>(e0, e1, e2, e3);
+  dft4<DIR>(o0, o1, o2, o3);
+  o1 = rot45<DIR>(o1);
+  o2 = rot90<DIR>(o2);
+  o3 = rot135<DIR>(o3);
+  v[0] = cadd(e0, o0); v[4] = csub(e0, o0);
+  v[1] = cadd(e1, o1); v[5] = csub(e1, o1);
+  v[2] = cadd(e2, o2); v[6] = csub(e2, o2);
+  v[3] = cadd(e3, o3); v[7] = csub(e3, o3);
+}
+
+template <int DIR, typename C> __device__ __forceinline__ void dft16(C* v) {
+  typedef decltype(v[0].x) T;
+  C e[8], o[8];
+#pragma unroll
+  for (int i = 0; i < 8; ++i) { e[i] = v[2 * i]; o[i] = v[2 * i + 1]; }
+  dft8<DIR>(e);
+  dft8<DIR>(o);
+  const T c1 = T(0.92387953251128675612818318939678828682);  // cos(pi/8)
+  const T s1 = T(0.38268343236508977172845998403039886676);  // sin(pi/8)
+  o[1] = rotc<DIR>(o[1], c1, s1);
+  o[2] = rot45<DIR>(o[2]);
+  o[3] = rotc<DIR>(o[3], s1, c1);
+  o[4] = rot90<DIR>(o[4]);
+  o[5] = rot90<DIR>(rotc<DIR>(o[5], c1, s1));
+  o[6] = rot135<DIR>(o[6]);
+  o[7] = rot90<DIR>(rotc<DIR>(o[7], s1, c1));
+#pragma unroll
+  for (int k = 0; k < 8; ++k) {
+    v[k] = cadd(e[k], o[k]);
+    v[k + 8] = csub(e[k], o[k]);
+  }
+}
+
+template <int RAD, int DIR, typename C> __device__ __forceinline__ void dft(C* v) {
+  if (RAD == 2) dft2<DIR>(v[0], v[1]);
+  else if (RAD == 4) dft4<DIR>(v[0], v[1], v[2], v[3]);
+  else if (RAD == 8) dft8<DIR>(v);
+  else if (RAD == 16) dft16<DIR>(v);
+}
+
+// ---- plans ----------------------------------------------------------------
+
+template <int... Rs> struct RadixList {};
+template <int L> struct PlanFor;
+template <> struct PlanFor<16> { using type = RadixList<16>; static constexpr int maxrad = 16; };
+template <> struct PlanFor<32> { using type = RadixList<8, 4>; static constexpr int maxrad = 8; };
+template <> struct PlanFor<64> { using type = RadixList<8, 8>; static constexpr int maxrad = 8; };
+template <> struct PlanFor<128> { using type = RadixList<16, 8>; static constexpr int maxrad = 16; };
+template <> struct PlanFor<256> { using type = RadixList<16, 16>; static constexpr int maxrad = 16; };
+template <> struct PlanFor<512> { using type = RadixList<8, 8, 8>; static constexpr int maxrad = 8; };
+template <> struct PlanFor<1024> { using type = RadixList<16, 16, 4>; static constexpr int maxrad = 16; };
+template <> struct PlanFor<2048> { using type = RadixList<16, 16, 8>; static constexpr int maxrad = 16; };
+template <> struct PlanFor<4096> { using type = RadixList<16, 16, 16>; static constexpr int maxrad = 16; };
+
+__host__ __device__ constexpr int padded(int L) { return L + L / 16; }
+__device__ __forceinline__ int pidx(int i) { return i + (i >> 4); }
+
+// One Stockham stage over R rows held in s (pitch LP), NT threads.
+template <typename T, int L, int R, int NT, int RAD, int NS, int DIR>
+__device__ __forceinline__ void stockham_stage(cplx<T>* s, const cplx<T>* __restrict__ tw) {
+  typedef cplx<T> C;
+  constexpr int NB = L / RAD;
+  constexpr int LP = padded(L);
+  static_assert((R * NB) % NT == 0, "threads must tile the butterflies");
+  constexpr int PER = (R * NB) / NT;
+  C v[PER][RAD];
+#pragma unroll
+  for (int p = 0; p < PER; ++p) {
+    const int b = threadIdx.x + p * NT;
+    const int row = b / NB, j = b % NB;
+    const C* sr = s + row * LP;
+#pragma unroll
+    for (int m = 0; m < RAD; ++m) v[p][m] = sr[pidx(j + m * NB)];
+    if (NS > 1) {
+      const int jj = j % NS;
+#pragma unroll
+      for (int m = 1; m < RAD; ++m) {
+        C w = __ldg(tw + jj * m * (L / (NS * RAD)));
+        if (DIR > 0) w.y = -w.y;
+        v[p][m] = cmul(v[p][m], w);
+      }
+    }
+    dft<RAD, DIR>(v[p]);
+  }
+  __syncthreads();
+#pragma unroll
+  for (int p = 0; p < PER; ++p) {
+    const int b = threadIdx.x + p * NT;
+    const int row = b / NB, j = b % NB;
+    C* sr = s + row * LP;
+    const int base = (j / NS) * NS * RAD + (j % NS);
+#pragma unroll
+    for (int m = 0; m < RAD; ++m) sr[pidx(base + m * NS)] = v[p][m];
+  }
+  __syncthreads();
+}
+
+template <typename T, int L, int R, int NT, int DIR, int NS>
+__device__ __forceinline__ void run_stages(cplx<T>*, const cplx<T>*, RadixList<>) {}
+
+template <typename T, int L, int R, int NT, int DIR, int NS, int RAD, int... Rest>
+__device__ __forceinline__ void run_stages(cplx<T>* s, const cplx<T>* tw, RadixList<RAD, Rest...>) {
+  stockham_stage<T, L, R, NT, RAD, NS, DIR>(s, tw);
+  run_stages<T, L, R, NT, DIR, NS * RAD>(s, tw, RadixList<Rest...>());
+}
+
+// In-place FFT of R rows in shared memory.  Caller must __syncthreads()
+// after filling s; on return s holds the natural-order transform and all
+// threads are synchronised.  DIR = -1 forward, +1 inverse (unnormalised).
+template <typename T, int L, int R, int NT, int DIR>
+__device__ __forceinline__ void fft_rows(cplx<T>* s, const cplx<T>* __restrict__ tw) {
+  run_stages<T, L, R, NT, DIR, 1>(s, tw, typename PlanFor<L>::type());
+}
+
+template <int L> struct RowCfg { static constexpr int maxrad = PlanFor<L>::maxrad; };
+
+}  // namespace vk

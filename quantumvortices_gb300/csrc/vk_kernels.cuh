@@ -1,0 +1,564 @@
+// vk_kernels.cuh -- fused row-pass kernels of the 2D GPE stepper (sm_103a).
+//
+// Every 2D transform is two row passes.  The "x pass" holds rows y of a
+// physical-space field (x contiguous) and writes its x-spectrum TRANSPOSED,
+// [kx][y]; the "y pass" holds rows kx of that (y contiguous) and finishes the
+// 2D transform along y, so the Fourier state sits in the reference's
+// transposed layout kpsi[kx][ky] (src/mod_fft.f90:143-146) and every pass
+// reads contiguous rows.  The pointwise work of gpe_rhs / gpe_rk4 / ARGLE is
+// fused into the passes:
+//
+//   X1  Ta[y][kx] --F^-1_x--> psi (stored)   rho=|psi|^2 --F_x (two real rows
+//       per complex FFT)--> Tb[kx][y], kx in [0,K]
+//   Y1  Tb --F_y--> 2/3 mask --F^-1_y--> Tc[y][kx], kx in [0,K]
+//   X2  Tc --F^-1_x (two real rows per FFT)--> P_G rho;  N = g P_G rho psi
+//       (+ V psi) --F_x--> Td[kx][y]
+//   Y2  Td --F_y--> N^; RK4 stage / ARGLE update of kpsi, str1, str2;
+//       kpsi_new --F^-1_y--> Ta[y][kx]
+//
+// K is the largest |k| kept by the 2/3 rule (k1^2+k2^2 < (Nx/3)^2); with the
+// RK4 mask every column |kx| > K of kpsi, of the RHS and of Ta is zero, so
+// the RK4 passes skip those rows (identical arithmetic on every kept mode).
+#pragma once
+#include "vk_fft.cuh"
+
+namespace vk {
+
+// Launch geometry per (precision, row length): R rows per CTA (even, for the
+// real-row pairing), NT threads = R*L/maxrad (one max-radix butterfly per
+// thread and stage).
+template <typename T, int L> struct Geo;
+#define VK_GEO(TT, LL, RR)                                                  \
+  template <> struct Geo<TT, LL> {                                          \
+    static constexpr int L = LL, R = RR, LP = padded(LL);                   \
+    static constexpr int NT = RR * LL / PlanFor<LL>::maxrad;                \
+    static constexpr int NTH = (RR / 2) * LL / PlanFor<LL>::maxrad;         \
+  };
+VK_GEO(double, 16, 16) VK_GEO(double, 32, 16) VK_GEO(double, 64, 16) VK_GEO(double, 128, 8)
+VK_GEO(double, 256, 4) VK_GEO(double, 512, 2) VK_GEO(double, 1024, 2) VK_GEO(double, 2048, 2)
+VK_GEO(double, 4096, 2)
+VK_GEO(float, 16, 16) VK_GEO(float, 32, 16) VK_GEO(float, 64, 16) VK_GEO(float, 128, 8)
+VK_GEO(float, 256, 8) VK_GEO(float, 512, 4) VK_GEO(float, 1024, 4) VK_GEO(float, 2048, 2)
+VK_GEO(float, 4096, 2)
+#undef VK_GEO
+
+// FFT of the first NR rows of s with only the first NTA threads doing work;
+// all threads must call it (it synchronises).
+template <typename T, int L, int NR, int NTA, int DIR, int NTB>
+__device__ __forceinline__ void fft_rows_sub(cplx<T>* s, const cplx<T>* __restrict__ tw);
+
+template <typename T, int L, int NR, int NTA, int DIR, int NS, int NTB>
+__device__ __forceinline__ void run_stages_sub(cplx<T>*, const cplx<T>*, RadixList<>) {}
+
+template <typename T, int L, int NR, int NTA, int RAD, int NS, int DIR, int NTB>
+__device__ __forceinline__ void stockham_stage_sub(cplx<T>* s, const cplx<T>* __restrict__ tw) {
+  typedef cplx<T> C;
+  constexpr int NB = L / RAD;
+  constexpr int LP = padded(L);
+  static_assert((NR * NB) % NTA == 0, "threads must tile the butterflies");
+  constexpr int PER = (NR * NB) / NTA;
+  const bool active = (NTA == NTB) || (threadIdx.x < NTA);
+  C v[PER][RAD];
+  if (active) {
+#pragma unroll
+    for (int p = 0; p < PER; ++p) {
+      const int b = threadIdx.x + p * NTA;
+      const int row = b / NB, j = b % NB;
+      const C* sr = s + row * LP;
+#pragma unroll
+      for (int m = 0; m < RAD; ++m) v[p][m] = sr[pidx(j + m * NB)];
+      if (NS > 1) {
+        const int jj = j % NS;
+#pragma unroll
+        for (int m = 1; m < RAD; ++m) {
+          C w = __ldg(tw + jj * m * (L / (NS * RAD)));
+          if (DIR > 0) w.y = -w.y;
+          v[p][m] = cmul(v[p][m], w);
+        }
+      }
+      dft<RAD, DIR>(v[p]);
+    }
+  }
+  __syncthreads();
+  if (active) {
+#pragma unroll
+    for (int p = 0; p < PER; ++p) {
+      const int b = threadIdx.x + p * NTA;
+      const int row = b / NB, j = b % NB;
+      C* sr = s + row * LP;
+      const int base = (j / NS) * NS * RAD + (j % NS);
+#pragma unroll
+      for (int m = 0; m < RAD; ++m) sr[pidx(base + m * NS)] = v[p][m];
+    }
+  }
+  __syncthreads();
+}
+
+template <typename T, int L, int NR, int NTA, int DIR, int NS, int NTB, int RAD, int... Rest>
+__device__ __forceinline__ void run_stages_sub(cplx<T>* s, const cplx<T>* tw, RadixList<RAD, Rest...>) {
+  stockham_stage_sub<T, L, NR, NTA, RAD, NS, DIR, NTB>(s, tw);
+  run_stages_sub<T, L, NR, NTA, DIR, NS * RAD, NTB>(s, tw, RadixList<Rest...>());
+}
+
+template <typename T, int L, int NR, int NTA, int DIR, int NTB>
+__device__ __forceinline__ void fft_rows_sub(cplx<T>* s, const cplx<T>* __restrict__ tw) {
+  run_stages_sub<T, L, NR, NTA, DIR, 1, NTB>(s, tw, typename PlanFor<L>::type());
+}
+
+__device__ __forceinline__ int kwn(int i, int n) { return i < n / 2 ? i : i - n; }
+
+// Row index of logical row l when only |kx| <= K rows are processed.
+__device__ __forceinline__ int pruned_row(int l, int K, int n) { return l <= K ? l : n - (2 * K + 1 - l); }
+
+// Scalars shared by the passes (by value in the launch).
+struct StepConsts {
+  int nx, ny;        // grid
+  int K;             // max |k| kept by the 2/3 rule
+  int k2max;         // largest kept k1^2+k2^2
+  int pk;            // row pitch of Tc (>= K+1)
+  double alpha, g, omega, dt;
+  double prefac_re, prefac_im;   // (1 - i*disp_factor)/i
+  double scale;      // 1/(nx*ny)
+};
+
+// ------------------------------------------------------------------------
+// Generic passes (set_psi, readback, diagnostics helpers).
+// ------------------------------------------------------------------------
+
+// rows y of src[y][x] -> F_x -> dst[kx][y] (all kx).
+template <typename T, int L>
+__global__ void __launch_bounds__(Geo<T, L>::NT) k_xfwd(const cplx<T>* __restrict__ src, cplx<T>* __restrict__ dst,
+                                                     const cplx<T>* __restrict__ tw, int ny) {
+  typedef Geo<T, L> G;
+  typedef cplx<T> C;
+  extern __shared__ __align__(16) unsigned char smraw[];
+  C* s = reinterpret_cast<C*>(smraw);
+  const int y0 = blockIdx.x * G::R;
+  for (int e = threadIdx.x; e < G::R * L; e += G::NT) {
+    const int r = e / L, x = e % L;
+    s[r * G::LP + pidx(x)] = src[(size_t)(y0 + r) * L + x];
+  }
+  __syncthreads();
+  fft_rows<T, L, G::R, G::NT, -1>(s, tw);
+  for (int e = threadIdx.x; e < G::R * L; e += G::NT) {
+    const int r = e % G::R, k = e / G::R;
+    dst[(size_t)k * ny + y0 + r] = s[r * G::LP + pidx(k)];
+  }
+}
+
+// rows kx of src[kx][y] -> F_y -> dst[kx][ky].  With MASKOUT the 2/3 mask
+// (and an optional shell amplification, ic_OTOC_gpe) is applied on the way out.
+template <typename T, int L, bool OTOC>
+__global__ void __launch_bounds__(Geo<T, L>::NT) k_yfwd(const cplx<T>* __restrict__ src, cplx<T>* __restrict__ dst,
+                                                     const cplx<T>* __restrict__ tw, int nx, int k2max,
+                                                     double k_otoc, double eps_otoc) {
+  typedef Geo<T, L> G;
+  typedef cplx<T> C;
+  extern __shared__ __align__(16) unsigned char smraw[];
+  C* s = reinterpret_cast<C*>(smraw);
+  const int x0 = blockIdx.x * G::R;
+  for (int e = threadIdx.x; e < G::R * L; e += G::NT) {
+    const int r = e / L, y = e % L;
+    s[r * G::LP + pidx(y)] = src[(size_t)(x0 + r) * L + y];
+  }
+  __syncthreads();
+  fft_rows<T, L, G::R, G::NT, -1>(s, tw);
+  for (int e = threadIdx.x; e < G::R * L; e += G::NT) {
+    const int r = e / L, ky = e % L;
+    C v = s[r * G::LP + pidx(ky)];
+    if (OTOC) {
+      const int k1 = kwn(x0 + r, nx), k2 = kwn(ky, L);
+      const int ksq = k1 * k1 + k2 * k2;
+      const double rk = sqrt((double)ksq);
+      const int mshl = (int)llrint(rk);  // nint(rk): |rk| is never a half-integer
+      if ((double)mshl == k_otoc) v = cscale(v, T(1.0 + eps_otoc));
+      if (ksq > k2max) v = mkc<T>(T(0), T(0));
+    }
+    dst[(size_t)(x0 + r) * L + ky] = v;
+  }
+}
+
+// rows kx of src[kx][ky] -> F^-1_y -> dst[y][kx] (pitch nx).
+template <typename T, int L>
+__global__ void __launch_bounds__(Geo<T, L>::NT) k_yinv(const cplx<T>* __restrict__ src, cplx<T>* __restrict__ dst,
+                                                     const cplx<T>* __restrict__ tw, int nx) {
+  typedef Geo<T, L> G;
+  typedef cplx<T> C;
+  extern __shared__ __align__(16) unsigned char smraw[];
+  C* s = reinterpret_cast<C*>(smraw);
+  const int x0 = blockIdx.x * G::R;
+  for (int e = threadIdx.x; e < G::R * L; e += G::NT) {
+    const int r = e / L, y = e % L;
+    s[r * G::LP + pidx(y)] = src[(size_t)(x0 + r) * L + y];
+  }
+  __syncthreads();
+  fft_rows<T, L, G::R, G::NT, +1>(s, tw);
+  for (int e = threadIdx.x; e < G::R * L; e += G::NT) {
+    const int r = e % G::R, y = e / G::R;
+    dst[(size_t)y * nx + x0 + r] = s[r * G::LP + pidx(y)];
+  }
+}
+
+// rows y of src[y][kx] -> F^-1_x -> * scale -> dst[y][x].  With PRUNE only
+// columns |kx| <= K are read (the rest are known zero).
+template <typename T, int L, bool PRUNE>
+__global__ void __launch_bounds__(Geo<T, L>::NT) k_xinv(const cplx<T>* __restrict__ src, cplx<T>* __restrict__ dst,
+                                                     const cplx<T>* __restrict__ tw, T scale, int K) {
+  typedef Geo<T, L> G;
+  typedef cplx<T> C;
+  extern __shared__ __align__(16) unsigned char smraw[];
+  C* s = reinterpret_cast<C*>(smraw);
+  const int y0 = blockIdx.x * G::R;
+  for (int e = threadIdx.x; e < G::R * L; e += G::NT) {
+    const int r = e / L, k = e % L;
+    C v = mkc<T>(T(0), T(0));
+    if (!PRUNE || k <= K || k >= L - K) v = src[(size_t)(y0 + r) * L + k];
+    s[r * G::LP + pidx(k)] = v;
+  }
+  __syncthreads();
+  fft_rows<T, L, G::R, G::NT, +1>(s, tw);
+  for (int e = threadIdx.x; e < G::R * L; e += G::NT) {
+    const int r = e / L, x = e % L;
+    dst[(size_t)(y0 + r) * L + x] = cscale(s[r * G::LP + pidx(x)], scale);
+  }
+}
+
+// Zero kpsi rows |kx| > K and in-row modes outside the 2/3 disk (the mask at
+// the start of gpe_rk4, src/gpe.f90:338-355).
+template <typename T>
+__global__ void k_mask_four(cplx<T>* __restrict__ f, int nx, int ny, int k2max) {
+  const size_t n = (size_t)nx * ny;
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+    const int kx = (int)(i / ny), ky = (int)(i % ny);
+    const int k1 = kwn(kx, nx), k2 = kwn(ky, ny);
+    if (k1 * k1 + k2 * k2 > k2max) f[i] = mkc<T>(T(0), T(0));
+  }
+}
+
+// ------------------------------------------------------------------------
+// X1: psi and the x-spectrum of rho = |psi|^2.
+//   FROM_T: Ta[y][kx] --F^-1_x, *scale--> psi (written); else psi is read.
+//   PRUNE : Ta columns |kx| > K are zero (RK4).
+// Output Tb[kx][y] for kx in [0, K] (Hermitian half of the real rows).
+// ------------------------------------------------------------------------
+template <typename T, int L, bool FROM_T, bool PRUNE>
+__global__ void __launch_bounds__(Geo<T, L>::NT) k_x1(const cplx<T>* __restrict__ Ta, cplx<T>* __restrict__ psi,
+                                                   cplx<T>* __restrict__ Tb, const cplx<T>* __restrict__ tw,
+                                                   StepConsts c) {
+  typedef Geo<T, L> G;
+  typedef cplx<T> C;
+  extern __shared__ __align__(16) unsigned char smraw[];
+  C* s = reinterpret_cast<C*>(smraw);
+  const int y0 = blockIdx.x * G::R;
+  const int ny = c.ny, K = c.K;
+  if (FROM_T) {
+    for (int e = threadIdx.x; e < G::R * L; e += G::NT) {
+      const int r = e / L, k = e % L;
+      C v = mkc<T>(T(0), T(0));
+      if (!PRUNE || k <= K || k >= L - K) v = Ta[(size_t)(y0 + r) * L + k];
+      s[r * G::LP + pidx(k)] = v;
+    }
+    __syncthreads();
+    fft_rows<T, L, G::R, G::NT, +1>(s, tw);
+    const T scale = T(c.scale);
+    for (int e = threadIdx.x; e < G::R * L; e += G::NT) {
+      const int r = e / L, x = e % L;
+      C v = cscale(s[r * G::LP + pidx(x)], scale);
+      s[r * G::LP + pidx(x)] = v;
+      psi[(size_t)(y0 + r) * L + x] = v;
+    }
+  } else {
+    for (int e = threadIdx.x; e < G::R * L; e += G::NT) {
+      const int r = e / L, x = e % L;
+      s[r * G::LP + pidx(x)] = psi[(size_t)(y0 + r) * L + x];
+    }
+  }
+  __syncthreads();
+  // rho for row pairs: z_p(x) = rho(x, y0+2p) + i rho(x, y0+2p+1), into row p.
+  constexpr int NPAIR = G::R / 2;
+  constexpr int PER = NPAIR * L / G::NT;
+  static_assert(NPAIR * L % G::NT == 0, "pairing tile");
+  C z[PER];
+#pragma unroll
+  for (int q = 0; q < PER; ++q) {
+    const int e = threadIdx.x + q * G::NT;
+    const int p = e / L, x = e % L;
+    const C a = s[(2 * p) * G::LP + pidx(x)], b = s[(2 * p + 1) * G::LP + pidx(x)];
+    z[q] = mkc<T>(a.x * a.x + a.y * a.y, b.x * b.x + b.y * b.y);
+  }
+  __syncthreads();
+#pragma unroll
+  for (int q = 0; q < PER; ++q) {
+    const int e = threadIdx.x + q * G::NT;
+    const int p = e / L, x = e % L;
+    s[p * G::LP + pidx(x)] = z[q];
+  }
+  __syncthreads();
+  fft_rows_sub<T, L, NPAIR, G::NTH, -1, G::NT>(s, tw);
+  // unpack: A(k) = (Z(k) + conj Z(-k))/2, B(k) = -i (Z(k) - conj Z(-k))/2
+  for (int e = threadIdx.x; e < G::R * (K + 1); e += G::NT) {
+    const int r = e % G::R, k = e / G::R;
+    const int p = r >> 1;
+    const C zk = s[p * G::LP + pidx(k)];
+    const C zm = s[p * G::LP + pidx((L - k) & (L - 1))];
+    C v;
+    if ((r & 1) == 0) v = mkc<T>(T(0.5) * (zk.x + zm.x), T(0.5) * (zk.y - zm.y));
+    else v = mkc<T>(T(0.5) * (zk.y + zm.y), T(0.5) * (zm.x - zk.x));
+    Tb[(size_t)k * ny + y0 + r] = v;
+  }
+}
+
+// ------------------------------------------------------------------------
+// Y1: rows kx in [0,K] of Tb: F_y, 2/3 mask, F^-1_y -> Tc[y][kx] (pitch pk).
+// ------------------------------------------------------------------------
+template <typename T, int L>
+__global__ void __launch_bounds__(Geo<T, L>::NT) k_y1(const cplx<T>* __restrict__ Tb, cplx<T>* __restrict__ Tc,
+                                                   const cplx<T>* __restrict__ tw, StepConsts c) {
+  typedef Geo<T, L> G;
+  typedef cplx<T> C;
+  extern __shared__ __align__(16) unsigned char smraw[];
+  C* s = reinterpret_cast<C*>(smraw);
+  const int l0 = blockIdx.x * G::R;
+  const int K = c.K;
+  for (int e = threadIdx.x; e < G::R * L; e += G::NT) {
+    const int r = e / L, y = e % L;
+    C v = mkc<T>(T(0), T(0));
+    if (l0 + r <= K) v = Tb[(size_t)(l0 + r) * L + y];
+    s[r * G::LP + pidx(y)] = v;
+  }
+  __syncthreads();
+  fft_rows<T, L, G::R, G::NT, -1>(s, tw);
+  for (int e = threadIdx.x; e < G::R * L; e += G::NT) {
+    const int r = e / L, ky = e % L;
+    const int k1 = l0 + r, k2 = kwn(ky, L);
+    if (k1 * k1 + k2 * k2 > c.k2max) s[r * G::LP + pidx(ky)] = mkc<T>(T(0), T(0));
+  }
+  __syncthreads();
+  fft_rows<T, L, G::R, G::NT, +1>(s, tw);
+  for (int e = threadIdx.x; e < G::R * L; e += G::NT) {
+    const int r = e % G::R, y = e / G::R;
+    if (l0 + r <= K) Tc[(size_t)y * c.pk + l0 + r] = s[r * G::LP + pidx(y)];
+  }
+}
+
+// ------------------------------------------------------------------------
+// X2: rows y of Tc (kx in [0,K]) -> P_G rho (real, two rows per complex
+// F^-1_x) -> N = SIGN*g*P_G rho*psi [+ SIGN*V*psi] -> F_x -> Td[kx][y].
+// SIGN = +1 for gpe_rhs (src/gpe.f90:583-594), -1 for ARGLE (:101-112).
+// PRUNE_OUT: only |kx| <= K columns of Td are written (RK4).
+// ------------------------------------------------------------------------
+template <typename T, int L, int SIGN, bool PRUNE_OUT, bool POT>
+__global__ void __launch_bounds__(Geo<T, L>::NT) k_x2(const cplx<T>* __restrict__ Tc, const cplx<T>* __restrict__ psi,
+                                                   const T* __restrict__ vpot, cplx<T>* __restrict__ Td,
+                                                   const cplx<T>* __restrict__ tw, StepConsts c) {
+  typedef Geo<T, L> G;
+  typedef cplx<T> C;
+  extern __shared__ __align__(16) unsigned char smraw[];
+  C* s = reinterpret_cast<C*>(smraw);
+  const int y0 = blockIdx.x * G::R;
+  const int K = c.K, ny = c.ny, pk = c.pk;
+  constexpr int NPAIR = G::R / 2;
+  // Z_p(k) = A(k) + i B(k) with the Hermitian extension to negative k.
+  for (int e = threadIdx.x; e < NPAIR * L; e += G::NT) {
+    const int p = e / L, k = e % L;
+    C v = mkc<T>(T(0), T(0));
+    const size_t ra = (size_t)(y0 + 2 * p) * pk, rb = ra + pk;
+    if (k <= K) {
+      const C a = Tc[ra + k], b = Tc[rb + k];
+      v = mkc<T>(a.x - b.y, a.y + b.x);
+    } else if (k >= L - K) {
+      const C a = Tc[ra + (L - k)], b = Tc[rb + (L - k)];
+      // conj(a) + i conj(b)
+      v = mkc<T>(a.x + b.y, b.x - a.y);
+    }
+    s[p * G::LP + pidx(k)] = v;
+  }
+  __syncthreads();
+  fft_rows_sub<T, L, NPAIR, G::NTH, +1, G::NT>(s, tw);
+  constexpr int PER = G::R * L / G::NT;
+  C nv[PER];
+  const T gs = T(SIGN * c.g);
+  const T scale = T(c.scale);
+#pragma unroll
+  for (int q = 0; q < PER; ++q) {
+    const int e = threadIdx.x + q * G::NT;
+    const int r = e / L, x = e % L;
+    const C z = s[(r >> 1) * G::LP + pidx(x)];
+    const T pg = ((r & 1) == 0 ? z.x : z.y) * scale;  // P_G[|psi|^2](x, y0+r)
+    const C ps = psi[(size_t)(y0 + r) * L + x];
+    const T gp = gs * pg;
+    C n = mkc<T>(gp * ps.x, gp * ps.y);
+    if (POT) {
+      const T v = T(SIGN) * vpot[(size_t)(y0 + r) * L + x];
+      n.x += v * ps.x;
+      n.y += v * ps.y;
+    }
+    nv[q] = n;
+  }
+  __syncthreads();
+#pragma unroll
+  for (int q = 0; q < PER; ++q) {
+    const int e = threadIdx.x + q * G::NT;
+    const int r = e / L, x = e % L;
+    s[r * G::LP + pidx(x)] = nv[q];
+  }
+  __syncthreads();
+  fft_rows<T, L, G::R, G::NT, -1>(s, tw);
+  if (PRUNE_OUT) {
+    const int ncol = 2 * K + 1;
+    for (int e = threadIdx.x; e < G::R * ncol; e += G::NT) {
+      const int r = e % G::R, l = e / G::R;
+      const int k = pruned_row(l, K, L);
+      Td[(size_t)k * ny + y0 + r] = s[r * G::LP + pidx(k)];
+    }
+  } else {
+    for (int e = threadIdx.x; e < G::R * L; e += G::NT) {
+      const int r = e % G::R, k = e / G::R;
+      Td[(size_t)k * ny + y0 + r] = s[r * G::LP + pidx(k)];
+    }
+  }
+}
+
+// ------------------------------------------------------------------------
+// Y2 (RK4 stage STAGE = 1..4): rows |kx| <= K of Td: F_y -> N^ ->
+// rhs = prefac*((alpha k^2 - Omega) kpsi + N^), masked (src/gpe.f90:609-669)
+// then the stage update of src/gpe.f90:366-489; kpsi_new --F^-1_y--> Ta.
+// ------------------------------------------------------------------------
+template <typename T, int L, int STAGE>
+__global__ void __launch_bounds__(Geo<T, L>::NT) k_y2_rk4(const cplx<T>* __restrict__ Td, cplx<T>* __restrict__ kpsi,
+                                                       cplx<T>* __restrict__ str1, cplx<T>* __restrict__ str2,
+                                                       cplx<T>* __restrict__ Ta, const cplx<T>* __restrict__ tw,
+                                                       StepConsts c) {
+  typedef Geo<T, L> G;
+  typedef cplx<T> C;
+  extern __shared__ __align__(16) unsigned char smraw[];
+  C* s = reinterpret_cast<C*>(smraw);
+  const int l0 = blockIdx.x * G::R;
+  const int K = c.K, nx = c.nx;
+  const int nrow = 2 * K + 1;
+  for (int e = threadIdx.x; e < G::R * L; e += G::NT) {
+    const int r = e / L, y = e % L;
+    C v = mkc<T>(T(0), T(0));
+    if (l0 + r < nrow) v = Td[(size_t)pruned_row(l0 + r, K, nx) * L + y];
+    s[r * G::LP + pidx(y)] = v;
+  }
+  __syncthreads();
+  fft_rows<T, L, G::R, G::NT, -1>(s, tw);
+  // Stage coefficients with the reference's evaluation order:
+  // dt*oney6, dt*oney6*two, dt*half, dt.
+  const double oney6 = 1.0 / 6.0;
+  const T c2 = T((STAGE == 1 || STAGE == 4) ? c.dt * oney6 : c.dt * oney6 * 2.0);
+  const T c1 = T(STAGE == 3 ? c.dt : c.dt * 0.5);
+  const T pr = T(c.prefac_re), pi_ = T(c.prefac_im);
+  const T al = T(c.alpha), om = T(c.omega);
+  for (int e = threadIdx.x; e < G::R * L; e += G::NT) {
+    const int r = e / L, ky = e % L;
+    if (l0 + r >= nrow) continue;
+    const int kxi = pruned_row(l0 + r, K, nx);
+    const int k1 = kwn(kxi, nx), k2 = kwn(ky, L);
+    const int ksq = k1 * k1 + k2 * k2;
+    const size_t gi = (size_t)kxi * L + ky;
+    C nw = mkc<T>(T(0), T(0));
+    if (ksq <= c.k2max) {
+      const C ps = kpsi[gi];
+      const C nh = s[r * G::LP + pidx(ky)];
+      const T kin = al * T(ksq) - om;
+      const C t = mkc<T>(kin * ps.x + nh.x, kin * ps.y + nh.y);
+      const C rhs = mkc<T>(pr * t.x - pi_ * t.y, pr * t.y + pi_ * t.x);
+      if (STAGE == 1) {
+        str1[gi] = ps;
+        str2[gi] = mkc<T>(c2 * rhs.x, c2 * rhs.y);
+        nw = mkc<T>(ps.x + c1 * rhs.x, ps.y + c1 * rhs.y);
+      } else {
+        const C s1 = str1[gi];
+        C s2 = str2[gi];
+        s2 = mkc<T>(s2.x + c2 * rhs.x, s2.y + c2 * rhs.y);
+        if (STAGE < 4) {
+          str2[gi] = s2;
+          nw = mkc<T>(s1.x + c1 * rhs.x, s1.y + c1 * rhs.y);
+        } else {
+          nw = mkc<T>(s1.x + s2.x, s1.y + s2.y);
+        }
+      }
+    }
+    kpsi[gi] = nw;
+    s[r * G::LP + pidx(ky)] = nw;
+  }
+  __syncthreads();
+  fft_rows<T, L, G::R, G::NT, +1>(s, tw);
+  for (int e = threadIdx.x; e < G::R * L; e += G::NT) {
+    const int r = e % G::R, y = e / G::R;
+    if (l0 + r < nrow) Ta[(size_t)y * nx + pruned_row(l0 + r, K, nx)] = s[r * G::LP + pidx(y)];
+  }
+}
+
+// ------------------------------------------------------------------------
+// Y2 (ARGLE, src/gpe.f90:181-222, no mask): all rows kx of Td: F_y -> N^,
+// kpsi <- (kpsi + dt (N^ + Omega kpsi)) / (1 + alpha k^2 dt);
+// kpsi_new --F^-1_y--> Ta.  RESID: per-CTA FP64 partial sums of
+// |new-old|^2, |old|^2, |new|^2 into part[blockIdx][3].
+// ------------------------------------------------------------------------
+template <typename T, int L, bool RESID>
+__global__ void __launch_bounds__(Geo<T, L>::NT) k_y2_argle(const cplx<T>* __restrict__ Td, cplx<T>* __restrict__ kpsi,
+                                                         cplx<T>* __restrict__ Ta, const cplx<T>* __restrict__ tw,
+                                                         double* __restrict__ part, StepConsts c) {
+  typedef Geo<T, L> G;
+  typedef cplx<T> C;
+  extern __shared__ __align__(16) unsigned char smraw[];
+  C* s = reinterpret_cast<C*>(smraw);
+  static_assert(G::NT <= 512, "reduction buffer");
+  __shared__ double red[3][512];
+  const int x0 = blockIdx.x * G::R;
+  const int nx = c.nx;
+  for (int e = threadIdx.x; e < G::R * L; e += G::NT) {
+    const int r = e / L, y = e % L;
+    s[r * G::LP + pidx(y)] = Td[(size_t)(x0 + r) * L + y];
+  }
+  __syncthreads();
+  fft_rows<T, L, G::R, G::NT, -1>(s, tw);
+  const T al = T(c.alpha), om = T(c.omega), dt = T(c.dt);
+  double dsum = 0.0, osum = 0.0, nsum = 0.0;
+  for (int e = threadIdx.x; e < G::R * L; e += G::NT) {
+    const int r = e / L, ky = e % L;
+    const int k1 = kwn(x0 + r, nx), k2 = kwn(ky, L);
+    const size_t gi = (size_t)(x0 + r) * L + ky;
+    const C old = kpsi[gi];
+    const C nh = s[r * G::LP + pidx(ky)];
+    const C t1 = mkc<T>(nh.x + om * old.x, nh.y + om * old.y);
+    const T t2 = T(1) + al * T(k1 * k1 + k2 * k2) * dt;
+    C nw = mkc<T>(old.x + dt * t1.x, old.y + dt * t1.y);
+    nw.x = nw.x / t2;
+    nw.y = nw.y / t2;
+    kpsi[gi] = nw;
+    s[r * G::LP + pidx(ky)] = nw;
+    if (RESID) {
+      const double dx = (double)nw.x - (double)old.x, dy = (double)nw.y - (double)old.y;
+      dsum += dx * dx + dy * dy;
+      osum += (double)old.x * old.x + (double)old.y * old.y;
+      nsum += (double)nw.x * nw.x + (double)nw.y * nw.y;
+    }
+  }
+  if (RESID) {
+    red[0][threadIdx.x] = dsum;
+    red[1][threadIdx.x] = osum;
+    red[2][threadIdx.x] = nsum;
+  }
+  __syncthreads();
+  if (RESID && threadIdx.x == 0) {  // fixed order: deterministic
+    double a = 0, b = 0, d = 0;
+    for (int t = 0; t < G::NT; ++t) { a += red[0][t]; b += red[1][t]; d += red[2][t]; }
+    part[blockIdx.x * 3 + 0] = a;
+    part[blockIdx.x * 3 + 1] = b;
+    part[blockIdx.x * 3 + 2] = d;
+  }
+  fft_rows<T, L, G::R, G::NT, +1>(s, tw);
+  for (int e = threadIdx.x; e < G::R * L; e += G::NT) {
+    const int r = e % G::R, y = e / G::R;
+    Ta[(size_t)y * nx + x0 + r] = s[r * G::LP + pidx(y)];
+  }
+}
+
+// Sum per-CTA partials in a fixed order (deterministic) into out[0..2].
+__global__ void k_reduce_partials3(const double* __restrict__ part, int nblk, double* __restrict__ out);
+
+}  // namespace vk

@@ -1,0 +1,39 @@
+// vk_solver.h -- host-side solver interface behind the C ABI.
+#pragma once
+#include <string>
+#include <cstdint>
+#include "../../include/vk.h"
+
+namespace vk {
+
+// Thread-local error message used by vk_last_error().
+void set_error(const std::string& msg);
+
+class SolverBase {
+ public:
+  virtual ~SolverBase() {}
+  virtual int set_psi(const double* psi) = 0;
+  virtual int set_kpsi(const double* kpsi) = 0;
+  virtual int get_psi(double* psi) = 0;
+  virtual int get_kpsi(double* kpsi) = 0;
+  virtual int rk4(int nsteps) = 0;
+  virtual int argle(int nsteps, double* residual) = 0;
+  virtual int diagnostics(double* scalars, double* spec, int32_t* nvort) = 0;
+  virtual int particles_set(const double* pos, const double* vel, const double* f0ext) = 0;
+  virtual int particles_get(double* pos, double* vel, double* frc) = 0;
+  virtual void* stream() = 0;
+  virtual int64_t launches() const = 0;
+  virtual int timing_begin() = 0;
+  virtual int timing_end(int cap, char* tags, double* ms, int64_t* counts, int* ntags) = 0;
+};
+
+// Factories (one per precision, each in its own translation unit).
+SolverBase* make_solver_f64(const vk_params& p, int* status);
+SolverBase* make_solver_f32(const vk_params& p, int* status);
+
+// Host helpers shared by both precisions (vk_host.cpp).
+void twiddle_table(int n, double* out_interleaved);      // exp(-2 pi i k/n), k < n
+int k2max_for(int nx);                                     // largest k1^2+k2^2 kept by the 2/3 rule
+int kmax_for(int k2max);                                   // largest |k| with k^2 <= k2max
+
+}  // namespace vk

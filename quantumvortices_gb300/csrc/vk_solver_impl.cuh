@@ -1,0 +1,504 @@
+// vk_solver_impl.cuh -- Solver<T>: device state and launch sequences.
+// Included once per precision (vk_f64.cu, vk_f32.cu).
+#pragma once
+#include <cuda_runtime.h>
+#include <cmath>
+#include <cstring>
+#include <mutex>
+#include <string>
+#include <type_traits>
+#include <unordered_set>
+#include <vector>
+#include "vk_kernels.cuh"
+#include "vk_diag.cuh"
+#include "vk_solver.h"
+
+namespace vk {
+
+#define VK_CUDA_TRY(expr)                                                              \
+  do {                                                                                 \
+    cudaError_t e_ = (expr);                                                           \
+    if (e_ != cudaSuccess) {                                                           \
+      set_error(std::string(#expr) + ": " + cudaGetErrorString(e_));                   \
+      return VK_E_CUDA;                                                                \
+    }                                                                                  \
+  } while (0)
+
+template <int L> using LC = std::integral_constant<int, L>;
+
+// Calls f(LC<n>()) for a supported row length n.
+template <typename F> bool with_len(int n, F&& f) {
+  switch (n) {
+    case 16: f(LC<16>()); return true;
+    case 32: f(LC<32>()); return true;
+    case 64: f(LC<64>()); return true;
+    case 128: f(LC<128>()); return true;
+    case 256: f(LC<256>()); return true;
+    case 512: f(LC<512>()); return true;
+    case 1024: f(LC<1024>()); return true;
+    case 2048: f(LC<2048>()); return true;
+    case 4096: f(LC<4096>()); return true;
+    default: return false;
+  }
+}
+
+inline void ensure_smem_attr(const void* fn, size_t bytes) {
+  static std::mutex mu;
+  static std::unordered_set<const void*> done;
+  if (bytes <= 48 * 1024) return;
+  std::lock_guard<std::mutex> g(mu);
+  if (done.count(fn)) return;
+  cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+  done.insert(fn);
+}
+
+template <typename T> __global__ void k_from_f64(const double2* __restrict__ in, cplx<T>* __restrict__ out, size_t n) {
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
+    out[i] = mkc<T>(T(in[i].x), T(in[i].y));
+}
+template <typename T> __global__ void k_to_f64(const cplx<T>* __restrict__ in, double2* __restrict__ out, size_t n) {
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
+    out[i] = make_double2((double)in[i].x, (double)in[i].y);
+}
+template <typename T> __global__ void k_scale_two(cplx<T>* __restrict__ a, cplx<T>* __restrict__ b, size_t n,
+                                                  const double* __restrict__ sums, double factor_num) {
+  // renormalisation: s = sqrt(Nparticle / norm), norm = factor * sum|kpsi|^2
+  const double s = sqrt(factor_num / sums[2]);
+  const T st = T(s);
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+    a[i] = cscale(a[i], st);
+    b[i] = cscale(b[i], st);
+  }
+}
+
+enum TaState { TA_INVALID = 0, TA_PRUNED = 1, TA_FULL = 2 };
+
+template <typename T>
+class Solver : public SolverBase {
+  typedef cplx<T> C;
+
+ public:
+  explicit Solver(const vk_params& p) : p_(p) {}
+  ~Solver() override { release(); }
+
+  int init() {
+    nx_ = p_.nx;
+    ny_ = p_.ny;
+    n2_ = (size_t)nx_ * ny_;
+    k2max_ = k2max_for(nx_);
+    K_ = kmax_for(k2max_);
+    if (K_ >= nx_ / 2 || K_ >= ny_ / 2) {
+      set_error("grid too small for the 2/3 rule");
+      return VK_E_INVALID;
+    }
+    pk_ = (K_ + 2) & ~1;
+    nshell_ = vk_nshell(nx_);
+    VK_CUDA_TRY(cudaStreamCreateWithFlags(&st_, cudaStreamNonBlocking));
+    const size_t fb = n2_ * sizeof(C);
+    VK_CUDA_TRY(cudaMalloc(&psi_, fb));
+    VK_CUDA_TRY(cudaMalloc(&kpsi_, fb));
+    VK_CUDA_TRY(cudaMalloc(&str1_, fb));
+    VK_CUDA_TRY(cudaMalloc(&str2_, fb));
+    VK_CUDA_TRY(cudaMalloc(&Ta_, fb));
+    VK_CUDA_TRY(cudaMalloc(&Td_, fb));
+    VK_CUDA_TRY(cudaMalloc(&Tb_, sizeof(C) * (size_t)(K_ + 1) * ny_));
+    VK_CUDA_TRY(cudaMalloc(&Tc_, sizeof(C) * (size_t)ny_ * pk_));
+    VK_CUDA_TRY(cudaMalloc(&stage64_, n2_ * sizeof(double2)));
+    VK_CUDA_TRY(cudaMemsetAsync(psi_, 0, fb, st_));
+    VK_CUDA_TRY(cudaMemsetAsync(kpsi_, 0, fb, st_));
+    VK_CUDA_TRY(cudaMemsetAsync(str1_, 0, fb, st_));
+    VK_CUDA_TRY(cudaMemsetAsync(str2_, 0, fb, st_));
+    VK_CUDA_TRY(cudaMemsetAsync(Ta_, 0, fb, st_));
+    VK_CUDA_TRY(cudaMemsetAsync(Td_, 0, fb, st_));
+    VK_CUDA_TRY(cudaMemsetAsync(Tb_, 0, sizeof(C) * (size_t)(K_ + 1) * ny_, st_));
+    VK_CUDA_TRY(cudaMemsetAsync(Tc_, 0, sizeof(C) * (size_t)ny_ * pk_, st_));
+    const int maxblk = std::max(nx_, ny_);
+    VK_CUDA_TRY(cudaMalloc(&part_, sizeof(double) * 3 * (size_t)maxblk));
+    VK_CUDA_TRY(cudaMalloc(&sums_, sizeof(double) * 8));
+    // twiddle tables
+    int trc = upload_twiddles(nx_, &twx_);
+    if (trc) return trc;
+    if (ny_ == nx_) twy_ = twx_;
+    else if ((trc = upload_twiddles(ny_, &twy_))) return trc;
+    c_.nx = nx_;
+    c_.ny = ny_;
+    c_.K = K_;
+    c_.k2max = k2max_;
+    c_.pk = pk_;
+    c_.alpha = p_.alpha;
+    c_.g = p_.gstrength;
+    c_.omega = p_.omega_chem;
+    c_.dt = p_.dt;
+    // prefacrhs = (one - zi*disp_factor)/zi = (-disp_factor, -1)  (src/gpe.f90:529)
+    c_.prefac_re = -p_.disp_factor;
+    c_.prefac_im = -1.0;
+    c_.scale = 1.0 / ((double)nx_ * (double)ny_);
+    VK_CUDA_TRY(cudaStreamSynchronize(st_));
+    return VK_OK;
+  }
+
+  void* stream() override { return (void*)st_; }
+  int64_t launches() const override { return launches_; }
+
+  // ---------------------------------------------------------------- I/O --
+  int set_psi(const double* psi) override {
+    int rc = upload(psi, psi_);
+    if (rc) return rc;
+    fwd2d(psi_, kpsi_, p_.otoc != 0);
+    if (p_.otoc) {
+      inv2d(kpsi_, psi_, true);
+      kpsi_masked_ = true;
+      ta_ = TA_FULL;
+    } else {
+      kpsi_masked_ = false;
+      ta_ = TA_INVALID;
+    }
+    have_psi_ = true;
+    return sync_check();
+  }
+  int set_kpsi(const double* kpsi) override {
+    int rc = upload(kpsi, kpsi_);
+    if (rc) return rc;
+    inv2d(kpsi_, psi_, false);
+    kpsi_masked_ = false;
+    ta_ = TA_FULL;
+    have_psi_ = true;
+    return sync_check();
+  }
+  int get_psi(double* out) override { return download(psi_, out); }
+  int get_kpsi(double* out) override { return download(kpsi_, out); }
+
+  // ---------------------------------------------------------------- RK4 --
+  int rk4(int nsteps) override {
+    if (!have_psi_) { set_error("vk_gpe_rk4: no psi set"); return VK_E_STATE; }
+    if (nsteps <= 0) return VK_OK;
+    if (!kpsi_masked_) {
+      launch_simple("k_mask_four", k_mask_four<T>, kpsi_, nx_, ny_, k2max_);
+      kpsi_masked_ = true;
+    }
+    for (int s = 0; s < nsteps; ++s) {
+      for (int stage = 1; stage <= 4; ++stage) {
+        const bool from_psi = (s == 0 && stage == 1);
+        x1(from_psi ? 0 : 1, true);
+        y1();
+        x2(+1, true);
+        y2_rk4(stage);
+      }
+    }
+    xinv_from_ta(true);
+    ta_ = TA_PRUNED;
+    return check_launch();
+  }
+
+  // -------------------------------------------------------------- ARGLE --
+  int argle(int nsteps, double* residual) override {
+    if (!have_psi_) { set_error("vk_argle: no psi set"); return VK_E_STATE; }
+    if (nsteps <= 0) return VK_OK;
+    if (ta_ != TA_FULL) yinv_to_ta();
+    const int nblk = nx_ / geo_rows(ny_);
+    for (int s = 0; s < nsteps; ++s) {
+      const bool last = (s == nsteps - 1);
+      const bool resid = last || p_.argle_renorm;
+      x1(1, false);
+      y1();
+      x2(-1, false);
+      y2_argle(resid);
+      if (resid) launch_raw("k_reduce_partials3", k_reduce_partials3, 1, 256, 0, (const double*)part_, nblk, sums_);
+      if (p_.argle_renorm) {
+        // norm = dvol * (1/(nx ny)) * sum |kpsi|^2; target Nparticle = Lx*Ly
+        const double two_pi = 6.283185307179586476925286766559;
+        const double dvol = (two_pi / nx_) * (two_pi / ny_);
+        const double area = two_pi * two_pi;
+        launch_raw("k_scale_two", k_scale_two<T>, 1024, 256, 0, kpsi_, Ta_, n2_, (const double*)sums_, area / (dvol * c_.scale));
+      }
+    }
+    ta_ = TA_FULL;
+    kpsi_masked_ = false;
+    int rc = check_launch();
+    if (rc) return rc;
+    if (residual) {
+      double h[3];
+      VK_CUDA_TRY(cudaMemcpyAsync(h, sums_, sizeof(h), cudaMemcpyDeviceToHost, st_));
+      VK_CUDA_TRY(cudaStreamSynchronize(st_));
+      *residual = std::sqrt(h[0]) / (p_.dt * std::sqrt(h[1]));
+    }
+    return VK_OK;
+  }
+
+  int diagnostics(double* scalars, double* spec, int32_t* nvort) override {
+    if (!have_psi_) { set_error("vk_diagnostics: no psi set"); return VK_E_STATE; }
+    return diag_.run(*this, scalars, spec, nvort);
+  }
+
+  int particles_set(const double*, const double*, const double*) override {
+    set_error("particles: not built in this configuration");
+    return VK_E_INVALID;
+  }
+  int particles_get(double*, double*, double*) override {
+    set_error("particles: not built in this configuration");
+    return VK_E_INVALID;
+  }
+
+  // ------------------------------------------------- launch helpers --
+  template <typename... KA, typename... A>
+  void launch_raw(const char* tag, void (*kern)(KA...), int grid, int block, size_t smem, A... args) {
+    ensure_smem_attr((const void*)kern, smem);
+    if (timing_ && ev_used_ == 0) record_event(nullptr);
+    kern<<<grid, block, smem, st_>>>(args...);
+    ++launches_;
+    if (timing_) record_event(tag);
+  }
+  template <typename... KA, typename... A>
+  void launch_simple(const char* tag, void (*kern)(KA...), A... args) {
+    const int grid = (int)std::min<size_t>((n2_ + 255) / 256, 152 * 16);
+    launch_raw(tag, kern, grid, 256, 0, args...);
+  }
+
+  // ------------------------------------------------------ timing --
+  void record_event(const char* tag) {
+    if (ev_used_ >= (int)ev_.size()) {
+      cudaEvent_t e;
+      if (cudaEventCreate(&e) != cudaSuccess) return;
+      ev_.push_back(e);
+      ev_tag_.push_back(nullptr);
+    }
+    cudaEventRecord(ev_[ev_used_], st_);
+    ev_tag_[ev_used_] = tag;
+    ++ev_used_;
+  }
+  int timing_begin() override {
+    timing_ = true;
+    ev_used_ = 0;
+    return VK_OK;
+  }
+  int timing_end(int cap, char* tags, double* ms, int64_t* counts, int* ntags) override {
+    timing_ = false;
+    VK_CUDA_TRY(cudaStreamSynchronize(st_));
+    std::vector<std::string> names;
+    std::vector<double> tot;
+    std::vector<int64_t> cnt;
+    for (int i = 1; i < ev_used_; ++i) {
+      float t = 0.f;
+      VK_CUDA_TRY(cudaEventElapsedTime(&t, ev_[i - 1], ev_[i]));
+      const std::string nm = ev_tag_[i] ? ev_tag_[i] : "?";
+      size_t j = 0;
+      while (j < names.size() && names[j] != nm) ++j;
+      if (j == names.size()) { names.push_back(nm); tot.push_back(0.0); cnt.push_back(0); }
+      tot[j] += t;
+      cnt[j] += 1;
+    }
+    const int n = (int)std::min<size_t>(names.size(), (size_t)std::max(cap, 0));
+    for (int j = 0; j < n; ++j) {
+      std::memset(tags + 24 * j, 0, 24);
+      std::strncpy(tags + 24 * j, names[j].c_str(), 23);
+      ms[j] = tot[j];
+      counts[j] = cnt[j];
+    }
+    *ntags = (int)names.size();
+    ev_used_ = 0;
+    return VK_OK;
+  }
+  static int geo_rows(int L) {
+    int r = 0;
+    with_len(L, [&](auto lc) { r = Geo<T, decltype(lc)::value>::R; });
+    return r;
+  }
+
+  // Forward 2D FFT phys[y][x] -> four[kx][ky] (Td as the transposed scratch).
+  void fwd2d(const C* phys, C* four, bool otoc) {
+    with_len(nx_, [&](auto lc) {
+      constexpr int L = decltype(lc)::value;
+      typedef Geo<T, L> G;
+      launch_raw("k_xfwd", k_xfwd<T, L>, ny_ / G::R, G::NT, sizeof(C) * G::R * G::LP, phys, Td_, (const C*)twx_, ny_);
+    });
+    with_len(ny_, [&](auto lc) {
+      constexpr int L = decltype(lc)::value;
+      typedef Geo<T, L> G;
+      if (otoc)
+        launch_raw("k_yfwd", k_yfwd<T, L, true>, nx_ / G::R, G::NT, sizeof(C) * G::R * G::LP, (const C*)Td_, four,
+                   (const C*)twy_, nx_, k2max_, p_.k_otoc_gp, p_.eps_otoc_gp);
+      else
+        launch_raw("k_yfwd", k_yfwd<T, L, false>, nx_ / G::R, G::NT, sizeof(C) * G::R * G::LP, (const C*)Td_, four,
+                   (const C*)twy_, nx_, k2max_, 0.0, 0.0);
+    });
+  }
+  // Inverse 2D FFT four[kx][ky] -> phys[y][x] (scaled), through Ta.
+  void inv2d(const C* four, C* phys, bool prune) {
+    with_len(ny_, [&](auto lc) {
+      constexpr int L = decltype(lc)::value;
+      typedef Geo<T, L> G;
+      launch_raw("k_yinv", k_yinv<T, L>, nx_ / G::R, G::NT, sizeof(C) * G::R * G::LP, four, Ta_, (const C*)twy_, nx_);
+    });
+    with_len(nx_, [&](auto lc) {
+      constexpr int L = decltype(lc)::value;
+      typedef Geo<T, L> G;
+      if (prune)
+        launch_raw("k_xinv", k_xinv<T, L, true>, ny_ / G::R, G::NT, sizeof(C) * G::R * G::LP, (const C*)Ta_, phys,
+                   (const C*)twx_, T(c_.scale), K_);
+      else
+        launch_raw("k_xinv", k_xinv<T, L, false>, ny_ / G::R, G::NT, sizeof(C) * G::R * G::LP, (const C*)Ta_, phys,
+                   (const C*)twx_, T(c_.scale), K_);
+    });
+  }
+  void yinv_to_ta() {
+    with_len(ny_, [&](auto lc) {
+      constexpr int L = decltype(lc)::value;
+      typedef Geo<T, L> G;
+      launch_raw("k_yinv", k_yinv<T, L>, nx_ / G::R, G::NT, sizeof(C) * G::R * G::LP, (const C*)kpsi_, Ta_, (const C*)twy_, nx_);
+    });
+  }
+  void xinv_from_ta(bool prune) {
+    with_len(nx_, [&](auto lc) {
+      constexpr int L = decltype(lc)::value;
+      typedef Geo<T, L> G;
+      if (prune)
+        launch_raw("k_xinv", k_xinv<T, L, true>, ny_ / G::R, G::NT, sizeof(C) * G::R * G::LP, (const C*)Ta_, psi_,
+                   (const C*)twx_, T(c_.scale), K_);
+      else
+        launch_raw("k_xinv", k_xinv<T, L, false>, ny_ / G::R, G::NT, sizeof(C) * G::R * G::LP, (const C*)Ta_, psi_,
+                   (const C*)twx_, T(c_.scale), K_);
+    });
+  }
+  void x1(int from_t, bool prune) {
+    with_len(nx_, [&](auto lc) {
+      constexpr int L = decltype(lc)::value;
+      typedef Geo<T, L> G;
+      const size_t sm = sizeof(C) * G::R * G::LP;
+      if (!from_t) launch_raw("k_x1", k_x1<T, L, false, false>, ny_ / G::R, G::NT, sm, (const C*)Ta_, psi_, Tb_, (const C*)twx_, c_);
+      else if (prune) launch_raw("k_x1", k_x1<T, L, true, true>, ny_ / G::R, G::NT, sm, (const C*)Ta_, psi_, Tb_, (const C*)twx_, c_);
+      else launch_raw("k_x1", k_x1<T, L, true, false>, ny_ / G::R, G::NT, sm, (const C*)Ta_, psi_, Tb_, (const C*)twx_, c_);
+    });
+  }
+  void y1() {
+    with_len(ny_, [&](auto lc) {
+      constexpr int L = decltype(lc)::value;
+      typedef Geo<T, L> G;
+      launch_raw("k_y1", k_y1<T, L>, (K_ + 1 + G::R - 1) / G::R, G::NT, sizeof(C) * G::R * G::LP, (const C*)Tb_, Tc_,
+                 (const C*)twy_, c_);
+    });
+  }
+  void x2(int sign, bool prune_out) {
+    with_len(nx_, [&](auto lc) {
+      constexpr int L = decltype(lc)::value;
+      typedef Geo<T, L> G;
+      const size_t sm = sizeof(C) * G::R * G::LP;
+      const T* vp = vpot_;
+      if (sign > 0) {
+        if (vp) launch_raw("k_x2", k_x2<T, L, +1, true, true>, ny_ / G::R, G::NT, sm, (const C*)Tc_, (const C*)psi_, vp, Td_, (const C*)twx_, c_);
+        else launch_raw("k_x2", k_x2<T, L, +1, true, false>, ny_ / G::R, G::NT, sm, (const C*)Tc_, (const C*)psi_, vp, Td_, (const C*)twx_, c_);
+      } else {
+        if (vp) launch_raw("k_x2", k_x2<T, L, -1, false, true>, ny_ / G::R, G::NT, sm, (const C*)Tc_, (const C*)psi_, vp, Td_, (const C*)twx_, c_);
+        else launch_raw("k_x2", k_x2<T, L, -1, false, false>, ny_ / G::R, G::NT, sm, (const C*)Tc_, (const C*)psi_, vp, Td_, (const C*)twx_, c_);
+      }
+      (void)prune_out;
+    });
+  }
+  void y2_rk4(int stage) {
+    with_len(ny_, [&](auto lc) {
+      constexpr int L = decltype(lc)::value;
+      typedef Geo<T, L> G;
+      const int grid = (2 * K_ + 1 + G::R - 1) / G::R;
+      const size_t sm = sizeof(C) * G::R * G::LP;
+      switch (stage) {
+        case 1: launch_raw("k_y2_rk4", k_y2_rk4<T, L, 1>, grid, G::NT, sm, (const C*)Td_, kpsi_, str1_, str2_, Ta_, (const C*)twy_, c_); break;
+        case 2: launch_raw("k_y2_rk4", k_y2_rk4<T, L, 2>, grid, G::NT, sm, (const C*)Td_, kpsi_, str1_, str2_, Ta_, (const C*)twy_, c_); break;
+        case 3: launch_raw("k_y2_rk4", k_y2_rk4<T, L, 3>, grid, G::NT, sm, (const C*)Td_, kpsi_, str1_, str2_, Ta_, (const C*)twy_, c_); break;
+        default: launch_raw("k_y2_rk4", k_y2_rk4<T, L, 4>, grid, G::NT, sm, (const C*)Td_, kpsi_, str1_, str2_, Ta_, (const C*)twy_, c_); break;
+      }
+    });
+  }
+  void y2_argle(bool resid) {
+    with_len(ny_, [&](auto lc) {
+      constexpr int L = decltype(lc)::value;
+      typedef Geo<T, L> G;
+      const size_t sm = sizeof(C) * G::R * G::LP;
+      if (resid) launch_raw("k_y2_argle", k_y2_argle<T, L, true>, nx_ / G::R, G::NT, sm, (const C*)Td_, kpsi_, Ta_, (const C*)twy_, part_, c_);
+      else launch_raw("k_y2_argle", k_y2_argle<T, L, false>, nx_ / G::R, G::NT, sm, (const C*)Td_, kpsi_, Ta_, (const C*)twy_, part_, c_);
+    });
+  }
+
+  int check_launch() {
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) {
+      set_error(std::string("kernel launch: ") + cudaGetErrorString(e));
+      return VK_E_CUDA;
+    }
+    return VK_OK;
+  }
+  int sync_check() {
+    int rc = check_launch();
+    if (rc) return rc;
+    VK_CUDA_TRY(cudaStreamSynchronize(st_));
+    return VK_OK;
+  }
+
+  int upload(const double* host, C* dev) {
+    if (std::is_same<T, double>::value) {
+      VK_CUDA_TRY(cudaMemcpyAsync(dev, host, n2_ * sizeof(double2), cudaMemcpyHostToDevice, st_));
+    } else {
+      VK_CUDA_TRY(cudaMemcpyAsync(stage64_, host, n2_ * sizeof(double2), cudaMemcpyHostToDevice, st_));
+      launch_simple("k_from_f64", k_from_f64<T>, (const double2*)stage64_, dev, n2_);
+    }
+    return check_launch();
+  }
+  int download(const C* dev, double* host) {
+    if (std::is_same<T, double>::value) {
+      VK_CUDA_TRY(cudaMemcpyAsync(host, dev, n2_ * sizeof(double2), cudaMemcpyDeviceToHost, st_));
+    } else {
+      launch_simple("k_to_f64", k_to_f64<T>, dev, (double2*)stage64_, n2_);
+      VK_CUDA_TRY(cudaMemcpyAsync(host, stage64_, n2_ * sizeof(double2), cudaMemcpyDeviceToHost, st_));
+    }
+    return sync_check();
+  }
+
+  int upload_twiddles(int n, C** dst) {
+    std::vector<double> h(2 * (size_t)n);
+    twiddle_table(n, h.data());
+    std::vector<C> t(n);
+    for (int k = 0; k < n; ++k) { t[k].x = T(h[2 * k]); t[k].y = T(h[2 * k + 1]); }
+    VK_CUDA_TRY(cudaMalloc(dst, sizeof(C) * n));
+    VK_CUDA_TRY(cudaMemcpy(*dst, t.data(), sizeof(C) * n, cudaMemcpyHostToDevice));
+    return VK_OK;
+  }
+
+  void release() {
+    diag_.release();
+    for (auto e : ev_) cudaEventDestroy(e);
+    ev_.clear();
+    if (twy_ && twy_ != twx_) cudaFree(twy_);
+    C* bufs[] = {psi_, kpsi_, str1_, str2_, Ta_, Td_, Tb_, Tc_, twx_};
+    for (C* b : bufs)
+      if (b) cudaFree(b);
+    if (vpot_) cudaFree(vpot_);
+    if (stage64_) cudaFree(stage64_);
+    if (part_) cudaFree(part_);
+    if (sums_) cudaFree(sums_);
+    if (st_) cudaStreamDestroy(st_);
+    psi_ = kpsi_ = str1_ = str2_ = Ta_ = Td_ = Tb_ = Tc_ = twx_ = twy_ = nullptr;
+    st_ = nullptr;
+  }
+
+  // state (public for the diagnostics helper)
+  vk_params p_;
+  int nx_ = 0, ny_ = 0, K_ = 0, k2max_ = 0, pk_ = 0, nshell_ = 0;
+  size_t n2_ = 0;
+  cudaStream_t st_ = nullptr;
+  C *psi_ = nullptr, *kpsi_ = nullptr, *str1_ = nullptr, *str2_ = nullptr;
+  C *Ta_ = nullptr, *Tb_ = nullptr, *Tc_ = nullptr, *Td_ = nullptr;
+  C *twx_ = nullptr, *twy_ = nullptr;
+  T* vpot_ = nullptr;
+  void* stage64_ = nullptr;
+  double* part_ = nullptr;
+  double* sums_ = nullptr;
+  StepConsts c_{};
+  bool kpsi_masked_ = false, have_psi_ = false;
+  int ta_ = TA_INVALID;
+  int64_t launches_ = 0;
+  bool timing_ = false;
+  int ev_used_ = 0;
+  std::vector<cudaEvent_t> ev_;
+  std::vector<const char*> ev_tag_;
+  Diagnostics<T> diag_;
+};
+
+}  // namespace vk

@@ -1,0 +1,155 @@
+"""GPU path (libvk kernels through the C ABI) against the CPU FP64 oracle.
+
+Tolerances: FP64 path psi / kpsi relative L2 <= 1e-12 after 100 RK4 steps
+(the stated parity bar); FFT round trips <= 1e-13; the FP32 bulk path
+<= 1e-5 relative L2 against the FP64 oracle after 100 steps.
+"""
+import numpy as np
+import pytest
+
+from oracle.oracle import Oracle
+from quantumvortices_gb300 import vk
+
+pytestmark = pytest.mark.gpu
+
+
+def rel(a, b):
+    return float(np.linalg.norm(a - b) / np.linalg.norm(b))
+
+
+def _pair(n, ny=None, dt=1e-3, prec=vk.VK_PREC_FP64, otoc=True, nv=8, seed=1):
+    ny = ny or n
+    p = vk.params_for(n, ny, dt=dt, precision=prec, otoc=otoc)
+    psi0, _ = vk.ic_vortices(n, ny, nv, seed=seed)
+    s = vk.GPESolver(p)
+    s.set_psi(psi0)
+    o = Oracle.from_vk_params(p)
+    o.set_psi(psi0, otoc=otoc, k_otoc=p.k_otoc_gp, eps_otoc=p.eps_otoc_gp)
+    return s, o, psi0
+
+
+@pytest.mark.parametrize("nx,ny", [(16, 16), (32, 32), (64, 64), (128, 128), (256, 256), (512, 512),
+                                   (1024, 1024), (2048, 2048), (64, 32), (32, 128)])
+def test_forward_fft_and_state_upload(nx, ny):
+    s, o, psi0 = _pair(nx, ny, otoc=False, nv=4)
+    assert rel(s.get_kpsi(), o.get_kpsi()) < 1e-13
+    assert np.array_equal(s.get_psi(), psi0)
+    s.close()
+
+
+@pytest.mark.parametrize("n", [64, 4096])
+def test_otoc_band_limit(n):
+    s, o, _ = _pair(n, nv=8)
+    assert rel(s.get_psi(), o.get_psi()) < 1e-13
+    assert rel(s.get_kpsi(), o.get_kpsi()) < 1e-13
+    s.close()
+
+
+@pytest.mark.parametrize("n,steps", [(128, 100), (256, 50)])
+def test_rk4_parity_fp64(n, steps):
+    s, o, _ = _pair(n, nv=8)
+    s.gpe_rk4(steps)
+    o.gpe_rk4(steps)
+    assert rel(s.get_psi(), o.get_psi()) < 1e-12
+    assert rel(s.get_kpsi(), o.get_kpsi()) < 1e-12
+    s.close()
+
+
+def test_rk4_parity_fp64_1024():
+    s, o, _ = _pair(1024, dt=5e-4, nv=64, seed=11)
+    s.gpe_rk4(100)
+    o.gpe_rk4(100)
+    assert rel(s.get_psi(), o.get_psi()) < 1e-12
+    s.close()
+
+
+def test_rk4_without_otoc_uses_raw_psi_first_stage():
+    s, o, _ = _pair(64, otoc=False, nv=4)
+    s.gpe_rk4(10)
+    o.gpe_rk4(10)
+    assert rel(s.get_psi(), o.get_psi()) < 1e-12
+    s.close()
+
+
+def test_rk4_split_calls_equal_one_call():
+    a, _, psi0 = _pair(128, nv=8)
+    b, _, _ = _pair(128, nv=8)
+    a.gpe_rk4(5)
+    b.gpe_rk4(3)
+    b.gpe_rk4(2)
+    assert rel(a.get_psi(), b.get_psi()) < 1e-15
+    a.close()
+    b.close()
+
+
+def test_rk4_nonsquare():
+    s, o, _ = _pair(64, 128, nv=6)
+    s.gpe_rk4(20)
+    o.gpe_rk4(20)
+    assert rel(s.get_psi(), o.get_psi()) < 1e-12
+    s.close()
+
+
+def test_argle_parity_and_residual():
+    s, o, _ = _pair(128, nv=8)
+    r_gpu = s.argle(100)
+    r_ref = o.argle(100)
+    assert rel(s.get_kpsi(), o.get_kpsi()) < 1e-12
+    assert rel(s.get_psi(), o.get_psi()) < 1e-12  # psi is the stale start-of-step field
+    assert abs(r_gpu - r_ref) / r_ref < 1e-9
+    s.close()
+
+
+def test_argle_then_rk4():
+    s, o, _ = _pair(128, nv=8, otoc=False)
+    s.argle(30)
+    o.argle(30)
+    s.gpe_rk4(30)
+    o.gpe_rk4(30)
+    assert rel(s.get_psi(), o.get_psi()) < 1e-12
+    s.close()
+
+
+def test_set_kpsi_path():
+    n = 64
+    p = vk.params_for(n)
+    rng = np.random.default_rng(2)
+    k = rng.standard_normal((n, n)) + 1j * rng.standard_normal((n, n))
+    s = vk.GPESolver(p)
+    s.set_kpsi(k)
+    o = Oracle.from_vk_params(p)
+    assert rel(s.get_psi(), o.fft_inverse(k)) < 1e-13
+    s.close()
+
+
+def test_fp32_bulk_error_vs_fp64_oracle():
+    s, o, _ = _pair(128, nv=8, prec=vk.VK_PREC_FP32)
+    s.gpe_rk4(100)
+    o.gpe_rk4(100)
+    err = rel(s.get_psi(), o.get_psi())
+    assert err < 1e-5, err
+    s.close()
+
+
+def test_state_errors():
+    p = vk.params_for(32)
+    s = vk.GPESolver(p)
+    with pytest.raises(vk.VkError, match="VK_E_STATE"):
+        s.gpe_rk4(1)
+    bad = np.ones((32, 32), complex)
+    bad[3, 4] = np.nan
+    with pytest.raises(vk.VkError, match="VK_E_NUMERIC"):
+        s.set_psi(bad)
+    s.close()
+
+
+def test_kernel_launch_count_and_timing():
+    s, _, _ = _pair(64, nv=4)
+    n0 = s.launches
+    s.timing_begin()
+    s.gpe_rk4(2)
+    t = s.timing_end()
+    assert s.launches - n0 == 2 * 16 + 1
+    assert {"k_x1", "k_y1", "k_x2", "k_y2_rk4"} <= set(t)
+    assert t["k_x2"][1] == 8
+    s.close()

@@ -1,0 +1,230 @@
+"""The CPU FP64 oracle against independent answers (no GPU).
+
+Parity with the reference binary is unpinned (no Fortran/FFTW here and no
+reference tests), so the oracle is pinned by: numpy's FFT, exact
+known answers of the equation, and an independent numpy restatement of one
+RK4 step, one ARGLE step and the diagnostics.
+"""
+import math
+
+import numpy as np
+import pytest
+
+from oracle.oracle import Oracle
+from quantumvortices_gb300 import vk
+
+
+@pytest.mark.parametrize("nx,ny", [(16, 16), (32, 64), (64, 32), (128, 128), (256, 256)])
+def test_fft_matches_numpy(nx, ny):
+    rng = np.random.default_rng(nx * 7 + ny)
+    o = Oracle(nx, ny)
+    a = rng.standard_normal((ny, nx)) + 1j * rng.standard_normal((ny, nx))
+    f = o.fft_forward(a)
+    ref = np.fft.fft2(a).T  # reference layout kpsi[kx][ky]
+    assert np.abs(f - ref).max() / np.abs(ref).max() < 1e-15
+    back = o.fft_inverse(f)
+    assert np.abs(back - a).max() < 1e-14
+
+
+def test_grid_constants():
+    # nshell = int(1.414*Nx/2.0d0)+1 with a single-precision 1.414 (src/mod_grid.f90:77)
+    for n, want in [(128, 91), (256, 181), (512, 362), (1024, 724), (4096, 2896)]:
+        assert vk.nshell(n) == want
+    from oracle.oracle import lib
+    assert [lib().vko_kwn(8, i) for i in range(1, 9)] == [0, 1, 2, 3, -4, -3, -2, -1]
+
+
+def _grid(n):
+    x = np.arange(n) * 2 * np.pi / n
+    return np.meshgrid(x, x)
+
+
+def _plane_wave_rk4(al, g, om, dt, k2, nsteps):
+    f = lambda a: -1j * (al * k2 - om + g * abs(a) ** 2) * a
+    a = 1.0 + 0j
+    for _ in range(nsteps):
+        k1 = f(a); k2_ = f(a + dt / 2 * k1); k3 = f(a + dt / 2 * k2_); k4 = f(a + dt * k3)
+        a = a + dt / 6 * (k1 + 2 * k2_ + 2 * k3 + k4)
+    return a
+
+
+@pytest.mark.parametrize("k", [(3, -2), (0, 5), (-7, 0)])
+def test_plane_wave_rk4_known_answer(k):
+    """A plane wave keeps |psi|=1 on the grid; RK4 then reduces to the scalar ODE."""
+    n = 32
+    p = vk.params_for(n, dt=1e-3)
+    o = Oracle.from_vk_params(p)
+    X, Y = _grid(n)
+    psi0 = np.exp(1j * (k[0] * X + k[1] * Y))
+    o.set_psi(psi0)
+    o.gpe_rk4(7)
+    a = _plane_wave_rk4(p.alpha, p.gstrength, p.omega_chem, p.dt, k[0] ** 2 + k[1] ** 2, 7)
+    assert np.abs(o.get_psi() - a * psi0).max() < 1e-13
+
+
+def test_uniform_state_stationary():
+    n = 32
+    p = vk.params_for(n, dt=1e-3)
+    o = Oracle.from_vk_params(p)
+    o.set_psi(np.ones((n, n), complex))
+    o.gpe_rk4(5)
+    assert np.abs(o.get_psi() - 1).max() < 1e-14
+    o2 = Oracle.from_vk_params(p)
+    o2.set_psi(np.ones((n, n), complex))
+    r = o2.argle(5)
+    assert np.abs(o2.get_kpsi()[0, 0] - n * n) < 1e-10
+    assert r < 1e-12
+
+
+def test_linear_dispersion_g0():
+    n = 32
+    p = vk.params_for(n, dt=2e-3)
+    o = Oracle(n, n, dt=p.dt, alpha=p.alpha, gstrength=0.0, omega_chem=0.0)
+    X, Y = _grid(n)
+    rng = np.random.default_rng(5)
+    kpsi = np.zeros((n, n), complex)
+    modes = [(1, 2), (-3, 4), (5, -1)]
+    psi0 = np.zeros((n, n), complex)
+    for kx, ky in modes:
+        c = rng.standard_normal() + 1j * rng.standard_normal()
+        psi0 += c * np.exp(1j * (kx * X + ky * Y))
+    o.set_psi(psi0)
+    o.gpe_rk4(4)
+    ref = np.zeros((n, n), complex)
+    f = np.fft.fft2(psi0)
+    kk = np.fft.fftfreq(n, 1.0 / n)
+    KX, KY = np.meshgrid(kk, kk)
+    z = -1j * p.alpha * (KX ** 2 + KY ** 2) * p.dt
+    R = 1 + z + z * z / 2 + z ** 3 / 6 + z ** 4 / 24
+    ref = np.fft.ifft2(f * R ** 4)
+    assert np.abs(o.get_psi() - ref).max() < 1e-13
+
+
+# ---------------------------------------------------------------- numpy restatement
+
+def _np_setup(nx):
+    k = np.array([(i - 1) - nx * (i // (nx // 2 + 1)) for i in range(1, nx + 1)])
+    K1, K2 = np.meshgrid(k, k, indexing="ij")  # [kx][ky]
+    ksq = K1 ** 2 + K2 ** 2
+    mask = ksq.astype(float) >= (nx / 3.0) ** 2
+    return K1, K2, ksq, mask
+
+
+def _F(a):
+    return np.fft.fft2(a).T
+
+
+def _Fi(f):
+    return np.fft.ifft2(f.T)
+
+
+def _np_rhs(psi, kpsi, p, nx):
+    K1, K2, ksq, mask = _np_setup(nx)
+    rho = np.abs(psi) ** 2 + 0j
+    r = _F(rho)
+    tmp1 = (p.alpha * ksq - p.omega_chem) * kpsi
+    r[mask] = 0
+    pg = _Fi(r)
+    nl = _F(p.gstrength * pg * psi)
+    out = (-1j) * (tmp1 + nl)
+    out[mask] = 0
+    return out
+
+
+def _np_rk4(psi, kpsi, p, nx):
+    _, _, _, mask = _np_setup(nx)
+    kpsi = kpsi.copy()
+    kpsi[mask] = 0
+    s1, s2 = kpsi.copy(), np.zeros_like(kpsi)
+    dt = p.dt
+    for c1, c2 in [(dt / 2, dt / 6), (dt / 2, dt / 3), (dt, dt / 3), (None, dt / 6)]:
+        k = _np_rhs(psi, kpsi, p, nx)
+        s2 = s2 + c2 * k
+        kpsi = s1 + c1 * k if c1 is not None else s1 + s2
+        kpsi[mask] = 0
+        psi = _Fi(kpsi)
+    return psi, kpsi
+
+
+def test_rk4_matches_numpy_restatement():
+    n = 32
+    p = vk.params_for(n, dt=1e-3)
+    psi0, _ = vk.ic_vortices(n, n, 4, seed=3)
+    o = Oracle.from_vk_params(p)
+    o.set_psi(psi0, otoc=False)
+    o.gpe_rk4(1)
+    psi, kpsi = _np_rk4(psi0, _F(psi0), p, n)
+    assert np.abs(o.get_psi() - psi).max() < 1e-13
+    assert np.abs(o.get_kpsi() - kpsi).max() / np.abs(kpsi).max() < 1e-13
+
+
+def test_argle_matches_numpy_restatement():
+    n = 32
+    p = vk.params_for(n, dt=1e-3)
+    psi0, _ = vk.ic_vortices(n, n, 4, seed=4)
+    o = Oracle.from_vk_params(p)
+    o.set_psi(psi0, otoc=False)
+    r = o.argle(1)
+    K1, K2, ksq, mask = _np_setup(n)
+    kpsi = _F(psi0)
+    psi = _Fi(kpsi)
+    rh = _F(np.abs(psi) ** 2 + 0j)
+    rh[mask] = 0
+    nl = _F(-p.gstrength * _Fi(rh) * psi)
+    new = (kpsi + p.dt * (nl + p.omega_chem * kpsi)) / (1 + p.alpha * ksq * p.dt)
+    assert np.abs(o.get_kpsi() - new).max() / np.abs(new).max() < 1e-13
+    want = np.linalg.norm(new - kpsi) / (p.dt * np.linalg.norm(kpsi))
+    assert abs(r - want) / want < 1e-10
+
+
+def test_diagnostics_matches_numpy_restatement():
+    n = 32
+    p = vk.params_for(n, dt=1e-3)
+    psi0, _ = vk.ic_vortices(n, n, 4, seed=5)
+    o = Oracle.from_vk_params(p)
+    o.set_psi(psi0, otoc=True)
+    sc, spec = o.diagnostics()
+    psi, kpsi = o.get_psi(), o.get_kpsi()
+    K1, K2, ksq, mask = _np_setup(n)
+    al, g, om = p.alpha, p.gstrength, p.omega_chem
+    dx = 2 * np.pi / n
+    dvol, area = dx * dx, (2 * np.pi) ** 2
+    gx, gy = _Fi(1j * K1 * kpsi), _Fi(1j * K2 * kpsi)
+    momx = 2 * al * np.sum(np.imag(np.conj(psi) * gx)) * dvol / area
+    r = _F(np.abs(psi) ** 2 + 0j)
+    r[mask] = 0
+    pg = _Fi(r)
+    egrad = 2 * al * np.sum(al * (np.abs(gx) ** 2 + np.abs(gy) ** 2)) * dvol / area
+    eintr = 2 * al * np.sum(0.5 * g * np.abs(pg) * np.abs(psi) ** 2) * dvol / area
+    norm = np.sum(np.abs(psi) ** 2) * dvol
+    for got, want in [(sc[0], momx), (sc[2], egrad), (sc[4], eintr), (sc[6], norm)]:
+        assert abs(got - want) <= 1e-12 * max(1.0, abs(want))
+    # spectra
+    sm = float(np.float32(1e-30))
+    wx = np.conj(psi) * gx / (np.abs(psi) + sm)
+    wy = np.conj(psi) * gy / (np.abs(psi) + sm)
+    aa1, aa2 = _F(2 * al * wx.imag + 0j), _F(2 * al * wy.imag + 0j)
+    ee1, ee2 = _F(wx.real + 0j), _F(wy.real + 0j)
+    k2f = ksq.astype(float)
+    with np.errstate(divide="ignore", invalid="ignore"):
+        bb = np.where(ksq == 0, 0, -1j * (K1 / k2f) * aa1 - 1j * (K2 / k2f) * aa2)
+    cc1, cc2 = 1j * K1 * bb, 1j * K2 * bb
+    en = (1.0 / (n * n)) ** 2
+    mshl = np.rint(np.sqrt(k2f)).astype(int)
+    ns = vk.nshell(n)
+    want = np.zeros((6, ns + 1))
+    terms = [0.5 * en * (abs(aa1) ** 2 + abs(aa2) ** 2), 0.5 * en * (abs(aa1 - cc1) ** 2 + abs(aa2 - cc2) ** 2),
+             0.5 * en * (abs(cc1) ** 2 + abs(cc2) ** 2), en * (abs(ee1) ** 2 + abs(ee2) ** 2) * 2 * al * al,
+             en * abs(r) ** 2 * 0.5 * g * 2 * al, en * abs(kpsi) ** 2]
+    for j, t in enumerate(terms):
+        t = np.where(mask, 0, t)
+        np.add.at(want[j], mshl.ravel(), t.ravel())
+    assert np.abs(spec - want).max() <= 1e-12 * np.abs(want).max()
+
+
+def test_vortex_count_of_seeded_state():
+    n = 128
+    psi0, _ = vk.ic_vortices(n, n, 8, seed=1)
+    o = Oracle(n)
+    o.set_psi(psi0, otoc=False)
+    assert o.count_vortices() == (4, 4)
