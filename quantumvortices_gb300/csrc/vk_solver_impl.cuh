@@ -87,7 +87,7 @@ class Solver : public SolverBase {
     n2_ = (size_t)nx_ * ny_;
     k2max_ = k2max_for(nx_);
     K_ = kmax_for(k2max_);
-    if (K_ >= nx_ / 2 || K_ >= ny_ / 2) {
+    if (K_ >= nx_ / 2) {
       set_error("grid too small for the 2/3 rule");
       return VK_E_INVALID;
     }

@@ -143,20 +143,25 @@ def derive_params(nl: VkNamelist, precision: int = VK_PREC_FP64, otoc: bool = Tr
 
 
 def params_for(nx: int, ny: int | None = None, dt: float = 1e-3, precision: int = VK_PREC_FP64,
-               otoc: bool = True, g_is_one: bool = True, n_particles: int = 0, ppotd: float = 2.0,
-               ppotv0: float = 10.0, gp_mass_part: float = 0.0) -> VkParams:
-    """Parameters of i dpsi/dt = -1/2 lap psi + g|psi|^2 psi - mu psi, g = rho0 = mu = 1,
-    in the reference's parametrisation: csound = rho_avg = 1, xi_in = 1/(sqrt(2) dx),
-    which gives alpha = 1/2, g = Omega = 1 (src/driver.f90:362-370)."""
+               otoc: bool = True, xi_in: float = math.sqrt(2.0), n_particles: int = 0, ppotd: float = 2.0,
+               ppotv0: float = 10.0, gp_mass_part: float = 0.0, argle_renorm: bool = False) -> VkParams:
+    """Parameters of the benchmark equation in the reference's parametrisation.
+
+    csound = rho_avg = 1 and xi = xi_in*dx with xi_in = sqrt(2) (healing length
+    sqrt(2)*dx) give alpha = dx and g = Omega = 1/(2 dx) (src/driver.f90:362-370),
+    i.e. i dpsi/dt = -alpha lap psi + g |psi|^2 psi - g psi.  With lengths in
+    units of 2*dx and times in units of 1/g this is i dpsi/dtau = -1/2 lap psi
+    + |psi|^2 psi - psi (g = rho0 = mu = 1), healing length 1/sqrt(2)."""
     ny = ny or nx
     nl = VkNamelist()
     nl.nx, nl.ny, nl.dt_fix = nx, ny, dt
     nl.csound, nl.rho_avg, nl.disp_factor = 1.0, 1.0, 0.0
-    dx = 2.0 * math.pi / nx
-    nl.xi = 1.0 / (math.sqrt(2.0) * dx) if g_is_one else 1.0
+    nl.xi = xi_in
     nl.k_otoc_gp, nl.eps_otoc_gp = 1.8, 1.0e-4
     nl.gp_n_obj, nl.ppotd, nl.ppotv0, nl.gp_mass_part = n_particles, ppotd, ppotv0, gp_mass_part
-    return derive_params(nl, precision, otoc)
+    p = derive_params(nl, precision, otoc)
+    p.argle_renorm = int(argle_renorm)
+    return p
 
 
 def write_wf(path: str, psi: np.ndarray, iopoint: int = 0, time: float = 0.0, dt: float = 0.0) -> None:

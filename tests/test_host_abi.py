@@ -31,10 +31,17 @@ def test_library_exports_every_declared_symbol():
         assert hasattr(lib, n), n
 
 
-def test_params_mapping_g_one():
-    p = vk.params_for(128, dt=1e-3)
-    assert abs(p.alpha - 0.5) < 1e-15 and abs(p.gstrength - 1.0) < 1e-15 and abs(p.omega_chem - 1.0) < 1e-15
-    assert abs(p.xi - 1 / math.sqrt(2)) < 1e-15
+def test_params_mapping():
+    n = 128
+    dx = 2 * math.pi / n
+    p = vk.params_for(n, dt=1e-3)
+    assert abs(p.xi - math.sqrt(2) * dx) < 1e-16
+    assert abs(p.alpha - dx) < 1e-16 and abs(p.gstrength - 1 / (2 * dx)) < 1e-12
+    assert p.omega_chem == p.gstrength
+    # ppotV0 -> V0*g, ppotd -> d*xi (src/driver.f90:391-392)
+    q = vk.params_for(n, n_particles=16, ppotd=2.0, ppotv0=10.0, gp_mass_part=3.0)
+    assert abs(q.ppot_v0 - 10 * q.gstrength) < 1e-12 and abs(q.ppot_d - 2 * q.xi) < 1e-16
+    assert q.n_particles == 16 and q.gp_mass_part == 3.0
 
 
 def test_namelist_parsing(tmp_path):
