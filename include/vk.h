@@ -143,6 +143,21 @@ int vk_kernel_launches(void* ctx, int64_t* count);
 int vk_timing_begin(void* ctx);
 int vk_timing_end(void* ctx, int32_t cap, char* tags, double* total_ms, int64_t* counts, int32_t* ntags);
 
+/* Forward 2D FFT that allocates no device memory.  No counterpart in the
+ * reference.  For callers that must not call cudaMalloc, such as a Fortran
+ * code whose device arrays belong to an OpenACC / OpenMP-offload runtime, or
+ * an application with its own device pool.  psi_dev [ny][nx] and kpsi_dev
+ * [nx][ny] are DEVICE pointers to complex128 arrays owned by the caller;
+ * kpsi = unnormalised F[psi] in the transposed layout (what vk_set_psi puts in
+ * kpsi).  The transposed intermediate lives in a built-in device array of
+ * 262144 complex points (4 MiB, nx*ny must fit; nx, ny powers of two in
+ * [16, 4096]), held by every GPU that loads the library until exit.  The
+ * first call on a device resolves that array's address and fills the
+ * twiddle tables, so make it before any stream capture.  Calls share the
+ * array: calls that overlap on the GPU race.  Work is queued on `stream`
+ * (a cudaStream_t; NULL = legacy default stream) and is not synchronised. */
+int vk_fft2d_forward_noalloc(const double* psi_dev, double* kpsi_dev, int32_t nx, int32_t ny, void* stream);
+
 /* Thread-local message for the last failing call on this thread. */
 const char* vk_last_error(void);
 
