@@ -1,5 +1,6 @@
 // vk_common.cu -- small kernels shared by both precisions.
 #include "vk_kernels.cuh"
+#include "vk_particles.cuh"
 
 namespace vk {
 
@@ -29,6 +30,101 @@ __global__ void k_reduce_partials3(const double* __restrict__ part, int nblk, do
     out[0] = sh[0][0];
     out[1] = sh[1][0];
     out[2] = sh[2][0];
+  }
+}
+
+// spec[j*nsh + m] = sum_b hpart[b][j][m], fixed order over the CTAs b.
+__global__ void k_spec_reduce(const double* __restrict__ hpart, int nblk, int nsh, double* __restrict__ spec) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= 6 * nsh) return;
+  double a = 0.0;
+  for (int b = 0; b < nblk; ++b) a += hpart[(size_t)b * 6 * nsh + i];
+  spec[i] = a;
+}
+
+// e^{i k qx} for kx in [0,K] and e^{i k qy} for ky in [0, ny) (kwn order).
+__global__ void k_part_tables(PartState ps, PartConsts c) {
+  const int nx_tab = c.K + 1;
+  const int tot = c.np * (nx_tab + c.ny);
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < tot; i += gridDim.x * blockDim.x) {
+    double sn, cs;
+    if (i < c.np * nx_tab) {
+      const int p = i / nx_tab, k = i % nx_tab;
+      sincos((double)k * ps.pos[2 * p], &sn, &cs);
+      ps.tab_x[2 * i] = cs;
+      ps.tab_x[2 * i + 1] = sn;
+    } else {
+      const int j = i - c.np * nx_tab;
+      const int p = j / c.ny, k = j % c.ny;
+      const int kw = k < c.ny / 2 ? k : k - c.ny;
+      sincos((double)kw * ps.pos[2 * p + 1], &sn, &cs);
+      ps.tab_y[2 * j] = cs;
+      ps.tab_y[2 * j + 1] = sn;
+    }
+  }
+}
+
+// Sequential particle update of one RK4 stage (gp_particle_motion_rk4), or
+// with STAGE == 0 only the force evaluation at the current positions (the
+// diagnostics loop, src/diagnostics.f90:528-533).  One thread.
+__device__ __forceinline__ double ipow_d(double x, int n) {
+  double r = 1.0;
+  for (int i = 0; i < n; ++i) r *= x;
+  return r;
+}
+
+__global__ void k_part_update(PartState ps, PartConsts c, int stage) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  const int np = c.np;
+  if (stage == 1)
+    for (int i = 0; i < 2 * np; ++i) {
+      ps.tvel[i] = ps.vel[i];
+      ps.tpos[i] = ps.pos[i];
+    }
+  const double fl = -2.0 * c.alpha * c.dvol * c.scale;  // -2 alpha dvol (1/N^2)
+  for (int ip = 0; ip < np; ++ip) {
+    // fluid force: fixed-order sum of the per-CTA Parseval partials
+    double f[2] = {0.0, 0.0};
+    for (int b = 0; b < c.nblk; ++b) {
+      f[0] += ps.fpart[(size_t)b * 2 * np + 2 * ip];
+      f[1] += ps.fpart[(size_t)b * 2 * np + 2 * ip + 1];
+    }
+    // sum_x d rho V_i = f/N^2 (Parseval); force = -2 alpha dvol * that
+    f[0] *= fl;
+    f[1] *= fl;
+    // short-range repulsion with the current positions (shortrange_repulsion, :378-427)
+    double rep[2] = {0.0, 0.0};
+    if (np > 1)
+      for (int j = 0; j < np; ++j) {
+        if (j == ip) continue;
+        const double x = ps.pos[2 * ip] - ps.pos[2 * j], y = ps.pos[2 * ip + 1] - ps.pos[2 * j + 1];
+        const double den = ipow_d(-3.0 + cos(x) + cos(y), 7);
+        rep[0] += -c.rep_factor * sin(x) / den;
+        rep[1] += -c.rep_factor * sin(y) / den;
+      }
+    for (int d = 0; d < 2; ++d) {
+      const int i = 2 * ip + d;
+      const double ft = f[d] + rep[d] + ps.f0ext[i];
+      ps.frc[i] = ft;
+      if (stage == 0) continue;
+      const double ku = c.dt * ft / c.mass;
+      const double kq = c.dt * ps.vel[i];
+      ps.ku[(stage - 1) * 2 * np + i] = ku;
+      ps.kq[(stage - 1) * 2 * np + i] = kq;
+      if (stage == 1 || stage == 2) {
+        ps.vel[i] = ps.tvel[i] + 0.5 * ku;
+        ps.pos[i] = ps.tpos[i] + 0.5 * kq;
+      } else if (stage == 3) {
+        ps.vel[i] = ps.tvel[i] + ku;
+        ps.pos[i] = ps.tpos[i] + kq;
+      } else {
+        const double* K1 = ps.ku;
+        const double* Q1 = ps.kq;
+        const size_t o = 2 * (size_t)np;
+        ps.vel[i] = ps.tvel[i] + (1.0 / 6.0) * (K1[i] + 2.0 * K1[o + i] + 2.0 * K1[2 * o + i] + K1[3 * o + i]);
+        ps.pos[i] = ps.tpos[i] + (1.0 / 6.0) * (Q1[i] + 2.0 * Q1[o + i] + 2.0 * Q1[2 * o + i] + Q1[3 * o + i]);
+      }
+    }
   }
 }
 

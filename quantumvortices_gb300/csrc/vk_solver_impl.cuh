@@ -10,6 +10,7 @@
 #include <unordered_set>
 #include <vector>
 #include "vk_kernels.cuh"
+#include "vk_particles.cuh"
 #include "vk_diag.cuh"
 #include "vk_solver.h"
 
@@ -42,13 +43,18 @@ template <typename F> bool with_len(int n, F&& f) {
   }
 }
 
-inline void ensure_smem_attr(const void* fn, size_t bytes) {
+// Opt in to more than 48 KB of shared memory per CTA when static + dynamic
+// shared memory of `fn` needs it (once per kernel).
+inline void ensure_smem_attr(const void* fn, size_t dyn_bytes) {
   static std::mutex mu;
   static std::unordered_set<const void*> done;
-  if (bytes <= 48 * 1024) return;
   std::lock_guard<std::mutex> g(mu);
   if (done.count(fn)) return;
-  cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+  cudaFuncAttributes a;
+  size_t stat = 0;
+  if (cudaFuncGetAttributes(&a, fn) == cudaSuccess) stat = a.sharedSizeBytes;
+  if (stat + dyn_bytes > 48 * 1024)
+    cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)(227 * 1024 - stat));
   done.insert(fn);
 }
 
@@ -68,6 +74,19 @@ template <typename T> __global__ void k_scale_two(cplx<T>* __restrict__ a, cplx<
   for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
     a[i] = cscale(a[i], st);
     b[i] = cscale(b[i], st);
+  }
+}
+
+// vhat[kx][ky] = mask * full[kx][ky] for kx in [0, K] (particle_potential's
+// dealiased V^, src/gpe_particle.f90:67-88; V is real, so this half suffices).
+template <typename T>
+__global__ void k_extract_half(const cplx<T>* __restrict__ full, cplx<T>* __restrict__ half, int K, int nx, int ny,
+                               int k2max) {
+  const size_t n = (size_t)(K + 1) * ny;
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+    const int kx = (int)(i / ny), ky = (int)(i % ny);
+    const int k2 = kwn(ky, ny);
+    half[i] = (kx * kx + k2 * k2 > k2max) ? mkc<T>(T(0), T(0)) : full[(size_t)kx * ny + ky];
   }
 }
 
@@ -133,7 +152,56 @@ class Solver : public SolverBase {
     c_.prefac_re = -p_.disp_factor;
     c_.prefac_im = -1.0;
     c_.scale = 1.0 / ((double)nx_ * (double)ny_);
+    if (p_.n_particles > 0) {
+      int prc = init_particles();
+      if (prc) return prc;
+    }
     VK_CUDA_TRY(cudaStreamSynchronize(st_));
+    return VK_OK;
+  }
+
+  int init_particles() {
+    np_ = p_.n_particles;
+    if (nx_ < 32 || ny_ < 32) {
+      set_error("particles need nx, ny >= 32");
+      return VK_E_INVALID;
+    }
+    if (!(p_.gp_mass_part > 0) || !(p_.ppot_d > 0)) {
+      set_error("particles need gp_mass_part > 0 and ppotd > 0");
+      return VK_E_INVALID;
+    }
+    const int rp = geo_rows(ny_) / 2;
+    nblk_pot_ = (K_ + 1 + rp - 1) / rp;
+    double* d[10];
+    const size_t sz[10] = {2u * (size_t)np_, 2u * (size_t)np_, 2u * (size_t)np_, 2u * (size_t)np_, 8u * (size_t)np_,
+                           8u * (size_t)np_, 2u * (size_t)np_, 2u * (size_t)np_,
+                           2u * (size_t)np_ * (K_ + 1), 2u * (size_t)np_ * ny_};
+    for (int i = 0; i < 10; ++i) VK_CUDA_TRY(cudaMalloc(&d[i], sizeof(double) * sz[i]));
+    for (int i = 0; i < 10; ++i) VK_CUDA_TRY(cudaMemsetAsync(d[i], 0, sizeof(double) * sz[i], st_));
+    ps_.pos = d[0]; ps_.vel = d[1]; ps_.tpos = d[2]; ps_.tvel = d[3]; ps_.ku = d[4]; ps_.kq = d[5];
+    ps_.f0ext = d[6]; ps_.frc = d[7]; ps_.tab_x = d[8]; ps_.tab_y = d[9];
+    VK_CUDA_TRY(cudaMalloc(&ps_.fpart, sizeof(double) * 2 * (size_t)np_ * nblk_pot_));
+    VK_CUDA_TRY(cudaMalloc(&vhat_, sizeof(C) * (size_t)(K_ + 1) * ny_));
+    VK_CUDA_TRY(cudaMemsetAsync(vhat_, 0, sizeof(C) * (size_t)(K_ + 1) * ny_, st_));
+    VK_CUDA_TRY(cudaMalloc(&Tv_, sizeof(C) * (size_t)ny_ * pk_));
+    VK_CUDA_TRY(cudaMalloc(&vpot_, sizeof(T) * n2_));
+    const double two_pi = 6.283185307179586476925286766559, pi = two_pi / 2;
+    pc_.np = np_;
+    pc_.K = K_;
+    pc_.nx = nx_;
+    pc_.ny = ny_;
+    pc_.nblk = nblk_pot_;
+    pc_.dt = p_.dt;
+    pc_.mass = p_.gp_mass_part;
+    pc_.alpha = p_.alpha;
+    pc_.dvol = (two_pi / nx_) * (two_pi / ny_);
+    pc_.scale = c_.scale;
+    // shortrange_repulsion constants (src/gpe_particle.f90:395-401): gpdeltaE is
+    // assigned from a default-real literal, gpr0obj = 4.0*xi.
+    const double dE = (double)0.062f, r0 = 4.0 * p_.xi;
+    auto ip = [](double x, int n) { double r = 1.0; for (int i = 0; i < n; ++i) r *= x; return r; };
+    pc_.rep_factor = 384.0 * dE * ip(pi, 12) * ip(r0, 12) / ip(two_pi, 12);
+    erep_factor_ = 64.0 * dE * ip(pi, 12) * ip(r0, 12) / ip(two_pi, 12);
     return VK_OK;
   }
 
@@ -176,15 +244,24 @@ class Solver : public SolverBase {
       launch_simple("k_mask_four", k_mask_four<T>, kpsi_, nx_, ny_, k2max_);
       kpsi_masked_ = true;
     }
+    if (np_ > 0 && !have_particles_) { set_error("vk_gpe_rk4: particles not set"); return VK_E_STATE; }
     for (int s = 0; s < nsteps; ++s) {
       for (int stage = 1; stage <= 4; ++stage) {
         const bool from_psi = (s == 0 && stage == 1);
         x1(from_psi ? 0 : 1, true);
-        y1();
-        x2(+1, true);
+        if (np_ > 0) {
+          part_tables();
+          y1_pot(true, nullptr);
+          x2_pot(+1);
+        } else {
+          y1();
+          x2(+1, true);
+        }
         y2_rk4(stage);
+        if (np_ > 0) launch_raw("k_part_update", k_part_update, 1, 32, 0, ps_, pc_, stage);
       }
     }
+    if (np_ > 0) rep_init_ = true;
     xinv_from_ta(true);
     ta_ = TA_PRUNED;
     return check_launch();
@@ -194,14 +271,21 @@ class Solver : public SolverBase {
   int argle(int nsteps, double* residual) override {
     if (!have_psi_) { set_error("vk_argle: no psi set"); return VK_E_STATE; }
     if (nsteps <= 0) return VK_OK;
+    if (np_ > 0 && !have_particles_) { set_error("vk_argle: particles not set"); return VK_E_STATE; }
     if (ta_ != TA_FULL) yinv_to_ta();
     const int nblk = nx_ / geo_rows(ny_);
     for (int s = 0; s < nsteps; ++s) {
       const bool last = (s == nsteps - 1);
       const bool resid = last || p_.argle_renorm;
       x1(1, false);
-      y1();
-      x2(-1, false);
+      if (np_ > 0) {
+        if (s == 0) part_tables();
+        y1_pot(false, nullptr);
+        x2_pot(-1);
+      } else {
+        y1();
+        x2(-1, false);
+      }
       y2_argle(resid);
       if (resid) launch_raw("k_reduce_partials3", k_reduce_partials3, 1, 256, 0, (const double*)part_, nblk, sums_);
       if (p_.argle_renorm) {
@@ -230,13 +314,73 @@ class Solver : public SolverBase {
     return diag_.run(*this, scalars, spec, nvort);
   }
 
-  int particles_set(const double*, const double*, const double*) override {
-    set_error("particles: not built in this configuration");
-    return VK_E_INVALID;
+  // particle_potential + initialize_particles (src/gpe_particle.f90:3-141).
+  int particles_set(const double* pos, const double* vel, const double* f0ext) override {
+    const size_t b = sizeof(double) * 2 * np_;
+    VK_CUDA_TRY(cudaMemcpyAsync(ps_.pos, pos, b, cudaMemcpyHostToDevice, st_));
+    VK_CUDA_TRY(cudaMemcpyAsync(ps_.vel, vel, b, cudaMemcpyHostToDevice, st_));
+    VK_CUDA_TRY(cudaMemcpyAsync(ps_.f0ext, f0ext, b, cudaMemcpyHostToDevice, st_));
+    // origin-centred Gaussian on the sin chart x~ = (1/c)(s + s^3/6 + s^5/40),
+    // s = sin(c x), c = 2 pi/(2 L)  (src/gpe_particle.f90:34-59)
+    const double two_pi = 6.283185307179586476925286766559;
+    const double L = two_pi, cc = two_pi / (2.0 * L), dx = L / nx_, dy = L / ny_;
+    const double v0 = p_.ppot_v0, d = p_.ppot_d;
+    std::vector<double> v((size_t)2 * n2_);
+    for (int y = 0; y < ny_; ++y) {
+      const double sy = std::sin(cc * (y * dy));
+      const double yp = (1.0 / cc) * (sy + (1.0 / 6.0) * (sy * sy * sy) + (1.0 / 40.0) * (sy * sy * sy * sy * sy));
+      for (int x = 0; x < nx_; ++x) {
+        const double sx = std::sin(cc * (x * dx));
+        const double xp = (1.0 / cc) * (sx + (1.0 / 6.0) * (sx * sx * sx) + (1.0 / 40.0) * (sx * sx * sx * sx * sx));
+        const double r = std::sqrt(xp * xp + yp * yp);
+        v[2 * ((size_t)y * nx_ + x)] = v0 * std::exp(-(r * r) / (2.0 * (d * d)));
+        v[2 * ((size_t)y * nx_ + x) + 1] = 0.0;
+      }
+    }
+    int rc = upload(v.data(), Ta_);
+    if (rc) return rc;
+    ta_ = TA_INVALID;
+    fwd2d(Ta_, str1_, false);
+    launch_simple("k_extract_half", k_extract_half<T>, (const C*)str1_, vhat_, K_, nx_, ny_, k2max_);
+    have_particles_ = true;
+    return sync_check();
   }
-  int particles_get(double*, double*, double*) override {
-    set_error("particles: not built in this configuration");
-    return VK_E_INVALID;
+  int particles_get(double* pos, double* vel, double* frc) override {
+    const size_t b = sizeof(double) * 2 * np_;
+    if (pos) VK_CUDA_TRY(cudaMemcpyAsync(pos, ps_.pos, b, cudaMemcpyDeviceToHost, st_));
+    if (vel) VK_CUDA_TRY(cudaMemcpyAsync(vel, ps_.vel, b, cudaMemcpyDeviceToHost, st_));
+    if (frc) VK_CUDA_TRY(cudaMemcpyAsync(frc, ps_.frc, b, cudaMemcpyDeviceToHost, st_));
+    VK_CUDA_TRY(cudaStreamSynchronize(st_));
+    return VK_OK;
+  }
+  void part_tables() {
+    const int tot = np_ * (K_ + 1 + ny_);
+    launch_raw("k_part_tables", k_part_tables, std::min((tot + 255) / 256, 152 * 8), 256, 0, ps_, pc_);
+  }
+  void y1_pot(bool force, C* rhohat) {
+    with_len(ny_, [&](auto lc) {
+      constexpr int L = decltype(lc)::value;
+      typedef Geo<T, L> G;
+      const size_t sm = sizeof(C) * G::R * G::LP;
+      if (force) launch_raw("k_y1_pot", k_y1_pot<T, L, true>, nblk_pot_, G::NT, sm, (const C*)Tb_, (const C*)vhat_, Tc_, Tv_, rhohat, ps_, pc_, (const C*)twy_, c_);
+      else launch_raw("k_y1_pot", k_y1_pot<T, L, false>, nblk_pot_, G::NT, sm, (const C*)Tb_, (const C*)vhat_, Tc_, Tv_, rhohat, ps_, pc_, (const C*)twy_, c_);
+    });
+  }
+  void x2_pot(int sign) {
+    with_len(nx_, [&](auto lc) {
+      constexpr int L = decltype(lc)::value;
+      typedef Geo<T, L> G;
+      const size_t sm = sizeof(C) * G::R * G::LP;
+      if (sign > 0) launch_raw("k_x2_pot", k_x2_pot<T, L, +1, true>, ny_ / G::R, G::NT, sm, (const C*)Tc_, (const C*)Tv_, (const C*)psi_, Td_, (const C*)twx_, c_);
+      else launch_raw("k_x2_pot", k_x2_pot<T, L, -1, false>, ny_ / G::R, G::NT, sm, (const C*)Tc_, (const C*)Tv_, (const C*)psi_, Td_, (const C*)twx_, c_);
+    });
+  }
+  void vtot_phys() {
+    with_len(nx_, [&](auto lc) {
+      constexpr int L = decltype(lc)::value;
+      typedef Geo<T, L> G;
+      launch_raw("k_vtot_x", k_vtot_x<T, L>, ny_ / G::R, G::NT, sizeof(C) * G::R * G::LP, (const C*)Tv_, vpot_, (const C*)twx_, c_);
+    });
   }
 
   // ------------------------------------------------- launch helpers --
@@ -246,6 +390,11 @@ class Solver : public SolverBase {
     if (timing_ && ev_used_ == 0) record_event(nullptr);
     kern<<<grid, block, smem, st_>>>(args...);
     ++launches_;
+    const cudaError_t le = cudaGetLastError();
+    if (le != cudaSuccess && launch_err_ == cudaSuccess) {
+      launch_err_ = le;
+      launch_err_tag_ = tag;
+    }
     if (timing_) record_event(tag);
   }
   template <typename... KA, typename... A>
@@ -382,14 +531,8 @@ class Solver : public SolverBase {
       constexpr int L = decltype(lc)::value;
       typedef Geo<T, L> G;
       const size_t sm = sizeof(C) * G::R * G::LP;
-      const T* vp = vpot_;
-      if (sign > 0) {
-        if (vp) launch_raw("k_x2", k_x2<T, L, +1, true, true>, ny_ / G::R, G::NT, sm, (const C*)Tc_, (const C*)psi_, vp, Td_, (const C*)twx_, c_);
-        else launch_raw("k_x2", k_x2<T, L, +1, true, false>, ny_ / G::R, G::NT, sm, (const C*)Tc_, (const C*)psi_, vp, Td_, (const C*)twx_, c_);
-      } else {
-        if (vp) launch_raw("k_x2", k_x2<T, L, -1, false, true>, ny_ / G::R, G::NT, sm, (const C*)Tc_, (const C*)psi_, vp, Td_, (const C*)twx_, c_);
-        else launch_raw("k_x2", k_x2<T, L, -1, false, false>, ny_ / G::R, G::NT, sm, (const C*)Tc_, (const C*)psi_, vp, Td_, (const C*)twx_, c_);
-      }
+      if (sign > 0) launch_raw("k_x2", k_x2<T, L, +1, true, false>, ny_ / G::R, G::NT, sm, (const C*)Tc_, (const C*)psi_, (const T*)nullptr, Td_, (const C*)twx_, c_);
+      else launch_raw("k_x2", k_x2<T, L, -1, false, false>, ny_ / G::R, G::NT, sm, (const C*)Tc_, (const C*)psi_, (const T*)nullptr, Td_, (const C*)twx_, c_);
       (void)prune_out;
     });
   }
@@ -418,9 +561,13 @@ class Solver : public SolverBase {
   }
 
   int check_launch() {
-    cudaError_t e = cudaGetLastError();
+    cudaError_t e = launch_err_;
+    std::string tag = launch_err_tag_ ? launch_err_tag_ : "";
+    launch_err_ = cudaSuccess;
+    launch_err_tag_ = nullptr;
+    if (e == cudaSuccess) e = cudaGetLastError();
     if (e != cudaSuccess) {
-      set_error(std::string("kernel launch: ") + cudaGetErrorString(e));
+      set_error(std::string("kernel launch ") + tag + ": " + cudaGetErrorString(e));
       return VK_E_CUDA;
     }
     return VK_OK;
@@ -470,6 +617,14 @@ class Solver : public SolverBase {
     for (C* b : bufs)
       if (b) cudaFree(b);
     if (vpot_) cudaFree(vpot_);
+    if (vhat_) cudaFree(vhat_);
+    if (Tv_) cudaFree(Tv_);
+    double* pb[] = {ps_.pos, ps_.vel, ps_.tpos, ps_.tvel, ps_.ku, ps_.kq, ps_.f0ext, ps_.frc, ps_.tab_x, ps_.tab_y, ps_.fpart};
+    for (double* b : pb)
+      if (b) cudaFree(b);
+    ps_ = PartState{};
+    vpot_ = nullptr;
+    vhat_ = Tv_ = nullptr;
     if (stage64_) cudaFree(stage64_);
     if (part_) cudaFree(part_);
     if (sums_) cudaFree(sums_);
@@ -486,7 +641,13 @@ class Solver : public SolverBase {
   C *psi_ = nullptr, *kpsi_ = nullptr, *str1_ = nullptr, *str2_ = nullptr;
   C *Ta_ = nullptr, *Tb_ = nullptr, *Tc_ = nullptr, *Td_ = nullptr;
   C *twx_ = nullptr, *twy_ = nullptr;
-  T* vpot_ = nullptr;
+  T* vpot_ = nullptr;   // V_tot(x), real (diagnostics)
+  C *vhat_ = nullptr, *Tv_ = nullptr;
+  PartState ps_{};
+  PartConsts pc_{};
+  int np_ = 0, nblk_pot_ = 0;
+  bool have_particles_ = false, rep_init_ = false;
+  double erep_factor_ = 0.0;
   void* stage64_ = nullptr;
   double* part_ = nullptr;
   double* sums_ = nullptr;
@@ -495,6 +656,8 @@ class Solver : public SolverBase {
   int ta_ = TA_INVALID;
   int64_t launches_ = 0;
   bool timing_ = false;
+  cudaError_t launch_err_ = cudaSuccess;
+  const char* launch_err_tag_ = nullptr;
   int ev_used_ = 0;
   std::vector<cudaEvent_t> ev_;
   std::vector<const char*> ev_tag_;
