@@ -36,9 +36,9 @@ __device__ __forceinline__ int shell_of(int k2) {
 
 // rows kx of kpsi --(* i kx  or  * i ky)--> F^-1_y --> dst[y][kx]
 template <typename T, int L, int AXIS>
-__global__ void __launch_bounds__(Geo<T, L>::NT) k_yinv_grad(const cplx<T>* __restrict__ kpsi, cplx<T>* __restrict__ dst,
+__global__ void __launch_bounds__(GeoY<T, L>::NT, GeoY<T, L>::MINB) k_yinv_grad(const cplx<T>* __restrict__ kpsi, cplx<T>* __restrict__ dst,
                                                           const cplx<T>* __restrict__ tw, int nx) {
-  typedef Geo<T, L> G;
+  typedef GeoY<T, L> G;
   typedef cplx<T> C;
   extern __shared__ __align__(16) unsigned char smraw[];
   C* s = reinterpret_cast<C*>(smraw);
@@ -60,10 +60,10 @@ __global__ void __launch_bounds__(Geo<T, L>::NT) k_yinv_grad(const cplx<T>* __re
 // Y1 of the diagnostics: like k_y1 but also stores the masked rho^ rows
 // kx in [0,K] (all ky) for the interaction spectrum.
 template <typename T, int L>
-__global__ void __launch_bounds__(Geo<T, L>::NT) k_y1_store(const cplx<T>* __restrict__ Tb, cplx<T>* __restrict__ Tc,
+__global__ void __launch_bounds__(GeoY<T, L>::NT, GeoY<T, L>::MINB) k_y1_store(const cplx<T>* __restrict__ Tb, cplx<T>* __restrict__ Tc,
                                                          cplx<T>* __restrict__ rhohat, const cplx<T>* __restrict__ tw,
                                                          StepConsts c) {
-  typedef Geo<T, L> G;
+  typedef GeoY<T, L> G;
   typedef cplx<T> C;
   extern __shared__ __align__(16) unsigned char smraw[];
   C* s = reinterpret_cast<C*>(smraw);
@@ -103,12 +103,12 @@ enum DiagSum { DS_MOMX = 0, DS_MOMY, DS_GRAD2, DS_RHO, DS_EINT, DS_EPOT, DS_N };
 // F12 holds f1's x-spectrum in rows [0,K] and f2's in rows [K+1, 2K+1];
 // F34 likewise for f3, f4.
 template <typename T, int L, bool POT>
-__global__ void __launch_bounds__(Geo<T, L>::NT) k_dx(const cplx<T>* __restrict__ Tc, const cplx<T>* __restrict__ psi,
+__global__ void __launch_bounds__(GeoX<T, L>::NT, GeoX<T, L>::MINB) k_dx(const cplx<T>* __restrict__ Tc, const cplx<T>* __restrict__ psi,
                                                    const cplx<T>* __restrict__ gx, const cplx<T>* __restrict__ gy,
                                                    const T* __restrict__ vpot, cplx<T>* __restrict__ F12,
                                                    cplx<T>* __restrict__ F34, double* __restrict__ part,
                                                    const cplx<T>* __restrict__ tw, StepConsts c) {
-  typedef Geo<T, L> G;
+  typedef GeoX<T, L> G;
   typedef cplx<T> C;
   extern __shared__ __align__(16) unsigned char smraw[];
   C* s = reinterpret_cast<C*>(smraw);
@@ -132,7 +132,7 @@ __global__ void __launch_bounds__(Geo<T, L>::NT) k_dx(const cplx<T>* __restrict_
     s[p * G::LP + pidx(k)] = v;
   }
   __syncthreads();
-  fft_rows_sub<T, L, NPAIR, G::NTH, +1, G::NT>(s, tw);
+  fft_rows<T, L, NPAIR, G::NT, +1, G::NT>(s, tw);
   constexpr int PER = G::R * L / G::NT;
   C z1[PER], z2[PER];
   double acc[DS_N] = {0, 0, 0, 0, 0, 0};
@@ -208,7 +208,7 @@ __global__ void __launch_bounds__(NTS) k_dy_spec(const cplx<T>* __restrict__ F12
                                               SpecConsts c) {
   typedef cplx<T> C;
   constexpr int LP = padded(L);
-  constexpr int NTA = 2 * L / PlanFor<L>::maxrad;  // threads doing FFT work
+  constexpr int NTA = 2 * L / 16;  // threads doing FFT work
   static_assert(NTA <= NTS, "block too small");
   extern __shared__ __align__(16) unsigned char smraw[];
   C* s = reinterpret_cast<C*>(smraw);
@@ -221,7 +221,7 @@ __global__ void __launch_bounds__(NTS) k_dy_spec(const cplx<T>* __restrict__ F12
     s[r * LP + pidx(y)] = F12[(size_t)(r * (K + 1) + kx) * L + y];
   }
   __syncthreads();
-  fft_rows_sub<T, L, 2, NTA, -1, NTS>(s, tw);
+  fft_rows<T, L, 2, NTA, -1, NTS>(s, tw);
   const double w = kx == 0 ? 1.0 : 2.0;  // this mode + its Hermitian mirror (-kx,-ky)
   const double en = c.enorm, al = c.alpha;
   const double kxd = (double)kx;
@@ -265,7 +265,7 @@ __global__ void __launch_bounds__(NTS) k_dy_spec(const cplx<T>* __restrict__ F12
     s[r * LP + pidx(y)] = F34[(size_t)(r * (K + 1) + kx) * L + y];
   }
   __syncthreads();
-  fft_rows_sub<T, L, 2, NTA, -1, NTS>(s, tw);
+  fft_rows<T, L, 2, NTA, -1, NTS>(s, tw);
   for (int ky = threadIdx.x; ky < L; ky += NTS) {
     const int k2i = kwn(ky, L);
     const int ksq = kx * kx + k2i * k2i;
@@ -375,14 +375,14 @@ struct Diagnostics {
     for (int axis = 0; axis < 2; ++axis) {
       with_len(ny, [&](auto lc) {
         constexpr int L = decltype(lc)::value;
-        typedef Geo<T, L> G;
+        typedef GeoY<T, L> G;
         const size_t sm = sizeof(C) * G::R * G::LP;
         if (axis == 0) S_.launch_raw("k_yinv_grad", k_yinv_grad<T, L, 0>, nx / G::R, G::NT, sm, (const C*)S_.kpsi_, dt_, (const C*)S_.twy_, nx);
         else S_.launch_raw("k_yinv_grad", k_yinv_grad<T, L, 1>, nx / G::R, G::NT, sm, (const C*)S_.kpsi_, dt_, (const C*)S_.twy_, nx);
       });
       with_len(nx, [&](auto lc) {
         constexpr int L = decltype(lc)::value;
-        typedef Geo<T, L> G;
+        typedef GeoX<T, L> G;
         S_.launch_raw("k_xinv", k_xinv<T, L, false>, ny / G::R, G::NT, sizeof(C) * G::R * G::LP, (const C*)dt_,
                       axis == 0 ? gx_ : gy_, (const C*)S_.twx_, T(c.scale), K);
       });
@@ -390,7 +390,7 @@ struct Diagnostics {
     // 2. rho round trip, storing the masked rho^
     with_len(nx, [&](auto lc) {
       constexpr int L = decltype(lc)::value;
-      typedef Geo<T, L> G;
+      typedef GeoX<T, L> G;
       S_.launch_raw("k_x1", k_x1<T, L, false, false>, ny / G::R, G::NT, sizeof(C) * G::R * G::LP, (const C*)S_.Ta_,
                     S_.psi_, S_.Tb_, (const C*)S_.twx_, c);
     });
@@ -403,16 +403,16 @@ struct Diagnostics {
     } else {
       with_len(ny, [&](auto lc) {
         constexpr int L = decltype(lc)::value;
-        typedef Geo<T, L> G;
+        typedef GeoY<T, L> G;
         S_.launch_raw("k_y1_store", k_y1_store<T, L>, (K + 1 + G::R - 1) / G::R, G::NT, sizeof(C) * G::R * G::LP,
                       (const C*)S_.Tb_, S_.Tc_, rhohat_, (const C*)S_.twy_, c);
       });
     }
     // 3. fused x pass
-    const int nblk_x = ny / S_.geo_rows(nx);
+    const int nblk_x = ny / S_.geo_rows_x(nx);
     with_len(nx, [&](auto lc) {
       constexpr int L = decltype(lc)::value;
-      typedef Geo<T, L> G;
+      typedef GeoX<T, L> G;
       const size_t sm = sizeof(C) * G::R * G::LP;
       if (S_.np_ > 0)
         S_.launch_raw("k_dx", k_dx<T, L, true>, ny / G::R, G::NT, sm, (const C*)S_.Tc_, (const C*)S_.psi_,
@@ -434,7 +434,7 @@ struct Diagnostics {
     sc.enorm = inv * inv;
     with_len(ny, [&](auto lc) {
       constexpr int L = decltype(lc)::value;
-      constexpr int NTS = (2 * L / PlanFor<L>::maxrad) < 32 ? 32 : (2 * L / PlanFor<L>::maxrad);
+      constexpr int NTS = (2 * L / 16) < 32 ? 32 : (2 * L / 16);
       const size_t sm = sizeof(C) * 2 * padded(L) + sizeof(double) * 6 * (size_t)nsh_;
       S_.launch_raw("k_dy_spec", k_dy_spec<T, L, NTS>, K + 1, NTS, sm, (const C*)f12_, (const C*)f34_,
                     (const C*)rhohat_, (const C*)S_.kpsi_, hpart_, (const C*)S_.twy_, sc);

@@ -124,79 +124,94 @@ template <int RAD, int DIR, typename C> __device__ __forceinline__ void dft(C* v
 }
 
 // ---- plans ----------------------------------------------------------------
+// PlanFor<L, MAXRAD>: radices of an L-point transform, none above MAXRAD.
+// Every plan costs about 31-32 FP64 instructions per point at L = 1024.
 
 template <int... Rs> struct RadixList {};
-template <int L> struct PlanFor;
-template <> struct PlanFor<16> { using type = RadixList<16>; static constexpr int maxrad = 16; };
-template <> struct PlanFor<32> { using type = RadixList<8, 4>; static constexpr int maxrad = 8; };
-template <> struct PlanFor<64> { using type = RadixList<8, 8>; static constexpr int maxrad = 8; };
-template <> struct PlanFor<128> { using type = RadixList<16, 8>; static constexpr int maxrad = 16; };
-template <> struct PlanFor<256> { using type = RadixList<16, 16>; static constexpr int maxrad = 16; };
-template <> struct PlanFor<512> { using type = RadixList<8, 8, 8>; static constexpr int maxrad = 8; };
-template <> struct PlanFor<1024> { using type = RadixList<16, 16, 4>; static constexpr int maxrad = 16; };
-template <> struct PlanFor<2048> { using type = RadixList<16, 16, 8>; static constexpr int maxrad = 16; };
-template <> struct PlanFor<4096> { using type = RadixList<16, 16, 16>; static constexpr int maxrad = 16; };
+template <int L, int MAXRAD> struct PlanFor;
+#define VK_PLAN(LL, MR, ...) \
+  template <> struct PlanFor<LL, MR> { using type = RadixList<__VA_ARGS__>; };
+VK_PLAN(16, 16, 16) VK_PLAN(32, 16, 8, 4) VK_PLAN(64, 16, 8, 8) VK_PLAN(128, 16, 16, 8)
+VK_PLAN(256, 16, 16, 16) VK_PLAN(512, 16, 8, 8, 8) VK_PLAN(1024, 16, 16, 16, 4)
+VK_PLAN(2048, 16, 16, 16, 8) VK_PLAN(4096, 16, 16, 16, 16)
+VK_PLAN(16, 8, 8, 2) VK_PLAN(32, 8, 8, 4) VK_PLAN(64, 8, 8, 8) VK_PLAN(128, 8, 8, 4, 4)
+VK_PLAN(256, 8, 8, 8, 4) VK_PLAN(512, 8, 8, 8, 8) VK_PLAN(1024, 8, 8, 8, 4, 4)
+VK_PLAN(2048, 8, 8, 8, 8, 4) VK_PLAN(4096, 8, 8, 8, 8, 8)
+VK_PLAN(16, 4, 4, 4) VK_PLAN(32, 4, 4, 4, 2) VK_PLAN(64, 4, 4, 4, 4) VK_PLAN(128, 4, 4, 4, 4, 2)
+VK_PLAN(256, 4, 4, 4, 4, 4) VK_PLAN(512, 4, 4, 4, 4, 4, 2) VK_PLAN(1024, 4, 4, 4, 4, 4, 4)
+VK_PLAN(2048, 4, 4, 4, 4, 4, 4, 2) VK_PLAN(4096, 4, 4, 4, 4, 4, 4, 4)
+#undef VK_PLAN
 
 __host__ __device__ constexpr int padded(int L) { return L + L / 16; }
 __device__ __forceinline__ int pidx(int i) { return i + (i >> 4); }
 
-// One Stockham stage over R rows held in s (pitch LP), NT threads.
-template <typename T, int L, int R, int NT, int RAD, int NS, int DIR>
+// One Stockham stage over NR rows held in s (pitch LP); threads [0, NTA) of
+// the block (size NTB) do the work, all threads pass the barriers.
+template <typename T, int L, int NR, int NTA, int RAD, int NS, int DIR, int NTB>
 __device__ __forceinline__ void stockham_stage(cplx<T>* s, const cplx<T>* __restrict__ tw) {
   typedef cplx<T> C;
   constexpr int NB = L / RAD;
   constexpr int LP = padded(L);
-  static_assert((R * NB) % NT == 0, "threads must tile the butterflies");
-  constexpr int PER = (R * NB) / NT;
+  static_assert((NR * NB) % NTA == 0, "threads must tile the butterflies");
+  constexpr int PER = (NR * NB) / NTA;
+  const bool active = (NTA == NTB) || ((int)threadIdx.x < NTA);
   C v[PER][RAD];
+  if (active) {
 #pragma unroll
-  for (int p = 0; p < PER; ++p) {
-    const int b = threadIdx.x + p * NT;
-    const int row = b / NB, j = b % NB;
-    const C* sr = s + row * LP;
+    for (int p = 0; p < PER; ++p) {
+      const int b = threadIdx.x + p * NTA;
+      const int row = b / NB, j = b % NB;
+      const C* sr = s + row * LP;
 #pragma unroll
-    for (int m = 0; m < RAD; ++m) v[p][m] = sr[pidx(j + m * NB)];
-    if (NS > 1) {
-      const int jj = j % NS;
+      for (int m = 0; m < RAD; ++m) v[p][m] = sr[pidx(j + m * NB)];
+      if (NS > 1) {
+        const int jj = j % NS;
 #pragma unroll
-      for (int m = 1; m < RAD; ++m) {
-        C w = __ldg(tw + jj * m * (L / (NS * RAD)));
-        if (DIR > 0) w.y = -w.y;
-        v[p][m] = cmul(v[p][m], w);
+        for (int m = 1; m < RAD; ++m) {
+          C w = __ldg(tw + jj * m * (L / (NS * RAD)));
+          if (DIR > 0) w.y = -w.y;
+          v[p][m] = cmul(v[p][m], w);
+        }
       }
+      dft<RAD, DIR>(v[p]);
     }
-    dft<RAD, DIR>(v[p]);
   }
   __syncthreads();
+  if (active) {
 #pragma unroll
-  for (int p = 0; p < PER; ++p) {
-    const int b = threadIdx.x + p * NT;
-    const int row = b / NB, j = b % NB;
-    C* sr = s + row * LP;
-    const int base = (j / NS) * NS * RAD + (j % NS);
+    for (int p = 0; p < PER; ++p) {
+      const int b = threadIdx.x + p * NTA;
+      const int row = b / NB, j = b % NB;
+      C* sr = s + row * LP;
+      const int base = (j / NS) * NS * RAD + (j % NS);
 #pragma unroll
-    for (int m = 0; m < RAD; ++m) sr[pidx(base + m * NS)] = v[p][m];
+      for (int m = 0; m < RAD; ++m) sr[pidx(base + m * NS)] = v[p][m];
+    }
   }
   __syncthreads();
 }
 
-template <typename T, int L, int R, int NT, int DIR, int NS>
+template <typename T, int L, int NR, int NTA, int DIR, int NS, int NTB>
 __device__ __forceinline__ void run_stages(cplx<T>*, const cplx<T>*, RadixList<>) {}
 
-template <typename T, int L, int R, int NT, int DIR, int NS, int RAD, int... Rest>
+template <typename T, int L, int NR, int NTA, int DIR, int NS, int NTB, int RAD, int... Rest>
 __device__ __forceinline__ void run_stages(cplx<T>* s, const cplx<T>* tw, RadixList<RAD, Rest...>) {
-  stockham_stage<T, L, R, NT, RAD, NS, DIR>(s, tw);
-  run_stages<T, L, R, NT, DIR, NS * RAD>(s, tw, RadixList<Rest...>());
+  stockham_stage<T, L, NR, NTA, RAD, NS, DIR, NTB>(s, tw);
+  run_stages<T, L, NR, NTA, DIR, NS * RAD, NTB>(s, tw, RadixList<Rest...>());
 }
 
-// In-place FFT of R rows in shared memory.  Caller must __syncthreads()
-// after filling s; on return s holds the natural-order transform and all
-// threads are synchronised.  DIR = -1 forward, +1 inverse (unnormalised).
-template <typename T, int L, int R, int NT, int DIR>
+__host__ __device__ constexpr int plan_maxrad(int e) { return e >= 16 ? 16 : (e >= 8 ? 8 : 4); }
+
+// In-place FFT of the first NR rows of s by threads [0, NTA) of a block of
+// NTB threads; every thread must call it.  The plan's largest radix is the
+// number of points per thread (NR*L/NTA), capped at 16.  The caller must
+// __syncthreads() after filling s; on return s holds the natural-order
+// transform and the block is synchronised.  DIR = -1 forward, +1 inverse.
+template <typename T, int L, int NR, int NTA, int DIR, int NTB = NTA>
 __device__ __forceinline__ void fft_rows(cplx<T>* s, const cplx<T>* __restrict__ tw) {
-  run_stages<T, L, R, NT, DIR, 1>(s, tw, typename PlanFor<L>::type());
+  constexpr int E = NR * L / NTA;
+  static_assert(E >= 4, "at least four points per thread");
+  run_stages<T, L, NR, NTA, DIR, 1, NTB>(s, tw, typename PlanFor<L, plan_maxrad(E)>::type());
 }
-
-template <int L> struct RowCfg { static constexpr int maxrad = PlanFor<L>::maxrad; };
 
 }  // namespace vk

@@ -24,86 +24,31 @@
 
 namespace vk {
 
-// Launch geometry per (precision, row length): R rows per CTA (even, for the
-// real-row pairing), NT threads = R*L/maxrad (one max-radix butterfly per
-// thread and stage).
-template <typename T, int L> struct Geo;
-#define VK_GEO(TT, LL, RR)                                                  \
-  template <> struct Geo<TT, LL> {                                          \
-    static constexpr int L = LL, R = RR, LP = padded(LL);                   \
-    static constexpr int NT = RR * LL / PlanFor<LL>::maxrad;                \
-    static constexpr int NTH = (RR / 2) * LL / PlanFor<LL>::maxrad;         \
+// Launch geometry.  x passes (rows y, GeoX) hold R >= 2 rows per CTA so two
+// real rows can share one complex FFT; y passes (rows kx, GeoY) hold R rows.
+// NT = R*L/16 threads: full-height transforms run radix-16 stages, the
+// half-height paired transforms radix-8 stages on the same threads.
+// MINB is the CTAs per SM the register budget is sized for.
+template <typename T, int L> struct GeoX;
+template <typename T, int L> struct GeoY;
+#define VK_GEO(KIND, TT, LL, RR, MB)                                         \
+  template <> struct KIND<TT, LL> {                                          \
+    static constexpr int L = LL, R = RR, LP = padded(LL), MINB = MB;         \
+    static constexpr int NT = RR * LL / 16;                                  \
   };
-VK_GEO(double, 16, 16) VK_GEO(double, 32, 16) VK_GEO(double, 64, 16) VK_GEO(double, 128, 8)
-VK_GEO(double, 256, 4) VK_GEO(double, 512, 2) VK_GEO(double, 1024, 2) VK_GEO(double, 2048, 2)
-VK_GEO(double, 4096, 2)
-VK_GEO(float, 16, 16) VK_GEO(float, 32, 16) VK_GEO(float, 64, 16) VK_GEO(float, 128, 8)
-VK_GEO(float, 256, 8) VK_GEO(float, 512, 4) VK_GEO(float, 1024, 4) VK_GEO(float, 2048, 2)
-VK_GEO(float, 4096, 2)
+VK_GEO(GeoX, double, 16, 16, 4) VK_GEO(GeoX, double, 32, 16, 4) VK_GEO(GeoX, double, 64, 16, 4)
+VK_GEO(GeoX, double, 128, 8, 4) VK_GEO(GeoX, double, 256, 4, 4) VK_GEO(GeoX, double, 512, 2, 4)
+VK_GEO(GeoX, double, 1024, 2, 4) VK_GEO(GeoX, double, 2048, 2, 2) VK_GEO(GeoX, double, 4096, 2, 1)
+VK_GEO(GeoY, double, 16, 16, 4) VK_GEO(GeoY, double, 32, 8, 8) VK_GEO(GeoY, double, 64, 4, 8)
+VK_GEO(GeoY, double, 128, 2, 8) VK_GEO(GeoY, double, 256, 1, 8) VK_GEO(GeoY, double, 512, 1, 8)
+VK_GEO(GeoY, double, 1024, 1, 8) VK_GEO(GeoY, double, 2048, 1, 4) VK_GEO(GeoY, double, 4096, 1, 2)
+VK_GEO(GeoX, float, 16, 16, 4) VK_GEO(GeoX, float, 32, 16, 4) VK_GEO(GeoX, float, 64, 16, 4)
+VK_GEO(GeoX, float, 128, 8, 4) VK_GEO(GeoX, float, 256, 4, 4) VK_GEO(GeoX, float, 512, 2, 8)
+VK_GEO(GeoX, float, 1024, 2, 4) VK_GEO(GeoX, float, 2048, 2, 2) VK_GEO(GeoX, float, 4096, 2, 1)
+VK_GEO(GeoY, float, 16, 16, 4) VK_GEO(GeoY, float, 32, 8, 8) VK_GEO(GeoY, float, 64, 4, 8)
+VK_GEO(GeoY, float, 128, 2, 8) VK_GEO(GeoY, float, 256, 1, 8) VK_GEO(GeoY, float, 512, 1, 8)
+VK_GEO(GeoY, float, 1024, 1, 8) VK_GEO(GeoY, float, 2048, 1, 4) VK_GEO(GeoY, float, 4096, 1, 2)
 #undef VK_GEO
-
-// FFT of the first NR rows of s with only the first NTA threads doing work;
-// all threads must call it (it synchronises).
-template <typename T, int L, int NR, int NTA, int DIR, int NTB>
-__device__ __forceinline__ void fft_rows_sub(cplx<T>* s, const cplx<T>* __restrict__ tw);
-
-template <typename T, int L, int NR, int NTA, int DIR, int NS, int NTB>
-__device__ __forceinline__ void run_stages_sub(cplx<T>*, const cplx<T>*, RadixList<>) {}
-
-template <typename T, int L, int NR, int NTA, int RAD, int NS, int DIR, int NTB>
-__device__ __forceinline__ void stockham_stage_sub(cplx<T>* s, const cplx<T>* __restrict__ tw) {
-  typedef cplx<T> C;
-  constexpr int NB = L / RAD;
-  constexpr int LP = padded(L);
-  static_assert((NR * NB) % NTA == 0, "threads must tile the butterflies");
-  constexpr int PER = (NR * NB) / NTA;
-  const bool active = (NTA == NTB) || (threadIdx.x < NTA);
-  C v[PER][RAD];
-  if (active) {
-#pragma unroll
-    for (int p = 0; p < PER; ++p) {
-      const int b = threadIdx.x + p * NTA;
-      const int row = b / NB, j = b % NB;
-      const C* sr = s + row * LP;
-#pragma unroll
-      for (int m = 0; m < RAD; ++m) v[p][m] = sr[pidx(j + m * NB)];
-      if (NS > 1) {
-        const int jj = j % NS;
-#pragma unroll
-        for (int m = 1; m < RAD; ++m) {
-          C w = __ldg(tw + jj * m * (L / (NS * RAD)));
-          if (DIR > 0) w.y = -w.y;
-          v[p][m] = cmul(v[p][m], w);
-        }
-      }
-      dft<RAD, DIR>(v[p]);
-    }
-  }
-  __syncthreads();
-  if (active) {
-#pragma unroll
-    for (int p = 0; p < PER; ++p) {
-      const int b = threadIdx.x + p * NTA;
-      const int row = b / NB, j = b % NB;
-      C* sr = s + row * LP;
-      const int base = (j / NS) * NS * RAD + (j % NS);
-#pragma unroll
-      for (int m = 0; m < RAD; ++m) sr[pidx(base + m * NS)] = v[p][m];
-    }
-  }
-  __syncthreads();
-}
-
-template <typename T, int L, int NR, int NTA, int DIR, int NS, int NTB, int RAD, int... Rest>
-__device__ __forceinline__ void run_stages_sub(cplx<T>* s, const cplx<T>* tw, RadixList<RAD, Rest...>) {
-  stockham_stage_sub<T, L, NR, NTA, RAD, NS, DIR, NTB>(s, tw);
-  run_stages_sub<T, L, NR, NTA, DIR, NS * RAD, NTB>(s, tw, RadixList<Rest...>());
-}
-
-template <typename T, int L, int NR, int NTA, int DIR, int NTB>
-__device__ __forceinline__ void fft_rows_sub(cplx<T>* s, const cplx<T>* __restrict__ tw) {
-  run_stages_sub<T, L, NR, NTA, DIR, 1, NTB>(s, tw, typename PlanFor<L>::type());
-}
 
 __device__ __forceinline__ int kwn(int i, int n) { return i < n / 2 ? i : i - n; }
 
@@ -127,9 +72,9 @@ struct StepConsts {
 
 // rows y of src[y][x] -> F_x -> dst[kx][y] (all kx).
 template <typename T, int L>
-__global__ void __launch_bounds__(Geo<T, L>::NT) k_xfwd(const cplx<T>* __restrict__ src, cplx<T>* __restrict__ dst,
+__global__ void __launch_bounds__(GeoX<T, L>::NT, GeoX<T, L>::MINB) k_xfwd(const cplx<T>* __restrict__ src, cplx<T>* __restrict__ dst,
                                                      const cplx<T>* __restrict__ tw, int ny) {
-  typedef Geo<T, L> G;
+  typedef GeoX<T, L> G;
   typedef cplx<T> C;
   extern __shared__ __align__(16) unsigned char smraw[];
   C* s = reinterpret_cast<C*>(smraw);
@@ -149,10 +94,10 @@ __global__ void __launch_bounds__(Geo<T, L>::NT) k_xfwd(const cplx<T>* __restric
 // rows kx of src[kx][y] -> F_y -> dst[kx][ky].  With MASKOUT the 2/3 mask
 // (and an optional shell amplification, ic_OTOC_gpe) is applied on the way out.
 template <typename T, int L, bool OTOC>
-__global__ void __launch_bounds__(Geo<T, L>::NT) k_yfwd(const cplx<T>* __restrict__ src, cplx<T>* __restrict__ dst,
+__global__ void __launch_bounds__(GeoY<T, L>::NT, GeoY<T, L>::MINB) k_yfwd(const cplx<T>* __restrict__ src, cplx<T>* __restrict__ dst,
                                                      const cplx<T>* __restrict__ tw, int nx, int k2max,
                                                      double k_otoc, double eps_otoc) {
-  typedef Geo<T, L> G;
+  typedef GeoY<T, L> G;
   typedef cplx<T> C;
   extern __shared__ __align__(16) unsigned char smraw[];
   C* s = reinterpret_cast<C*>(smraw);
@@ -180,9 +125,9 @@ __global__ void __launch_bounds__(Geo<T, L>::NT) k_yfwd(const cplx<T>* __restric
 
 // rows kx of src[kx][ky] -> F^-1_y -> dst[y][kx] (pitch nx).
 template <typename T, int L>
-__global__ void __launch_bounds__(Geo<T, L>::NT) k_yinv(const cplx<T>* __restrict__ src, cplx<T>* __restrict__ dst,
+__global__ void __launch_bounds__(GeoY<T, L>::NT, GeoY<T, L>::MINB) k_yinv(const cplx<T>* __restrict__ src, cplx<T>* __restrict__ dst,
                                                      const cplx<T>* __restrict__ tw, int nx) {
-  typedef Geo<T, L> G;
+  typedef GeoY<T, L> G;
   typedef cplx<T> C;
   extern __shared__ __align__(16) unsigned char smraw[];
   C* s = reinterpret_cast<C*>(smraw);
@@ -202,9 +147,9 @@ __global__ void __launch_bounds__(Geo<T, L>::NT) k_yinv(const cplx<T>* __restric
 // rows y of src[y][kx] -> F^-1_x -> * scale -> dst[y][x].  With PRUNE only
 // columns |kx| <= K are read (the rest are known zero).
 template <typename T, int L, bool PRUNE>
-__global__ void __launch_bounds__(Geo<T, L>::NT) k_xinv(const cplx<T>* __restrict__ src, cplx<T>* __restrict__ dst,
+__global__ void __launch_bounds__(GeoX<T, L>::NT, GeoX<T, L>::MINB) k_xinv(const cplx<T>* __restrict__ src, cplx<T>* __restrict__ dst,
                                                      const cplx<T>* __restrict__ tw, T scale, int K) {
-  typedef Geo<T, L> G;
+  typedef GeoX<T, L> G;
   typedef cplx<T> C;
   extern __shared__ __align__(16) unsigned char smraw[];
   C* s = reinterpret_cast<C*>(smraw);
@@ -242,10 +187,10 @@ __global__ void k_mask_four(cplx<T>* __restrict__ f, int nx, int ny, int k2max) 
 // Output Tb[kx][y] for kx in [0, K] (Hermitian half of the real rows).
 // ------------------------------------------------------------------------
 template <typename T, int L, bool FROM_T, bool PRUNE>
-__global__ void __launch_bounds__(Geo<T, L>::NT) k_x1(const cplx<T>* __restrict__ Ta, cplx<T>* __restrict__ psi,
+__global__ void __launch_bounds__(GeoX<T, L>::NT, GeoX<T, L>::MINB) k_x1(const cplx<T>* __restrict__ Ta, cplx<T>* __restrict__ psi,
                                                    cplx<T>* __restrict__ Tb, const cplx<T>* __restrict__ tw,
                                                    StepConsts c) {
-  typedef Geo<T, L> G;
+  typedef GeoX<T, L> G;
   typedef cplx<T> C;
   extern __shared__ __align__(16) unsigned char smraw[];
   C* s = reinterpret_cast<C*>(smraw);
@@ -294,7 +239,7 @@ __global__ void __launch_bounds__(Geo<T, L>::NT) k_x1(const cplx<T>* __restrict_
     s[p * G::LP + pidx(x)] = z[q];
   }
   __syncthreads();
-  fft_rows_sub<T, L, NPAIR, G::NTH, -1, G::NT>(s, tw);
+  fft_rows<T, L, NPAIR, G::NT, -1, G::NT>(s, tw);
   // unpack: A(k) = (Z(k) + conj Z(-k))/2, B(k) = -i (Z(k) - conj Z(-k))/2
   for (int e = threadIdx.x; e < G::R * (K + 1); e += G::NT) {
     const int r = e % G::R, k = e / G::R;
@@ -312,9 +257,9 @@ __global__ void __launch_bounds__(Geo<T, L>::NT) k_x1(const cplx<T>* __restrict_
 // Y1: rows kx in [0,K] of Tb: F_y, 2/3 mask, F^-1_y -> Tc[y][kx] (pitch pk).
 // ------------------------------------------------------------------------
 template <typename T, int L>
-__global__ void __launch_bounds__(Geo<T, L>::NT) k_y1(const cplx<T>* __restrict__ Tb, cplx<T>* __restrict__ Tc,
+__global__ void __launch_bounds__(GeoY<T, L>::NT, GeoY<T, L>::MINB) k_y1(const cplx<T>* __restrict__ Tb, cplx<T>* __restrict__ Tc,
                                                    const cplx<T>* __restrict__ tw, StepConsts c) {
-  typedef Geo<T, L> G;
+  typedef GeoY<T, L> G;
   typedef cplx<T> C;
   extern __shared__ __align__(16) unsigned char smraw[];
   C* s = reinterpret_cast<C*>(smraw);
@@ -348,10 +293,10 @@ __global__ void __launch_bounds__(Geo<T, L>::NT) k_y1(const cplx<T>* __restrict_
 // PRUNE_OUT: only |kx| <= K columns of Td are written (RK4).
 // ------------------------------------------------------------------------
 template <typename T, int L, int SIGN, bool PRUNE_OUT, bool POT>
-__global__ void __launch_bounds__(Geo<T, L>::NT) k_x2(const cplx<T>* __restrict__ Tc, const cplx<T>* __restrict__ psi,
+__global__ void __launch_bounds__(GeoX<T, L>::NT, GeoX<T, L>::MINB) k_x2(const cplx<T>* __restrict__ Tc, const cplx<T>* __restrict__ psi,
                                                    const T* __restrict__ vpot, cplx<T>* __restrict__ Td,
                                                    const cplx<T>* __restrict__ tw, StepConsts c) {
-  typedef Geo<T, L> G;
+  typedef GeoX<T, L> G;
   typedef cplx<T> C;
   extern __shared__ __align__(16) unsigned char smraw[];
   C* s = reinterpret_cast<C*>(smraw);
@@ -374,7 +319,7 @@ __global__ void __launch_bounds__(Geo<T, L>::NT) k_x2(const cplx<T>* __restrict_
     s[p * G::LP + pidx(k)] = v;
   }
   __syncthreads();
-  fft_rows_sub<T, L, NPAIR, G::NTH, +1, G::NT>(s, tw);
+  fft_rows<T, L, NPAIR, G::NT, +1, G::NT>(s, tw);
   constexpr int PER = G::R * L / G::NT;
   C nv[PER];
   const T gs = T(SIGN * c.g);
@@ -425,11 +370,11 @@ __global__ void __launch_bounds__(Geo<T, L>::NT) k_x2(const cplx<T>* __restrict_
 // then the stage update of src/gpe.f90:366-489; kpsi_new --F^-1_y--> Ta.
 // ------------------------------------------------------------------------
 template <typename T, int L, int STAGE>
-__global__ void __launch_bounds__(Geo<T, L>::NT) k_y2_rk4(const cplx<T>* __restrict__ Td, cplx<T>* __restrict__ kpsi,
+__global__ void __launch_bounds__(GeoY<T, L>::NT, GeoY<T, L>::MINB) k_y2_rk4(const cplx<T>* __restrict__ Td, cplx<T>* __restrict__ kpsi,
                                                        cplx<T>* __restrict__ str1, cplx<T>* __restrict__ str2,
                                                        cplx<T>* __restrict__ Ta, const cplx<T>* __restrict__ tw,
                                                        StepConsts c) {
-  typedef Geo<T, L> G;
+  typedef GeoY<T, L> G;
   typedef cplx<T> C;
   extern __shared__ __align__(16) unsigned char smraw[];
   C* s = reinterpret_cast<C*>(smraw);
@@ -499,10 +444,10 @@ __global__ void __launch_bounds__(Geo<T, L>::NT) k_y2_rk4(const cplx<T>* __restr
 // |new-old|^2, |old|^2, |new|^2 into part[blockIdx][3].
 // ------------------------------------------------------------------------
 template <typename T, int L, bool RESID>
-__global__ void __launch_bounds__(Geo<T, L>::NT) k_y2_argle(const cplx<T>* __restrict__ Td, cplx<T>* __restrict__ kpsi,
+__global__ void __launch_bounds__(GeoY<T, L>::NT, GeoY<T, L>::MINB) k_y2_argle(const cplx<T>* __restrict__ Td, cplx<T>* __restrict__ kpsi,
                                                          cplx<T>* __restrict__ Ta, const cplx<T>* __restrict__ tw,
                                                          double* __restrict__ part, StepConsts c) {
-  typedef Geo<T, L> G;
+  typedef GeoY<T, L> G;
   typedef cplx<T> C;
   extern __shared__ __align__(16) unsigned char smraw[];
   C* s = reinterpret_cast<C*>(smraw);

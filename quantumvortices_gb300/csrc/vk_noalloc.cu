@@ -126,14 +126,14 @@ extern "C" int vk_fft2d_forward_noalloc(const double* psi_dev, double* kpsi_dev,
   const double2* twy = slots->tw + (ny - 16);
   with_len_na(nx, [&](auto lc) {
     constexpr int L = decltype(lc)::value;
-    typedef Geo<double, L> G;
+    typedef GeoX<double, L> G;
     const size_t sm = sizeof(double2) * G::R * G::LP;
     if (sm > 48 * 1024) cudaFuncSetAttribute(k_xfwd<double, L>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
     k_xfwd<double, L><<<ny / G::R, G::NT, sm, st>>>(in, scratch, twx, ny);
   });
   with_len_na(ny, [&](auto lc) {
     constexpr int L = decltype(lc)::value;
-    typedef Geo<double, L> G;
+    typedef GeoY<double, L> G;
     const size_t sm = sizeof(double2) * G::R * G::LP;
     if (sm > 48 * 1024)
       cudaFuncSetAttribute(k_yfwd<double, L, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);

@@ -50,11 +50,11 @@ __global__ void k_part_tables(PartState ps, PartConsts c);
 // fpart[blk][p][d] of -w kx Im[rho^ conj(V^) e^{ik.q_p}] (w = 2 for kx > 0).
 // Particles are taken 16 at a time with register accumulators.
 template <typename T, int L, bool FORCE>
-__global__ void __launch_bounds__(Geo<T, L>::NT) k_y1_pot(const cplx<T>* __restrict__ Tb, const cplx<T>* __restrict__ vhat,
+__global__ void __launch_bounds__(GeoX<T, L>::NT, GeoX<T, L>::MINB) k_y1_pot(const cplx<T>* __restrict__ Tb, const cplx<T>* __restrict__ vhat,
                                                        cplx<T>* __restrict__ Tc, cplx<T>* __restrict__ Tv,
                                                        cplx<T>* __restrict__ rhohat, PartState ps, PartConsts pc,
                                                        const cplx<T>* __restrict__ tw, StepConsts c) {
-  typedef Geo<T, L> G;
+  typedef GeoX<T, L> G;
   typedef cplx<T> C;
   constexpr int RP = G::R / 2;
   constexpr int NW = G::NT / 32 > 0 ? G::NT / 32 : 1;
@@ -73,7 +73,7 @@ __global__ void __launch_bounds__(Geo<T, L>::NT) k_y1_pot(const cplx<T>* __restr
     s[r * G::LP + pidx(y)] = v;
   }
   __syncthreads();
-  fft_rows_sub<T, L, RP, G::NTH, -1, G::NT>(s, tw);
+  fft_rows<T, L, RP, G::NT, -1, G::NT>(s, tw);
   // mask rho^ in place, zero V^_tot
   for (int e = threadIdx.x; e < RP * L; e += G::NT) {
     const int r = e / L, ky = e % L;
@@ -152,10 +152,10 @@ __global__ void __launch_bounds__(Geo<T, L>::NT) k_y1_pot(const cplx<T>* __restr
 // N = SIGN*(g P_G rho psi + V_tot psi) -> F_x -> Td.  When VOUT is set the
 // real V_tot rows are also stored (diagnostics).
 template <typename T, int L, int SIGN, bool PRUNE_OUT>
-__global__ void __launch_bounds__(Geo<T, L>::NT) k_x2_pot(const cplx<T>* __restrict__ Tc, const cplx<T>* __restrict__ Tv,
+__global__ void __launch_bounds__(GeoX<T, L>::NT, GeoX<T, L>::MINB) k_x2_pot(const cplx<T>* __restrict__ Tc, const cplx<T>* __restrict__ Tv,
                                                        const cplx<T>* __restrict__ psi, cplx<T>* __restrict__ Td,
                                                        const cplx<T>* __restrict__ tw, StepConsts c) {
-  typedef Geo<T, L> G;
+  typedef GeoX<T, L> G;
   typedef cplx<T> C;
   extern __shared__ __align__(16) unsigned char smraw[];
   C* s = reinterpret_cast<C*>(smraw);
@@ -206,9 +206,9 @@ __global__ void __launch_bounds__(Geo<T, L>::NT) k_x2_pot(const cplx<T>* __restr
 
 // Real V_tot rows (diagnostics): Z = V^ Hermitian-extended, F^-1_x, real part.
 template <typename T, int L>
-__global__ void __launch_bounds__(Geo<T, L>::NT) k_vtot_x(const cplx<T>* __restrict__ Tv, T* __restrict__ vout,
+__global__ void __launch_bounds__(GeoX<T, L>::NT, GeoX<T, L>::MINB) k_vtot_x(const cplx<T>* __restrict__ Tv, T* __restrict__ vout,
                                                        const cplx<T>* __restrict__ tw, StepConsts c) {
-  typedef Geo<T, L> G;
+  typedef GeoX<T, L> G;
   typedef cplx<T> C;
   extern __shared__ __align__(16) unsigned char smraw[];
   C* s = reinterpret_cast<C*>(smraw);

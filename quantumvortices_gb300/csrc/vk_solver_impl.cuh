@@ -170,7 +170,7 @@ class Solver : public SolverBase {
       set_error("particles need gp_mass_part > 0 and ppotd > 0");
       return VK_E_INVALID;
     }
-    const int rp = geo_rows(ny_) / 2;
+    const int rp = geo_rows_x(ny_) / 2;
     nblk_pot_ = (K_ + 1 + rp - 1) / rp;
     double* d[10];
     const size_t sz[10] = {2u * (size_t)np_, 2u * (size_t)np_, 2u * (size_t)np_, 2u * (size_t)np_, 8u * (size_t)np_,
@@ -236,6 +236,57 @@ class Solver : public SolverBase {
   int get_psi(double* out) override { return download(psi_, out); }
   int get_kpsi(double* out) override { return download(kpsi_, out); }
 
+  // One RK4 step (gpe_rk4, src/gpe.f90:310-494): four stages of four fused
+  // passes, plus the particle tables/update when particles are on.
+  void rk4_step(bool from_psi) {
+    for (int stage = 1; stage <= 4; ++stage) {
+      x1((from_psi && stage == 1) ? 0 : 1, true);
+      if (np_ > 0) {
+        part_tables();
+        y1_pot(true, nullptr);
+        x2_pot(+1);
+      } else {
+        y1();
+        x2(+1, true);
+      }
+      y2_rk4(stage);
+      if (np_ > 0) launch_raw("k_part_update", k_part_update, 1, 32, 0, ps_, pc_, stage);
+    }
+  }
+
+  // Launch `body` through a CUDA graph captured on first use (one graph per
+  // kind of step; pointers and constants of a context never change).  Falls
+  // back to direct launches if capture is not possible.
+  template <typename F> int replay(cudaGraphExec_t& ge, int64_t& nk, F&& body) {
+    if (!ge && graphs_ok_) {
+      const int64_t l0 = launches_;
+      cudaGraph_t g = nullptr;
+      if (cudaStreamBeginCapture(st_, cudaStreamCaptureModeThreadLocal) == cudaSuccess) {
+        body();
+        if (cudaStreamEndCapture(st_, &g) == cudaSuccess && g &&
+            cudaGraphInstantiate(&ge, g, 0) == cudaSuccess) {
+          nk = launches_ - l0;
+        } else {
+          ge = nullptr;
+          graphs_ok_ = false;
+        }
+        if (g) cudaGraphDestroy(g);
+      } else {
+        graphs_ok_ = false;
+      }
+      launches_ = l0;
+      cudaGetLastError();
+      launch_err_ = cudaSuccess;
+    }
+    if (!ge) {
+      body();
+      return VK_OK;
+    }
+    VK_CUDA_TRY(cudaGraphLaunch(ge, st_));
+    launches_ += nk;
+    return VK_OK;
+  }
+
   // ---------------------------------------------------------------- RK4 --
   int rk4(int nsteps) override {
     if (!have_psi_) { set_error("vk_gpe_rk4: no psi set"); return VK_E_STATE; }
@@ -246,19 +297,11 @@ class Solver : public SolverBase {
     }
     if (np_ > 0 && !have_particles_) { set_error("vk_gpe_rk4: particles not set"); return VK_E_STATE; }
     for (int s = 0; s < nsteps; ++s) {
-      for (int stage = 1; stage <= 4; ++stage) {
-        const bool from_psi = (s == 0 && stage == 1);
-        x1(from_psi ? 0 : 1, true);
-        if (np_ > 0) {
-          part_tables();
-          y1_pot(true, nullptr);
-          x2_pot(+1);
-        } else {
-          y1();
-          x2(+1, true);
-        }
-        y2_rk4(stage);
-        if (np_ > 0) launch_raw("k_part_update", k_part_update, 1, 32, 0, ps_, pc_, stage);
+      if (s == 0 || timing_) {
+        rk4_step(s == 0);
+      } else {
+        int rc = replay(g_rk4_, g_rk4_n_, [&]() { rk4_step(false); });
+        if (rc) return rc;
       }
     }
     if (np_ > 0) rep_init_ = true;
@@ -267,33 +310,44 @@ class Solver : public SolverBase {
     return check_launch();
   }
 
+  // One ARGLE step (src/gpe.f90:5-224) with the new residual sums when resid.
+  void argle_step(bool resid, int nblk) {
+    x1(1, false);
+    if (np_ > 0) {
+      y1_pot(false, nullptr);
+      x2_pot(-1);
+    } else {
+      y1();
+      x2(-1, false);
+    }
+    y2_argle(resid);
+    if (resid) launch_raw("k_reduce_partials3", k_reduce_partials3, 1, 256, 0, (const double*)part_, nblk, sums_);
+    if (p_.argle_renorm) {
+      // norm = dvol * (1/(nx ny)) * sum |kpsi|^2; target Nparticle = Lx*Ly
+      const double two_pi = 6.283185307179586476925286766559;
+      const double dvol = (two_pi / nx_) * (two_pi / ny_);
+      const double area = two_pi * two_pi;
+      launch_raw("k_scale_two", k_scale_two<T>, 1024, 256, 0, kpsi_, Ta_, n2_, (const double*)sums_,
+                 area / (dvol * c_.scale));
+    }
+  }
+
   // -------------------------------------------------------------- ARGLE --
   int argle(int nsteps, double* residual) override {
     if (!have_psi_) { set_error("vk_argle: no psi set"); return VK_E_STATE; }
     if (nsteps <= 0) return VK_OK;
     if (np_ > 0 && !have_particles_) { set_error("vk_argle: particles not set"); return VK_E_STATE; }
     if (ta_ != TA_FULL) yinv_to_ta();
-    const int nblk = nx_ / geo_rows(ny_);
+    const int nblk = nx_ / geo_rows_y(ny_);
+    if (np_ > 0) part_tables();
     for (int s = 0; s < nsteps; ++s) {
       const bool last = (s == nsteps - 1);
       const bool resid = last || p_.argle_renorm;
-      x1(1, false);
-      if (np_ > 0) {
-        if (s == 0) part_tables();
-        y1_pot(false, nullptr);
-        x2_pot(-1);
+      if (resid || timing_) {
+        argle_step(resid, nblk);
       } else {
-        y1();
-        x2(-1, false);
-      }
-      y2_argle(resid);
-      if (resid) launch_raw("k_reduce_partials3", k_reduce_partials3, 1, 256, 0, (const double*)part_, nblk, sums_);
-      if (p_.argle_renorm) {
-        // norm = dvol * (1/(nx ny)) * sum |kpsi|^2; target Nparticle = Lx*Ly
-        const double two_pi = 6.283185307179586476925286766559;
-        const double dvol = (two_pi / nx_) * (two_pi / ny_);
-        const double area = two_pi * two_pi;
-        launch_raw("k_scale_two", k_scale_two<T>, 1024, 256, 0, kpsi_, Ta_, n2_, (const double*)sums_, area / (dvol * c_.scale));
+        int rc = replay(g_argle_, g_argle_n_, [&]() { argle_step(false, nblk); });
+        if (rc) return rc;
       }
     }
     ta_ = TA_FULL;
@@ -360,7 +414,7 @@ class Solver : public SolverBase {
   void y1_pot(bool force, C* rhohat) {
     with_len(ny_, [&](auto lc) {
       constexpr int L = decltype(lc)::value;
-      typedef Geo<T, L> G;
+      typedef GeoX<T, L> G;
       const size_t sm = sizeof(C) * G::R * G::LP;
       if (force) launch_raw("k_y1_pot", k_y1_pot<T, L, true>, nblk_pot_, G::NT, sm, (const C*)Tb_, (const C*)vhat_, Tc_, Tv_, rhohat, ps_, pc_, (const C*)twy_, c_);
       else launch_raw("k_y1_pot", k_y1_pot<T, L, false>, nblk_pot_, G::NT, sm, (const C*)Tb_, (const C*)vhat_, Tc_, Tv_, rhohat, ps_, pc_, (const C*)twy_, c_);
@@ -369,7 +423,7 @@ class Solver : public SolverBase {
   void x2_pot(int sign) {
     with_len(nx_, [&](auto lc) {
       constexpr int L = decltype(lc)::value;
-      typedef Geo<T, L> G;
+      typedef GeoX<T, L> G;
       const size_t sm = sizeof(C) * G::R * G::LP;
       if (sign > 0) launch_raw("k_x2_pot", k_x2_pot<T, L, +1, true>, ny_ / G::R, G::NT, sm, (const C*)Tc_, (const C*)Tv_, (const C*)psi_, Td_, (const C*)twx_, c_);
       else launch_raw("k_x2_pot", k_x2_pot<T, L, -1, false>, ny_ / G::R, G::NT, sm, (const C*)Tc_, (const C*)Tv_, (const C*)psi_, Td_, (const C*)twx_, c_);
@@ -378,7 +432,7 @@ class Solver : public SolverBase {
   void vtot_phys() {
     with_len(nx_, [&](auto lc) {
       constexpr int L = decltype(lc)::value;
-      typedef Geo<T, L> G;
+      typedef GeoX<T, L> G;
       launch_raw("k_vtot_x", k_vtot_x<T, L>, ny_ / G::R, G::NT, sizeof(C) * G::R * G::LP, (const C*)Tv_, vpot_, (const C*)twx_, c_);
     });
   }
@@ -447,9 +501,14 @@ class Solver : public SolverBase {
     ev_used_ = 0;
     return VK_OK;
   }
-  static int geo_rows(int L) {
+  static int geo_rows_x(int L) {
     int r = 0;
-    with_len(L, [&](auto lc) { r = Geo<T, decltype(lc)::value>::R; });
+    with_len(L, [&](auto lc) { r = GeoX<T, decltype(lc)::value>::R; });
+    return r;
+  }
+  static int geo_rows_y(int L) {
+    int r = 0;
+    with_len(L, [&](auto lc) { r = GeoY<T, decltype(lc)::value>::R; });
     return r;
   }
 
@@ -457,12 +516,12 @@ class Solver : public SolverBase {
   void fwd2d(const C* phys, C* four, bool otoc) {
     with_len(nx_, [&](auto lc) {
       constexpr int L = decltype(lc)::value;
-      typedef Geo<T, L> G;
+      typedef GeoX<T, L> G;
       launch_raw("k_xfwd", k_xfwd<T, L>, ny_ / G::R, G::NT, sizeof(C) * G::R * G::LP, phys, Td_, (const C*)twx_, ny_);
     });
     with_len(ny_, [&](auto lc) {
       constexpr int L = decltype(lc)::value;
-      typedef Geo<T, L> G;
+      typedef GeoY<T, L> G;
       if (otoc)
         launch_raw("k_yfwd", k_yfwd<T, L, true>, nx_ / G::R, G::NT, sizeof(C) * G::R * G::LP, (const C*)Td_, four,
                    (const C*)twy_, nx_, k2max_, p_.k_otoc_gp, p_.eps_otoc_gp);
@@ -475,12 +534,12 @@ class Solver : public SolverBase {
   void inv2d(const C* four, C* phys, bool prune) {
     with_len(ny_, [&](auto lc) {
       constexpr int L = decltype(lc)::value;
-      typedef Geo<T, L> G;
+      typedef GeoY<T, L> G;
       launch_raw("k_yinv", k_yinv<T, L>, nx_ / G::R, G::NT, sizeof(C) * G::R * G::LP, four, Ta_, (const C*)twy_, nx_);
     });
     with_len(nx_, [&](auto lc) {
       constexpr int L = decltype(lc)::value;
-      typedef Geo<T, L> G;
+      typedef GeoX<T, L> G;
       if (prune)
         launch_raw("k_xinv", k_xinv<T, L, true>, ny_ / G::R, G::NT, sizeof(C) * G::R * G::LP, (const C*)Ta_, phys,
                    (const C*)twx_, T(c_.scale), K_);
@@ -492,14 +551,14 @@ class Solver : public SolverBase {
   void yinv_to_ta() {
     with_len(ny_, [&](auto lc) {
       constexpr int L = decltype(lc)::value;
-      typedef Geo<T, L> G;
+      typedef GeoY<T, L> G;
       launch_raw("k_yinv", k_yinv<T, L>, nx_ / G::R, G::NT, sizeof(C) * G::R * G::LP, (const C*)kpsi_, Ta_, (const C*)twy_, nx_);
     });
   }
   void xinv_from_ta(bool prune) {
     with_len(nx_, [&](auto lc) {
       constexpr int L = decltype(lc)::value;
-      typedef Geo<T, L> G;
+      typedef GeoX<T, L> G;
       if (prune)
         launch_raw("k_xinv", k_xinv<T, L, true>, ny_ / G::R, G::NT, sizeof(C) * G::R * G::LP, (const C*)Ta_, psi_,
                    (const C*)twx_, T(c_.scale), K_);
@@ -511,7 +570,7 @@ class Solver : public SolverBase {
   void x1(int from_t, bool prune) {
     with_len(nx_, [&](auto lc) {
       constexpr int L = decltype(lc)::value;
-      typedef Geo<T, L> G;
+      typedef GeoX<T, L> G;
       const size_t sm = sizeof(C) * G::R * G::LP;
       if (!from_t) launch_raw("k_x1", k_x1<T, L, false, false>, ny_ / G::R, G::NT, sm, (const C*)Ta_, psi_, Tb_, (const C*)twx_, c_);
       else if (prune) launch_raw("k_x1", k_x1<T, L, true, true>, ny_ / G::R, G::NT, sm, (const C*)Ta_, psi_, Tb_, (const C*)twx_, c_);
@@ -521,7 +580,7 @@ class Solver : public SolverBase {
   void y1() {
     with_len(ny_, [&](auto lc) {
       constexpr int L = decltype(lc)::value;
-      typedef Geo<T, L> G;
+      typedef GeoY<T, L> G;
       launch_raw("k_y1", k_y1<T, L>, (K_ + 1 + G::R - 1) / G::R, G::NT, sizeof(C) * G::R * G::LP, (const C*)Tb_, Tc_,
                  (const C*)twy_, c_);
     });
@@ -529,7 +588,7 @@ class Solver : public SolverBase {
   void x2(int sign, bool prune_out) {
     with_len(nx_, [&](auto lc) {
       constexpr int L = decltype(lc)::value;
-      typedef Geo<T, L> G;
+      typedef GeoX<T, L> G;
       const size_t sm = sizeof(C) * G::R * G::LP;
       if (sign > 0) launch_raw("k_x2", k_x2<T, L, +1, true, false>, ny_ / G::R, G::NT, sm, (const C*)Tc_, (const C*)psi_, (const T*)nullptr, Td_, (const C*)twx_, c_);
       else launch_raw("k_x2", k_x2<T, L, -1, false, false>, ny_ / G::R, G::NT, sm, (const C*)Tc_, (const C*)psi_, (const T*)nullptr, Td_, (const C*)twx_, c_);
@@ -539,7 +598,7 @@ class Solver : public SolverBase {
   void y2_rk4(int stage) {
     with_len(ny_, [&](auto lc) {
       constexpr int L = decltype(lc)::value;
-      typedef Geo<T, L> G;
+      typedef GeoY<T, L> G;
       const int grid = (2 * K_ + 1 + G::R - 1) / G::R;
       const size_t sm = sizeof(C) * G::R * G::LP;
       switch (stage) {
@@ -553,7 +612,7 @@ class Solver : public SolverBase {
   void y2_argle(bool resid) {
     with_len(ny_, [&](auto lc) {
       constexpr int L = decltype(lc)::value;
-      typedef Geo<T, L> G;
+      typedef GeoY<T, L> G;
       const size_t sm = sizeof(C) * G::R * G::LP;
       if (resid) launch_raw("k_y2_argle", k_y2_argle<T, L, true>, nx_ / G::R, G::NT, sm, (const C*)Td_, kpsi_, Ta_, (const C*)twy_, part_, c_);
       else launch_raw("k_y2_argle", k_y2_argle<T, L, false>, nx_ / G::R, G::NT, sm, (const C*)Td_, kpsi_, Ta_, (const C*)twy_, part_, c_);
@@ -610,6 +669,9 @@ class Solver : public SolverBase {
 
   void release() {
     diag_.release();
+    if (g_rk4_) cudaGraphExecDestroy(g_rk4_);
+    if (g_argle_) cudaGraphExecDestroy(g_argle_);
+    g_rk4_ = g_argle_ = nullptr;
     for (auto e : ev_) cudaEventDestroy(e);
     ev_.clear();
     if (twy_ && twy_ != twx_) cudaFree(twy_);
@@ -656,6 +718,9 @@ class Solver : public SolverBase {
   int ta_ = TA_INVALID;
   int64_t launches_ = 0;
   bool timing_ = false;
+  bool graphs_ok_ = true;
+  cudaGraphExec_t g_rk4_ = nullptr, g_argle_ = nullptr;
+  int64_t g_rk4_n_ = 0, g_argle_n_ = 0;
   cudaError_t launch_err_ = cudaSuccess;
   const char* launch_err_tag_ = nullptr;
   int ev_used_ = 0;
