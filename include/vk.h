@@ -135,6 +135,21 @@ int vk_get_stream(void* ctx, void** stream);
 /* Number of kernels this context has launched so far. */
 int vk_kernel_launches(void* ctx, int64_t* count);
 
+/* Ensembles (new, no reference counterpart; BASELINE configs[3]): n
+ * independent fields of uneven sizes (nx, ny in {128, 256, 512, 1024}, one
+ * precision, no particles) stepped together.  Each RK4 pass is one
+ * persistent kernel over all members' row tiles; tile heights and grid sizes
+ * come from an autotuner run at vk_ens_init (vk_ens_report describes it);
+ * steps after the first replay one CUDA graph. */
+int vk_ens_init(const vk_params* members, int32_t n, void** ens);
+int vk_ens_finalize(void* ens);
+int vk_ens_set_psi(void* ens, int32_t member, const double* psi_phys);
+int vk_ens_get_psi(void* ens, int32_t member, double* psi_phys);
+int vk_ens_gpe_rk4(void* ens, int32_t nsteps);
+int vk_ens_report(void* ens, char* buf, int32_t cap);
+int vk_ens_get_stream(void* ens, void** stream);
+int vk_ens_kernel_launches(void* ens, int64_t* count);
+
 /* Per-kernel timing.  Between vk_timing_begin and vk_timing_end every kernel
  * this context launches is bracketed by CUDA events on the context's stream;
  * vk_timing_end synchronises and returns, per kernel tag (NUL-terminated,

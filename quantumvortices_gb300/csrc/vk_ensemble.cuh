@@ -1,0 +1,342 @@
+// vk_ensemble.cuh -- batched RK4 over an ensemble of independent fields of
+// uneven sizes (128, 256, 512 or 1024 points per side).
+//
+// Every pass of the single-field stepper (X1, Y1, X2, Y2 and the final
+// F^-1_x) becomes one persistent kernel over a work list of (member, row
+// tile) items for ALL members: a CTA walks items blockIdx.x, +gridDim.x, ...
+// and runs the same device body as the single-field kernel with that
+// member's buffers.  Tiles hold RL points (R = RL/L rows), so items of
+// different sizes cost about the same and a static stride balances.  One
+// RK4 step (16 persistent launches) is captured as one CUDA graph.
+//
+// Autotuner: at set-up it times, on the (still zero) ensemble buffers, every
+// compiled tile variant (x passes RL = 2048 or 4096 points, y passes
+// RL = 1024 or 2048) at 1, 2, 4 and 8 CTAs per SM, per pass kind, and keeps
+// the fastest.
+#pragma once
+#include <algorithm>
+#include <string>
+#include <vector>
+#include "vk_kernels.cuh"
+#include "vk_solver.h"
+#include <type_traits>
+
+namespace vk {
+
+template <typename T, int LL, int RL> struct GeoB {
+  static constexpr int L = LL, R = RL / LL, LP = padded(LL), MINB = 2;
+  static constexpr int NT = RL / 16;
+};
+
+#define VK_ENS_SWITCH(N, BODY)                      \
+  switch (N) {                                      \
+    case 128: { constexpr int L = 128; BODY; } break; \
+    case 256: { constexpr int L = 256; BODY; } break; \
+    case 512: { constexpr int L = 512; BODY; } break; \
+    case 1024: { constexpr int L = 1024; BODY; } break; \
+    default: break;                                 \
+  }
+
+template <typename T, int RL, bool FROM_T>
+__global__ void __launch_bounds__(RL / 16) kb_x1(const Field<T>* __restrict__ F, const int2* __restrict__ items, int n) {
+  extern __shared__ __align__(16) unsigned char smraw[];
+  cplx<T>* s = reinterpret_cast<cplx<T>*>(smraw);
+  for (int it = blockIdx.x; it < n; it += gridDim.x) {
+    const int2 w = items[it];
+    const Field<T>& f = F[w.x];
+    VK_ENS_SWITCH(f.c.nx, (x1_body<T, L, GeoB<T, L, RL>, FROM_T, true>(f.Ta, f.psi, f.Tb, f.twx, f.c, w.y, s)));
+    __syncthreads();
+  }
+}
+
+template <typename T, int RL>
+__global__ void __launch_bounds__(RL / 16) kb_y1(const Field<T>* __restrict__ F, const int2* __restrict__ items, int n) {
+  extern __shared__ __align__(16) unsigned char smraw[];
+  cplx<T>* s = reinterpret_cast<cplx<T>*>(smraw);
+  for (int it = blockIdx.x; it < n; it += gridDim.x) {
+    const int2 w = items[it];
+    const Field<T>& f = F[w.x];
+    VK_ENS_SWITCH(f.c.ny, (y1_body<T, L, GeoB<T, L, RL>>(f.Tb, f.Tc, f.twy, f.c, w.y, s)));
+    __syncthreads();
+  }
+}
+
+template <typename T, int RL>
+__global__ void __launch_bounds__(RL / 16) kb_x2(const Field<T>* __restrict__ F, const int2* __restrict__ items, int n) {
+  extern __shared__ __align__(16) unsigned char smraw[];
+  cplx<T>* s = reinterpret_cast<cplx<T>*>(smraw);
+  for (int it = blockIdx.x; it < n; it += gridDim.x) {
+    const int2 w = items[it];
+    const Field<T>& f = F[w.x];
+    VK_ENS_SWITCH(f.c.nx, (x2_body<T, L, GeoB<T, L, RL>, +1, true, false>(f.Tc, f.psi, (const T*)nullptr, f.Td,
+                                                                            f.twx, f.c, w.y, s)));
+    __syncthreads();
+  }
+}
+
+template <typename T, int RL, int STAGE>
+__global__ void __launch_bounds__(RL / 16) kb_y2(const Field<T>* __restrict__ F, const int2* __restrict__ items, int n) {
+  extern __shared__ __align__(16) unsigned char smraw[];
+  cplx<T>* s = reinterpret_cast<cplx<T>*>(smraw);
+  for (int it = blockIdx.x; it < n; it += gridDim.x) {
+    const int2 w = items[it];
+    const Field<T>& f = F[w.x];
+    VK_ENS_SWITCH(f.c.ny, (y2_rk4_body<T, L, GeoB<T, L, RL>, STAGE>(f.Td, f.kpsi, f.str1, f.str2, f.Ta, f.twy, f.c,
+                                                                      w.y, s)));
+    __syncthreads();
+  }
+}
+
+template <typename T, int RL>
+__global__ void __launch_bounds__(RL / 16) kb_xinv(const Field<T>* __restrict__ F, const int2* __restrict__ items, int n) {
+  extern __shared__ __align__(16) unsigned char smraw[];
+  cplx<T>* s = reinterpret_cast<cplx<T>*>(smraw);
+  for (int it = blockIdx.x; it < n; it += gridDim.x) {
+    const int2 w = items[it];
+    const Field<T>& f = F[w.x];
+    VK_ENS_SWITCH(f.c.nx, (xinv_body<T, L, GeoB<T, L, RL>, true>(f.Ta, f.psi, f.twx, T(f.c.scale), f.c.K, w.y, s)));
+    __syncthreads();
+  }
+}
+
+// Pass kinds the autotuner decides separately.
+enum EnsPass { EP_X1 = 0, EP_Y1, EP_X2, EP_Y2, EP_XINV, EP_N };
+
+template <typename T>
+class Ensemble {
+  typedef cplx<T> C;
+
+ public:
+  std::vector<SolverBase*> owned;
+  std::vector<Field<T>> fields;
+  int n = 0;
+  cudaStream_t st = nullptr;
+  Field<T>* dF = nullptr;
+  // work lists per pass kind and tile variant: [kind][variant]
+  int2* dItems[EP_N][2] = {};
+  int nItems[EP_N][2] = {};
+  int variant[EP_N] = {0, 0, 0, 0, 0};
+  int grid[EP_N] = {0, 0, 0, 0, 0};
+  int sms = 152;
+  bool masked = false;
+  cudaGraphExec_t gstep = nullptr;
+  int64_t launches = 0, gstep_n = 0;
+  std::string report;
+
+  static constexpr int XRL[2] = {2048, 4096};
+  static constexpr int YRL[2] = {1024, 2048};
+
+  int init(const vk_params* ps, int nmem) {
+    n = nmem;
+    int dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    for (int m = 0; m < n; ++m) {
+      const int nx = ps[m].nx, ny = ps[m].ny;
+      auto ok = [](int v) { return v == 128 || v == 256 || v == 512 || v == 1024; };
+      if (!ok(nx) || !ok(ny) || ps[m].n_particles != 0) {
+        set_error("vk_ens_init: members need nx, ny in {128, 256, 512, 1024} and no particles");
+        return VK_E_INVALID;
+      }
+      int rc = VK_OK;
+      SolverBase* sb = std::is_same<T, double>::value ? make_solver_f64(ps[m], &rc) : make_solver_f32(ps[m], &rc);
+      if (!sb) return rc ? rc : VK_E_CUDA;
+      owned.push_back(sb);
+      Field<T> f;
+      if ((rc = sb->field_view(&f, sizeof(f)))) return rc;
+      fields.push_back(f);
+    }
+    if (cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaMalloc(&dF, sizeof(Field<T>) * n) != cudaSuccess ||
+        cudaMemcpy(dF, fields.data(), sizeof(Field<T>) * n, cudaMemcpyHostToDevice) != cudaSuccess) {
+      set_error("vk_ens_init: device allocation failed");
+      return VK_E_NOMEM;
+    }
+    int rc = build_lists();
+    if (rc) return rc;
+    return autotune();
+  }
+
+  ~Ensemble() {
+    for (auto* o : owned) delete o;
+    if (gstep) cudaGraphExecDestroy(gstep);
+    for (auto& a : dItems)
+      for (auto* b : a)
+        if (b) cudaFree(b);
+    if (dF) cudaFree(dF);
+    if (st) cudaStreamDestroy(st);
+  }
+
+  static int rows_x(int L, int v) { return XRL[v] / L; }
+  static int rows_y(int L, int v) { return YRL[v] / L; }
+
+  int build_lists() {
+    for (int kind = 0; kind < EP_N; ++kind)
+      for (int v = 0; v < 2; ++v) {
+        // per member tile counts, then round-robin interleave across members
+        std::vector<int> cnt(n);
+        int tot = 0;
+        for (int m = 0; m < n; ++m) {
+          const StepConsts& c = fields[m].c;
+          const bool xk = (kind == EP_X1 || kind == EP_X2 || kind == EP_XINV);
+          const int R = xk ? rows_x(c.nx, v) : rows_y(c.ny, v);
+          const int rows = xk ? c.ny : (kind == EP_Y1 ? c.K + 1 : 2 * c.K + 1);
+          cnt[m] = (rows + R - 1) / R;
+          tot += cnt[m];
+        }
+        std::vector<int2> items;
+        items.reserve(tot);
+        const int mx = *std::max_element(cnt.begin(), cnt.end());
+        for (int t = 0; t < mx; ++t)
+          for (int m = 0; m < n; ++m)
+            if (t < cnt[m]) items.push_back(make_int2(m, t));
+        if (cudaMalloc(&dItems[kind][v], sizeof(int2) * items.size()) != cudaSuccess ||
+            cudaMemcpy(dItems[kind][v], items.data(), sizeof(int2) * items.size(), cudaMemcpyHostToDevice) !=
+                cudaSuccess) {
+          set_error("vk_ens_init: work list upload failed");
+          return VK_E_NOMEM;
+        }
+        nItems[kind][v] = (int)items.size();
+      }
+    return VK_OK;
+  }
+
+  template <typename K> void launch(K kern, int g, int threads, size_t smem, int kind, int v) {
+    ensure_smem_attr((const void*)kern, smem);
+    kern<<<g, threads, smem, st>>>(dF, dItems[kind][v], nItems[kind][v]);
+    ++launches;
+  }
+
+  void pass(int kind, int stage, bool from_t, int v, int g) {
+    constexpr size_t E = sizeof(C);
+    if (kind == EP_X1) {
+      if (v == 0) {
+        const size_t sm = E * 2048 * 17 / 16;
+        if (from_t) launch(kb_x1<T, 2048, true>, g, 128, sm, kind, v);
+        else launch(kb_x1<T, 2048, false>, g, 128, sm, kind, v);
+      } else {
+        const size_t sm = E * 4096 * 17 / 16;
+        if (from_t) launch(kb_x1<T, 4096, true>, g, 256, sm, kind, v);
+        else launch(kb_x1<T, 4096, false>, g, 256, sm, kind, v);
+      }
+    } else if (kind == EP_Y1) {
+      if (v == 0) launch(kb_y1<T, 1024>, g, 64, E * 1024 * 17 / 16, kind, v);
+      else launch(kb_y1<T, 2048>, g, 128, E * 2048 * 17 / 16, kind, v);
+    } else if (kind == EP_X2) {
+      if (v == 0) launch(kb_x2<T, 2048>, g, 128, E * 2048 * 17 / 16, kind, v);
+      else launch(kb_x2<T, 4096>, g, 256, E * 4096 * 17 / 16, kind, v);
+    } else if (kind == EP_Y2) {
+      const size_t sm0 = E * 1024 * 17 / 16, sm1 = E * 2048 * 17 / 16;
+      switch (stage) {
+        case 1: v == 0 ? launch(kb_y2<T, 1024, 1>, g, 64, sm0, kind, v) : launch(kb_y2<T, 2048, 1>, g, 128, sm1, kind, v); break;
+        case 2: v == 0 ? launch(kb_y2<T, 1024, 2>, g, 64, sm0, kind, v) : launch(kb_y2<T, 2048, 2>, g, 128, sm1, kind, v); break;
+        case 3: v == 0 ? launch(kb_y2<T, 1024, 3>, g, 64, sm0, kind, v) : launch(kb_y2<T, 2048, 3>, g, 128, sm1, kind, v); break;
+        default: v == 0 ? launch(kb_y2<T, 1024, 4>, g, 64, sm0, kind, v) : launch(kb_y2<T, 2048, 4>, g, 128, sm1, kind, v); break;
+      }
+    } else {
+      if (v == 0) launch(kb_xinv<T, 2048>, g, 128, E * 2048 * 17 / 16, kind, v);
+      else launch(kb_xinv<T, 4096>, g, 256, E * 4096 * 17 / 16, kind, v);
+    }
+  }
+
+  void step(bool first) {
+    for (int stage = 1; stage <= 4; ++stage) {
+      pass(EP_X1, stage, !(first && stage == 1), variant[EP_X1], grid[EP_X1]);
+      pass(EP_Y1, stage, true, variant[EP_Y1], grid[EP_Y1]);
+      pass(EP_X2, stage, true, variant[EP_X2], grid[EP_X2]);
+      pass(EP_Y2, stage, true, variant[EP_Y2], grid[EP_Y2]);
+    }
+  }
+
+  // Times each (variant, CTAs per SM) per pass kind on the current buffers.
+  int autotune() {
+    cudaEvent_t a, b;
+    if (cudaEventCreate(&a) || cudaEventCreate(&b)) {
+      set_error("vk_ens: event creation failed");
+      return VK_E_CUDA;
+    }
+    const int per_sm[4] = {1, 2, 4, 8};
+    const char* names[EP_N] = {"x1", "y1", "x2", "y2", "xinv"};
+    report.clear();
+    for (int kind = 0; kind < EP_N; ++kind) {
+      float best = 1e30f;
+      for (int v = 0; v < 2; ++v)
+        for (int k = 0; k < 4; ++k) {
+          const int g = sms * per_sm[k];
+          pass(kind, 2, true, v, g);  // warm
+          cudaEventRecord(a, st);
+          for (int r = 0; r < 3; ++r) pass(kind, 2, true, v, g);
+          cudaEventRecord(b, st);
+          cudaEventSynchronize(b);
+          float ms = 0.f;
+          cudaEventElapsedTime(&ms, a, b);
+          if (ms < best) {
+            best = ms;
+            variant[kind] = v;
+            grid[kind] = g;
+          }
+        }
+      char buf[160];
+      snprintf(buf, sizeof(buf), "%s: tile %d points, %d CTAs (%.1f us/launch); ", names[kind],
+               (kind == EP_Y1 || kind == EP_Y2) ? YRL[variant[kind]] : XRL[variant[kind]], grid[kind],
+               1e3f * best / 3.f);
+      report += buf;
+    }
+    cudaEventDestroy(a);
+    cudaEventDestroy(b);
+    const cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) {
+      set_error(std::string("vk_ens autotune: ") + cudaGetErrorString(e));
+      return VK_E_CUDA;
+    }
+    return VK_OK;
+  }
+
+  int rk4(int nsteps) {
+    if (nsteps <= 0) return VK_OK;
+    for (int m = 0; m < n; ++m)
+      if (!owned[m]->kpsi_is_masked()) {
+        const StepConsts& c = fields[m].c;
+        k_mask_four<T><<<512, 256, 0, st>>>(fields[m].kpsi, c.nx, c.ny, c.k2max);
+        ++launches;
+      }
+    for (int s = 0; s < nsteps; ++s) {
+      if (s == 0) {
+        step(true);
+        continue;
+      }
+      if (!gstep) {
+        const int64_t l0 = launches;
+        cudaGraph_t g = nullptr;
+        if (cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal) == cudaSuccess) {
+          step(false);
+          if (cudaStreamEndCapture(st, &g) != cudaSuccess || cudaGraphInstantiate(&gstep, g, 0) != cudaSuccess)
+            gstep = nullptr;
+          if (g) cudaGraphDestroy(g);
+        }
+        gstep_n = launches - l0;
+        launches = l0;
+        cudaGetLastError();
+      }
+      if (gstep) {
+        if (cudaGraphLaunch(gstep, st) != cudaSuccess) {
+          set_error("vk_ens_gpe_rk4: graph launch failed");
+          return VK_E_CUDA;
+        }
+        launches += gstep_n;
+      } else {
+        step(false);
+      }
+    }
+    pass(EP_XINV, 0, true, variant[EP_XINV], grid[EP_XINV]);
+    for (int m = 0; m < n; ++m) owned[m]->mark_rk4_done();
+    const cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) {
+      set_error(std::string("vk_ens_gpe_rk4: ") + cudaGetErrorString(e));
+      return VK_E_CUDA;
+    }
+    return VK_OK;
+  }
+};
+
+}  // namespace vk

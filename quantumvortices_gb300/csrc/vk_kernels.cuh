@@ -20,9 +20,27 @@
 // RK4 mask every column |kx| > K of kpsi, of the RHS and of Ta is zero, so
 // the RK4 passes skip those rows (identical arithmetic on every kept mode).
 #pragma once
+#include <mutex>
+#include <unordered_set>
 #include "vk_fft.cuh"
 
 namespace vk {
+
+// Opt in to more than 48 KB of shared memory per CTA when static + dynamic
+// shared memory of `fn` needs it (once per kernel).
+inline void ensure_smem_attr(const void* fn, size_t dyn_bytes) {
+  static std::mutex mu;
+  static std::unordered_set<const void*> done;
+  std::lock_guard<std::mutex> g(mu);
+  if (done.count(fn)) return;
+  cudaFuncAttributes a;
+  size_t stat = 0;
+  if (cudaFuncGetAttributes(&a, fn) == cudaSuccess) stat = a.sharedSizeBytes;
+  if (stat + dyn_bytes > 48 * 1024)
+    cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)(227 * 1024 - stat));
+  done.insert(fn);
+}
+
 
 // Launch geometry.  x passes (rows y, GeoX) hold R >= 2 rows per CTA so two
 // real rows can share one complex FFT; y passes (rows kx, GeoY) hold R rows.
@@ -64,6 +82,14 @@ struct StepConsts {
   double alpha, g, omega, dt;
   double prefac_re, prefac_im;   // (1 - i*disp_factor)/i
   double scale;      // 1/(nx*ny)
+};
+
+// Device view of one field's buffers and constants (ensemble work items
+// index an array of these).
+template <typename T> struct Field {
+  cplx<T>*psi, *kpsi, *str1, *str2, *Ta, *Tb, *Tc, *Td;
+  const cplx<T>*twx, *twy;
+  StepConsts c;
 };
 
 // ------------------------------------------------------------------------
@@ -146,14 +172,11 @@ __global__ void __launch_bounds__(GeoY<T, L>::NT, GeoY<T, L>::MINB) k_yinv(const
 
 // rows y of src[y][kx] -> F^-1_x -> * scale -> dst[y][x].  With PRUNE only
 // columns |kx| <= K are read (the rest are known zero).
-template <typename T, int L, bool PRUNE>
-__global__ void __launch_bounds__(GeoX<T, L>::NT, GeoX<T, L>::MINB) k_xinv(const cplx<T>* __restrict__ src, cplx<T>* __restrict__ dst,
-                                                     const cplx<T>* __restrict__ tw, T scale, int K) {
-  typedef GeoX<T, L> G;
+template <typename T, int L, class G, bool PRUNE>
+__device__ __forceinline__ void xinv_body(const cplx<T>* __restrict__ src, cplx<T>* __restrict__ dst,
+                                                     const cplx<T>* __restrict__ tw, T scale, int K, const int tile, cplx<T>* __restrict__ s) {
   typedef cplx<T> C;
-  extern __shared__ __align__(16) unsigned char smraw[];
-  C* s = reinterpret_cast<C*>(smraw);
-  const int y0 = blockIdx.x * G::R;
+  const int y0 = tile * G::R;
   for (int e = threadIdx.x; e < G::R * L; e += G::NT) {
     const int r = e / L, k = e % L;
     C v = mkc<T>(T(0), T(0));
@@ -166,6 +189,13 @@ __global__ void __launch_bounds__(GeoX<T, L>::NT, GeoX<T, L>::MINB) k_xinv(const
     const int r = e / L, x = e % L;
     dst[(size_t)(y0 + r) * L + x] = cscale(s[r * G::LP + pidx(x)], scale);
   }
+}
+
+template <typename T, int L, bool PRUNE>
+__global__ void __launch_bounds__(GeoX<T, L>::NT, GeoX<T, L>::MINB) k_xinv(const cplx<T>* __restrict__ src, cplx<T>* __restrict__ dst,
+                                                     const cplx<T>* __restrict__ tw, T scale, int K) {
+  extern __shared__ __align__(16) unsigned char smraw[];
+  xinv_body<T, L, GeoX<T, L>, PRUNE>(src, dst, tw, scale, K, blockIdx.x, reinterpret_cast<cplx<T>*>(smraw));
 }
 
 // Zero kpsi rows |kx| > K and in-row modes outside the 2/3 disk (the mask at
@@ -186,15 +216,12 @@ __global__ void k_mask_four(cplx<T>* __restrict__ f, int nx, int ny, int k2max) 
 //   PRUNE : Ta columns |kx| > K are zero (RK4).
 // Output Tb[kx][y] for kx in [0, K] (Hermitian half of the real rows).
 // ------------------------------------------------------------------------
-template <typename T, int L, bool FROM_T, bool PRUNE>
-__global__ void __launch_bounds__(GeoX<T, L>::NT, GeoX<T, L>::MINB) k_x1(const cplx<T>* __restrict__ Ta, cplx<T>* __restrict__ psi,
+template <typename T, int L, class G, bool FROM_T, bool PRUNE>
+__device__ __forceinline__ void x1_body(const cplx<T>* __restrict__ Ta, cplx<T>* __restrict__ psi,
                                                    cplx<T>* __restrict__ Tb, const cplx<T>* __restrict__ tw,
-                                                   StepConsts c) {
-  typedef GeoX<T, L> G;
+                                                   StepConsts c, const int tile, cplx<T>* __restrict__ s) {
   typedef cplx<T> C;
-  extern __shared__ __align__(16) unsigned char smraw[];
-  C* s = reinterpret_cast<C*>(smraw);
-  const int y0 = blockIdx.x * G::R;
+  const int y0 = tile * G::R;
   const int ny = c.ny, K = c.K;
   if (FROM_T) {
     for (int e = threadIdx.x; e < G::R * L; e += G::NT) {
@@ -253,17 +280,22 @@ __global__ void __launch_bounds__(GeoX<T, L>::NT, GeoX<T, L>::MINB) k_x1(const c
   }
 }
 
+template <typename T, int L, bool FROM_T, bool PRUNE>
+__global__ void __launch_bounds__(GeoX<T, L>::NT, GeoX<T, L>::MINB) k_x1(const cplx<T>* __restrict__ Ta, cplx<T>* __restrict__ psi,
+                                                   cplx<T>* __restrict__ Tb, const cplx<T>* __restrict__ tw,
+                                                   StepConsts c) {
+  extern __shared__ __align__(16) unsigned char smraw[];
+  x1_body<T, L, GeoX<T, L>, FROM_T, PRUNE>(Ta, psi, Tb, tw, c, blockIdx.x, reinterpret_cast<cplx<T>*>(smraw));
+}
+
 // ------------------------------------------------------------------------
 // Y1: rows kx in [0,K] of Tb: F_y, 2/3 mask, F^-1_y -> Tc[y][kx] (pitch pk).
 // ------------------------------------------------------------------------
-template <typename T, int L>
-__global__ void __launch_bounds__(GeoY<T, L>::NT, GeoY<T, L>::MINB) k_y1(const cplx<T>* __restrict__ Tb, cplx<T>* __restrict__ Tc,
-                                                   const cplx<T>* __restrict__ tw, StepConsts c) {
-  typedef GeoY<T, L> G;
+template <typename T, int L, class G>
+__device__ __forceinline__ void y1_body(const cplx<T>* __restrict__ Tb, cplx<T>* __restrict__ Tc,
+                                                   const cplx<T>* __restrict__ tw, StepConsts c, const int tile, cplx<T>* __restrict__ s) {
   typedef cplx<T> C;
-  extern __shared__ __align__(16) unsigned char smraw[];
-  C* s = reinterpret_cast<C*>(smraw);
-  const int l0 = blockIdx.x * G::R;
+  const int l0 = tile * G::R;
   const int K = c.K;
   for (int e = threadIdx.x; e < G::R * L; e += G::NT) {
     const int r = e / L, y = e % L;
@@ -286,21 +318,25 @@ __global__ void __launch_bounds__(GeoY<T, L>::NT, GeoY<T, L>::MINB) k_y1(const c
   }
 }
 
+template <typename T, int L>
+__global__ void __launch_bounds__(GeoY<T, L>::NT, GeoY<T, L>::MINB) k_y1(const cplx<T>* __restrict__ Tb, cplx<T>* __restrict__ Tc,
+                                                   const cplx<T>* __restrict__ tw, StepConsts c) {
+  extern __shared__ __align__(16) unsigned char smraw[];
+  y1_body<T, L, GeoY<T, L>>(Tb, Tc, tw, c, blockIdx.x, reinterpret_cast<cplx<T>*>(smraw));
+}
+
 // ------------------------------------------------------------------------
 // X2: rows y of Tc (kx in [0,K]) -> P_G rho (real, two rows per complex
 // F^-1_x) -> N = SIGN*g*P_G rho*psi [+ SIGN*V*psi] -> F_x -> Td[kx][y].
 // SIGN = +1 for gpe_rhs (src/gpe.f90:583-594), -1 for ARGLE (:101-112).
 // PRUNE_OUT: only |kx| <= K columns of Td are written (RK4).
 // ------------------------------------------------------------------------
-template <typename T, int L, int SIGN, bool PRUNE_OUT, bool POT>
-__global__ void __launch_bounds__(GeoX<T, L>::NT, GeoX<T, L>::MINB) k_x2(const cplx<T>* __restrict__ Tc, const cplx<T>* __restrict__ psi,
+template <typename T, int L, class G, int SIGN, bool PRUNE_OUT, bool POT>
+__device__ __forceinline__ void x2_body(const cplx<T>* __restrict__ Tc, const cplx<T>* __restrict__ psi,
                                                    const T* __restrict__ vpot, cplx<T>* __restrict__ Td,
-                                                   const cplx<T>* __restrict__ tw, StepConsts c) {
-  typedef GeoX<T, L> G;
+                                                   const cplx<T>* __restrict__ tw, StepConsts c, const int tile, cplx<T>* __restrict__ s) {
   typedef cplx<T> C;
-  extern __shared__ __align__(16) unsigned char smraw[];
-  C* s = reinterpret_cast<C*>(smraw);
-  const int y0 = blockIdx.x * G::R;
+  const int y0 = tile * G::R;
   const int K = c.K, ny = c.ny, pk = c.pk;
   constexpr int NPAIR = G::R / 2;
   // Z_p(k) = A(k) + i B(k) with the Hermitian extension to negative k.
@@ -364,21 +400,26 @@ __global__ void __launch_bounds__(GeoX<T, L>::NT, GeoX<T, L>::MINB) k_x2(const c
   }
 }
 
+template <typename T, int L, int SIGN, bool PRUNE_OUT, bool POT>
+__global__ void __launch_bounds__(GeoX<T, L>::NT, GeoX<T, L>::MINB) k_x2(const cplx<T>* __restrict__ Tc, const cplx<T>* __restrict__ psi,
+                                                   const T* __restrict__ vpot, cplx<T>* __restrict__ Td,
+                                                   const cplx<T>* __restrict__ tw, StepConsts c) {
+  extern __shared__ __align__(16) unsigned char smraw[];
+  x2_body<T, L, GeoX<T, L>, SIGN, PRUNE_OUT, POT>(Tc, psi, vpot, Td, tw, c, blockIdx.x, reinterpret_cast<cplx<T>*>(smraw));
+}
+
 // ------------------------------------------------------------------------
 // Y2 (RK4 stage STAGE = 1..4): rows |kx| <= K of Td: F_y -> N^ ->
 // rhs = prefac*((alpha k^2 - Omega) kpsi + N^), masked (src/gpe.f90:609-669)
 // then the stage update of src/gpe.f90:366-489; kpsi_new --F^-1_y--> Ta.
 // ------------------------------------------------------------------------
-template <typename T, int L, int STAGE>
-__global__ void __launch_bounds__(GeoY<T, L>::NT, GeoY<T, L>::MINB) k_y2_rk4(const cplx<T>* __restrict__ Td, cplx<T>* __restrict__ kpsi,
+template <typename T, int L, class G, int STAGE>
+__device__ __forceinline__ void y2_rk4_body(const cplx<T>* __restrict__ Td, cplx<T>* __restrict__ kpsi,
                                                        cplx<T>* __restrict__ str1, cplx<T>* __restrict__ str2,
                                                        cplx<T>* __restrict__ Ta, const cplx<T>* __restrict__ tw,
-                                                       StepConsts c) {
-  typedef GeoY<T, L> G;
+                                                       StepConsts c, const int tile, cplx<T>* __restrict__ s) {
   typedef cplx<T> C;
-  extern __shared__ __align__(16) unsigned char smraw[];
-  C* s = reinterpret_cast<C*>(smraw);
-  const int l0 = blockIdx.x * G::R;
+  const int l0 = tile * G::R;
   const int K = c.K, nx = c.nx;
   const int nrow = 2 * K + 1;
   for (int e = threadIdx.x; e < G::R * L; e += G::NT) {
@@ -437,23 +478,29 @@ __global__ void __launch_bounds__(GeoY<T, L>::NT, GeoY<T, L>::MINB) k_y2_rk4(con
   }
 }
 
+template <typename T, int L, int STAGE>
+__global__ void __launch_bounds__(GeoY<T, L>::NT, GeoY<T, L>::MINB) k_y2_rk4(const cplx<T>* __restrict__ Td, cplx<T>* __restrict__ kpsi,
+                                                       cplx<T>* __restrict__ str1, cplx<T>* __restrict__ str2,
+                                                       cplx<T>* __restrict__ Ta, const cplx<T>* __restrict__ tw,
+                                                       StepConsts c) {
+  extern __shared__ __align__(16) unsigned char smraw[];
+  y2_rk4_body<T, L, GeoY<T, L>, STAGE>(Td, kpsi, str1, str2, Ta, tw, c, blockIdx.x, reinterpret_cast<cplx<T>*>(smraw));
+}
+
 // ------------------------------------------------------------------------
 // Y2 (ARGLE, src/gpe.f90:181-222, no mask): all rows kx of Td: F_y -> N^,
 // kpsi <- (kpsi + dt (N^ + Omega kpsi)) / (1 + alpha k^2 dt);
 // kpsi_new --F^-1_y--> Ta.  RESID: per-CTA FP64 partial sums of
 // |new-old|^2, |old|^2, |new|^2 into part[blockIdx][3].
 // ------------------------------------------------------------------------
-template <typename T, int L, bool RESID>
-__global__ void __launch_bounds__(GeoY<T, L>::NT, GeoY<T, L>::MINB) k_y2_argle(const cplx<T>* __restrict__ Td, cplx<T>* __restrict__ kpsi,
+template <typename T, int L, class G, bool RESID>
+__device__ __forceinline__ void y2_argle_body(const cplx<T>* __restrict__ Td, cplx<T>* __restrict__ kpsi,
                                                          cplx<T>* __restrict__ Ta, const cplx<T>* __restrict__ tw,
-                                                         double* __restrict__ part, StepConsts c) {
-  typedef GeoY<T, L> G;
+                                                         double* __restrict__ part, StepConsts c, const int tile, cplx<T>* __restrict__ s) {
   typedef cplx<T> C;
-  extern __shared__ __align__(16) unsigned char smraw[];
-  C* s = reinterpret_cast<C*>(smraw);
   static_assert(G::NT <= 512, "reduction buffer");
   __shared__ double red[3][512];
-  const int x0 = blockIdx.x * G::R;
+  const int x0 = tile * G::R;
   const int nx = c.nx;
   for (int e = threadIdx.x; e < G::R * L; e += G::NT) {
     const int r = e / L, y = e % L;
@@ -492,15 +539,23 @@ __global__ void __launch_bounds__(GeoY<T, L>::NT, GeoY<T, L>::MINB) k_y2_argle(c
   if (RESID && threadIdx.x == 0) {  // fixed order: deterministic
     double a = 0, b = 0, d = 0;
     for (int t = 0; t < G::NT; ++t) { a += red[0][t]; b += red[1][t]; d += red[2][t]; }
-    part[blockIdx.x * 3 + 0] = a;
-    part[blockIdx.x * 3 + 1] = b;
-    part[blockIdx.x * 3 + 2] = d;
+    part[tile * 3 + 0] = a;
+    part[tile * 3 + 1] = b;
+    part[tile * 3 + 2] = d;
   }
   fft_rows<T, L, G::R, G::NT, +1>(s, tw);
   for (int e = threadIdx.x; e < G::R * L; e += G::NT) {
     const int r = e % G::R, y = e / G::R;
     Ta[(size_t)y * nx + x0 + r] = s[r * G::LP + pidx(y)];
   }
+}
+
+template <typename T, int L, bool RESID>
+__global__ void __launch_bounds__(GeoY<T, L>::NT, GeoY<T, L>::MINB) k_y2_argle(const cplx<T>* __restrict__ Td, cplx<T>* __restrict__ kpsi,
+                                                         cplx<T>* __restrict__ Ta, const cplx<T>* __restrict__ tw,
+                                                         double* __restrict__ part, StepConsts c) {
+  extern __shared__ __align__(16) unsigned char smraw[];
+  y2_argle_body<T, L, GeoY<T, L>, RESID>(Td, kpsi, Ta, tw, part, c, blockIdx.x, reinterpret_cast<cplx<T>*>(smraw));
 }
 
 // Sum per-CTA partials in a fixed order (deterministic) into out[0..2].

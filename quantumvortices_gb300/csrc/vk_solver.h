@@ -25,11 +25,31 @@ class SolverBase {
   virtual int64_t launches() const = 0;
   virtual int timing_begin() = 0;
   virtual int timing_end(int cap, char* tags, double* ms, int64_t* counts, int* ntags) = 0;
+  // Ensemble support: copy this field's device view (a Field<T>), query and
+  // update the state flags around batched steps.
+  virtual int field_view(void* out, size_t size) = 0;
+  virtual bool kpsi_is_masked() const = 0;
+  virtual void mark_rk4_done() = 0;
 };
 
 // Factories (one per precision, each in its own translation unit).
 SolverBase* make_solver_f64(const vk_params& p, int* status);
 SolverBase* make_solver_f32(const vk_params& p, int* status);
+
+// Ensembles of independent fields stepped by batched persistent kernels.
+class EnsembleBase {
+ public:
+  virtual ~EnsembleBase() {}
+  virtual int set_psi(int m, const double* psi) = 0;
+  virtual int get_psi(int m, double* psi) = 0;
+  virtual int rk4(int nsteps) = 0;
+  virtual const char* report() const = 0;
+  virtual void* stream() = 0;
+  virtual int64_t launches() const = 0;
+  virtual int size() const = 0;
+};
+EnsembleBase* make_ensemble_f64(const vk_params* p, int n, int* status);
+EnsembleBase* make_ensemble_f32(const vk_params* p, int n, int* status);
 
 // Host helpers shared by both precisions (vk_host.cpp).
 void twiddle_table(int n, double* out_interleaved);      // exp(-2 pi i k/n), k < n

@@ -43,21 +43,6 @@ template <typename F> bool with_len(int n, F&& f) {
   }
 }
 
-// Opt in to more than 48 KB of shared memory per CTA when static + dynamic
-// shared memory of `fn` needs it (once per kernel).
-inline void ensure_smem_attr(const void* fn, size_t dyn_bytes) {
-  static std::mutex mu;
-  static std::unordered_set<const void*> done;
-  std::lock_guard<std::mutex> g(mu);
-  if (done.count(fn)) return;
-  cudaFuncAttributes a;
-  size_t stat = 0;
-  if (cudaFuncGetAttributes(&a, fn) == cudaSuccess) stat = a.sharedSizeBytes;
-  if (stat + dyn_bytes > 48 * 1024)
-    cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)(227 * 1024 - stat));
-  done.insert(fn);
-}
-
 template <typename T> __global__ void k_from_f64(const double2* __restrict__ in, cplx<T>* __restrict__ out, size_t n) {
   for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
     out[i] = mkc<T>(T(in[i].x), T(in[i].y));
@@ -206,6 +191,23 @@ class Solver : public SolverBase {
   }
 
   void* stream() override { return (void*)st_; }
+  int field_view(void* out, size_t size) override {
+    if (size != sizeof(Field<T>)) {
+      set_error("field_view: size mismatch");
+      return VK_E_INVALID;
+    }
+    Field<T> f;
+    f.psi = psi_; f.kpsi = kpsi_; f.str1 = str1_; f.str2 = str2_;
+    f.Ta = Ta_; f.Tb = Tb_; f.Tc = Tc_; f.Td = Td_;
+    f.twx = twx_; f.twy = twy_; f.c = c_;
+    std::memcpy(out, &f, sizeof(f));
+    return VK_OK;
+  }
+  bool kpsi_is_masked() const override { return kpsi_masked_; }
+  void mark_rk4_done() override {
+    kpsi_masked_ = true;
+    ta_ = TA_PRUNED;
+  }
   int64_t launches() const override { return launches_; }
 
   // ---------------------------------------------------------------- I/O --

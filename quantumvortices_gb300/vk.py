@@ -103,6 +103,14 @@ def load_library(path: str | None = None) -> C.CDLL:
         "vk_write_wf": (C.c_int, [C.c_char_p, C.c_int32, C.c_double, C.c_double, C.c_int32, C.c_int32, dp]),
         "vk_read_wf": (C.c_int, [C.c_char_p, C.c_int32, C.c_int32, C.POINTER(C.c_int32), dp, dp, dp]),
         "vk_ic_vortices": (C.c_int, [C.c_int32, C.c_int32, C.c_int32, C.c_uint64, C.c_double, C.c_double, dp, dp]),
+        "vk_ens_init": (C.c_int, [C.POINTER(VkParams), C.c_int32, C.POINTER(vp)]),
+        "vk_ens_finalize": (C.c_int, [vp]),
+        "vk_ens_set_psi": (C.c_int, [vp, C.c_int32, dp]),
+        "vk_ens_get_psi": (C.c_int, [vp, C.c_int32, dp]),
+        "vk_ens_gpe_rk4": (C.c_int, [vp, C.c_int32]),
+        "vk_ens_report": (C.c_int, [vp, C.c_char_p, C.c_int32]),
+        "vk_ens_get_stream": (C.c_int, [vp, C.POINTER(vp)]),
+        "vk_ens_kernel_launches": (C.c_int, [vp, C.POINTER(C.c_int64)]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(lib, name)
@@ -320,4 +328,67 @@ class GPESolver:
     def launches(self) -> int:
         n = C.c_int64()
         _check(self.lib.vk_kernel_launches(self._h, C.byref(n)), "vk_kernel_launches")
+        return int(n.value)
+
+
+class Ensemble:
+    """Independent fields of uneven sizes stepped together (batched
+    persistent kernels, one CUDA graph per RK4 step)."""
+
+    def __init__(self, params: list):
+        self.lib = load_library()
+        self.params = list(params)
+        arr = (VkParams * len(self.params))(*self.params)
+        h = C.c_void_p()
+        _check(self.lib.vk_ens_init(arr, len(self.params), C.byref(h)), "vk_ens_init")
+        self._h = h
+
+    def close(self) -> None:
+        if getattr(self, "_h", None) is not None and self._h.value:
+            _check(self.lib.vk_ens_finalize(self._h), "vk_ens_finalize")
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def set_psi(self, m: int, psi: np.ndarray) -> None:
+        a = np.ascontiguousarray(psi, dtype=np.complex128)
+        p = self.params[m]
+        assert a.shape == (p.ny, p.nx)
+        _check(self.lib.vk_ens_set_psi(self._h, m, _dptr(a.view(np.float64))), "vk_ens_set_psi")
+
+    def get_psi(self, m: int) -> np.ndarray:
+        p = self.params[m]
+        a = np.empty((p.ny, p.nx), dtype=np.complex128)
+        _check(self.lib.vk_ens_get_psi(self._h, m, _dptr(a.view(np.float64))), "vk_ens_get_psi")
+        return a
+
+    def gpe_rk4(self, nsteps: int = 1) -> None:
+        _check(self.lib.vk_ens_gpe_rk4(self._h, nsteps), "vk_ens_gpe_rk4")
+
+    @property
+    def report(self) -> str:
+        buf = C.create_string_buffer(2048)
+        _check(self.lib.vk_ens_report(self._h, buf, 2048), "vk_ens_report")
+        return buf.value.decode()
+
+    @property
+    def stream(self) -> int:
+        s = C.c_void_p()
+        _check(self.lib.vk_ens_get_stream(self._h, C.byref(s)), "vk_ens_get_stream")
+        return int(s.value or 0)
+
+    @property
+    def launches(self) -> int:
+        n = C.c_int64()
+        _check(self.lib.vk_ens_kernel_launches(self._h, C.byref(n)), "vk_ens_kernel_launches")
         return int(n.value)
