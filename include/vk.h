@@ -135,6 +135,11 @@ int vk_get_stream(void* ctx, void** stream);
 /* Number of kernels this context has launched so far. */
 int vk_kernel_launches(void* ctx, int64_t* count);
 
+/* New (no reference counterpart): the vk_ic_vortices state computed on the
+ * GPU in FP64 (for large grids), then loaded as by vk_set_psi.  pos_out
+ * [2*n_vort] may be NULL. */
+int vk_set_psi_vortices(void* ctx, int32_t n_vort, uint64_t seed, double xi0, double min_sep, double* pos_out);
+
 /* Ensembles (new, no reference counterpart; BASELINE configs[3]): n
  * independent fields of uneven sizes (nx, ny in {128, 256, 512, 1024}, one
  * precision, no particles) stepped together.  Each RK4 pass is one

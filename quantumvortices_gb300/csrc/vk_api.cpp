@@ -176,3 +176,9 @@ extern "C" int vk_timing_end(void* ctx, int32_t cap, char* tags, double* total_m
   *ntags = n;
   return rc;
 }
+
+extern "C" int vk_set_psi_vortices(void* ctx, int32_t n_vort, uint64_t seed, double xi0, double min_sep,
+                                   double* pos_out) {
+  VK_CTX_OR_FAIL(ctx);
+  return c->s->set_psi_vortices(n_vort, seed, xi0, min_sep, pos_out);
+}

@@ -128,4 +128,66 @@ __global__ void k_part_update(PartState ps, PartConsts c, int stage) {
   }
 }
 
+// Seeded neutral vortex state on the device (FP64), same mathematics as the
+// host vk_ic_vortices: amplitude prod_j A(r_j) with the periodic minimum-image
+// distance, phase prod_j theta_1((z - z_j)/2 | e^{-pi})^{q_j} / |..| times
+// exp(-i y S/(2 pi)), S = sum_j q_j x_j.
+__global__ void k_ic_vortices(double2* __restrict__ out, int nx, int ny, const double* __restrict__ vx,
+                              const double* __restrict__ vy, const int* __restrict__ vq, int nv, double xi0,
+                              double S) {
+  const double two_pi = 6.283185307179586476925286766559, pi = two_pi / 2;
+  const double qn = exp(-pi);
+  double q2n[10];
+  for (int n = 1; n <= 9; ++n) q2n[n] = pow(qn, 2.0 * n);
+  const size_t np = (size_t)nx * ny;
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < np; i += (size_t)gridDim.x * blockDim.x) {
+    const int y = (int)(i / nx), x = (int)(i % nx);
+    const double xx = x * (two_pi / nx), yy = y * (two_pi / ny);
+    double amp = 1.0, pr = 1.0, pim = 0.0;
+    for (int j = 0; j < nv; ++j) {
+      const double ddx = xx - vx[j], ddy = yy - vy[j];
+      double wx = fmod(ddx, two_pi), wy = fmod(ddy, two_pi);
+      if (wx > pi) wx -= two_pi;
+      if (wx <= -pi) wx += two_pi;
+      if (wy > pi) wy -= two_pi;
+      if (wy <= -pi) wy += two_pi;
+      const double r = sqrt(wx * wx + wy * wy) / xi0;
+      amp *= r / sqrt(2.0 + r * r);
+      const double a = 0.5 * ddx, b = 0.5 * ddy;
+      double sa, ca;
+      sincos(a, &sa, &ca);
+      double fr = sa * cosh(b), fi = ca * sinh(b);
+      double s2, c2;
+      sincos(ddx, &s2, &c2);
+      const double em = exp(-ddy), ep = exp(ddy);
+      for (int n = 1; n <= 9; ++n) {
+        const double r1 = q2n[n] * em, r2 = q2n[n] * ep;
+        const double ar = 1.0 - r1 * c2, ai = -r1 * s2;
+        const double br = 1.0 - r2 * c2, bi = r2 * s2;
+        const double tr = ar * br - ai * bi, ti = ar * bi + ai * br;
+        const double nr = fr * tr - fi * ti, ni = fr * ti + fi * tr;
+        fr = nr;
+        fi = ni;
+      }
+      const double m = hypot(fr, fi);
+      if (m > 0) {
+        fr /= m;
+        fi /= m;
+      } else {
+        fr = 1.0;
+        fi = 0.0;
+      }
+      if (vq[j] < 0) fi = -fi;
+      const double nr = pr * fr - pim * fi, ni = pr * fi + pim * fr;
+      pr = nr;
+      pim = ni;
+    }
+    double sl, cl;
+    sincos(-yy * S / two_pi, &sl, &cl);
+    const double fr = pr * cl - pim * sl, fi = pr * sl + pim * cl;
+    const double m = hypot(fr, fi);
+    out[i] = make_double2(amp * fr / m, amp * fi / m);
+  }
+}
+
 }  // namespace vk

@@ -370,7 +370,8 @@ struct Diagnostics {
     int rc = alloc(S_);
     if (rc) return rc;
     const int nx = S_.nx_, ny = S_.ny_, K = S_.K_;
-    const StepConsts& c = S_.c_;
+    StepConsts c = S_.c_;
+    c.rho_bg = 0.0;  // the diagnostics need P_G rho itself
     // 1. gradients
     for (int axis = 0; axis < 2; ++axis) {
       with_len(ny, [&](auto lc) {

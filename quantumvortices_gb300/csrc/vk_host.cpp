@@ -315,15 +315,15 @@ inline double wrap_pi(double d) {  // into (-pi, pi]
 // contributes arg theta_1((z - z_j)/2 | q = e^{-pi}) (the odd Jacobi theta
 // function, zeros exactly at the periodic images of z_j), and the linear
 // term -y * sum_j q_j x_j / (2 pi) cancels the quasi-periodicity in y.
-extern "C" int vk_ic_vortices(int32_t nx, int32_t ny, int32_t n_vort, uint64_t seed, double xi0, double min_sep,
-                              double* psi, double* pos_out) {
-  if (!psi || nx <= 0 || ny <= 0 || n_vort < 0 || (n_vort % 2) != 0 || !(xi0 > 0)) {
-    set_error("vk_ic_vortices: need an even (neutral) vortex count, positive xi0 and a grid");
-    return VK_E_INVALID;
-  }
+namespace vk {
+// Seeded neutral vortex positions: SplitMix64(seed) uniform on [0,2pi)^2,
+// periodic minimum separation min_sep; charge +1 for the first half, -1 after.
+int vortex_positions(int n_vort, uint64_t seed, double min_sep, std::vector<double>& px, std::vector<double>& py,
+                     std::vector<int>& qc) {
   const double L = 2.0 * kPi;
-  std::vector<double> px(n_vort), py(n_vort);
-  std::vector<int> qc(n_vort);
+  px.assign(n_vort, 0.0);
+  py.assign(n_vort, 0.0);
+  qc.assign(n_vort, 0);
   SplitMix64 rng{seed};
   for (int j = 0; j < n_vort; ++j) {
     int tries = 0;
@@ -336,12 +336,27 @@ extern "C" int vk_ic_vortices(int32_t nx, int32_t ny, int32_t n_vort, uint64_t s
       }
       if (ok) { px[j] = x; py[j] = y; break; }
       if (++tries > 1000000) {
-        set_error("vk_ic_vortices: cannot place vortices with this minimum separation");
+        set_error("vortex IC: cannot place vortices with this minimum separation");
         return VK_E_INVALID;
       }
     }
     qc[j] = (j < n_vort / 2) ? +1 : -1;
   }
+  return VK_OK;
+}
+}  // namespace vk
+
+extern "C" int vk_ic_vortices(int32_t nx, int32_t ny, int32_t n_vort, uint64_t seed, double xi0, double min_sep,
+                              double* psi, double* pos_out) {
+  if (!psi || nx <= 0 || ny <= 0 || n_vort < 0 || (n_vort % 2) != 0 || !(xi0 > 0)) {
+    set_error("vk_ic_vortices: need an even (neutral) vortex count, positive xi0 and a grid");
+    return VK_E_INVALID;
+  }
+  const double L = 2.0 * kPi;
+  std::vector<double> px, py;
+  std::vector<int> qc;
+  int prc = vk::vortex_positions(n_vort, seed, min_sep, px, py, qc);
+  if (prc) return prc;
   double S = 0.0;
   for (int j = 0; j < n_vort; ++j) S += qc[j] * px[j];
   const int NT = 9;  // theta product terms: q^{2n} e^{2 pi} < 1e-20 for n = 9

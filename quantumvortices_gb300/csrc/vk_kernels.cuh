@@ -82,6 +82,12 @@ struct StepConsts {
   double alpha, g, omega, dt;
   double prefac_re, prefac_im;   // (1 - i*disp_factor)/i
   double scale;      // 1/(nx*ny)
+  // Background density moved out of the FFTs: the passes transform
+  // rho - rho_bg and add g*rho_bg back analytically in Fourier space
+  // (g P_G rho psi = g P_G(rho - rho_bg) psi + g rho_bg psi, F[psi] = kpsi).
+  // 0 on the plain FP64 path (the reference's arithmetic); Omega/g on the
+  // FP32 path, where it removes the large cancelling g psi / Omega kpsi pair.
+  double rho_bg;
 };
 
 // Device view of one field's buffers and constants (ensemble work items
@@ -256,7 +262,8 @@ __device__ __forceinline__ void x1_body(const cplx<T>* __restrict__ Ta, cplx<T>*
     const int e = threadIdx.x + q * G::NT;
     const int p = e / L, x = e % L;
     const C a = s[(2 * p) * G::LP + pidx(x)], b = s[(2 * p + 1) * G::LP + pidx(x)];
-    z[q] = mkc<T>(a.x * a.x + a.y * a.y, b.x * b.x + b.y * b.y);
+    const T bg = T(c.rho_bg);
+    z[q] = mkc<T>(a.x * a.x + a.y * a.y - bg, b.x * b.x + b.y * b.y - bg);
   }
   __syncthreads();
 #pragma unroll
@@ -448,7 +455,7 @@ __device__ __forceinline__ void y2_rk4_body(const cplx<T>* __restrict__ Td, cplx
     if (ksq <= c.k2max) {
       const C ps = kpsi[gi];
       const C nh = s[r * G::LP + pidx(ky)];
-      const T kin = al * T(ksq) - om;
+      const T kin = al * T(ksq) - (om - T(c.g * c.rho_bg));
       const C t = mkc<T>(kin * ps.x + nh.x, kin * ps.y + nh.y);
       const C rhs = mkc<T>(pr * t.x - pi_ * t.y, pr * t.y + pi_ * t.x);
       if (STAGE == 1) {
@@ -516,7 +523,8 @@ __device__ __forceinline__ void y2_argle_body(const cplx<T>* __restrict__ Td, cp
     const size_t gi = (size_t)(x0 + r) * L + ky;
     const C old = kpsi[gi];
     const C nh = s[r * G::LP + pidx(ky)];
-    const C t1 = mkc<T>(nh.x + om * old.x, nh.y + om * old.y);
+    const T omb = om - T(c.g * c.rho_bg);
+    const C t1 = mkc<T>(nh.x + omb * old.x, nh.y + omb * old.y);
     const T t2 = T(1) + al * T(k1 * k1 + k2 * k2) * dt;
     C nw = mkc<T>(old.x + dt * t1.x, old.y + dt * t1.y);
     nw.x = nw.x / t2;
@@ -557,6 +565,11 @@ __global__ void __launch_bounds__(GeoY<T, L>::NT, GeoY<T, L>::MINB) k_y2_argle(c
   extern __shared__ __align__(16) unsigned char smraw[];
   y2_argle_body<T, L, GeoY<T, L>, RESID>(Td, kpsi, Ta, tw, part, c, blockIdx.x, reinterpret_cast<cplx<T>*>(smraw));
 }
+
+// Seeded vortex state (vk_common.cu).
+__global__ void k_ic_vortices(double2* __restrict__ out, int nx, int ny, const double* __restrict__ vx,
+                              const double* __restrict__ vy, const int* __restrict__ vq, int nv, double xi0,
+                              double S);
 
 // Sum per-CTA partials in a fixed order (deterministic) into out[0..2].
 __global__ void k_reduce_partials3(const double* __restrict__ part, int nblk, double* __restrict__ out);

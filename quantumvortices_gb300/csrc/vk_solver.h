@@ -2,6 +2,7 @@
 #pragma once
 #include <string>
 #include <cstdint>
+#include <vector>
 #include "../../include/vk.h"
 
 namespace vk {
@@ -14,6 +15,7 @@ class SolverBase {
   virtual ~SolverBase() {}
   virtual int set_psi(const double* psi) = 0;
   virtual int set_kpsi(const double* kpsi) = 0;
+  virtual int set_psi_vortices(int n_vort, uint64_t seed, double xi0, double min_sep, double* pos_out) = 0;
   virtual int get_psi(double* psi) = 0;
   virtual int get_kpsi(double* kpsi) = 0;
   virtual int rk4(int nsteps) = 0;
@@ -55,5 +57,7 @@ EnsembleBase* make_ensemble_f32(const vk_params* p, int n, int* status);
 void twiddle_table(int n, double* out_interleaved);      // exp(-2 pi i k/n), k < n
 int k2max_for(int nx);                                     // largest k1^2+k2^2 kept by the 2/3 rule
 int kmax_for(int k2max);                                   // largest |k| with k^2 <= k2max
+int vortex_positions(int n_vort, uint64_t seed, double min_sep, std::vector<double>& px,
+                     std::vector<double>& py, std::vector<int>& qc);
 
 }  // namespace vk

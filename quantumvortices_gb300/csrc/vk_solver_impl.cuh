@@ -137,6 +137,7 @@ class Solver : public SolverBase {
     c_.prefac_re = -p_.disp_factor;
     c_.prefac_im = -1.0;
     c_.scale = 1.0 / ((double)nx_ * (double)ny_);
+    c_.rho_bg = std::is_same<T, double>::value ? 0.0 : (p_.gstrength != 0.0 ? p_.omega_chem / p_.gstrength : 0.0);
     if (p_.n_particles > 0) {
       int prc = init_particles();
       if (prc) return prc;
@@ -214,6 +215,51 @@ class Solver : public SolverBase {
   int set_psi(const double* psi) override {
     int rc = upload(psi, psi_);
     if (rc) return rc;
+    return set_psi_on_device();
+  }
+  // New (no reference counterpart): the seeded vortex state computed on the
+  // device, then the same path as set_psi.
+  int set_psi_vortices(int n_vort, uint64_t seed, double xi0, double min_sep, double* pos_out) override {
+    if (n_vort < 0 || (n_vort % 2) != 0 || !(xi0 > 0)) {
+      set_error("vk_set_psi_vortices: need an even (neutral) vortex count and positive xi0");
+      return VK_E_INVALID;
+    }
+    std::vector<double> px, py;
+    std::vector<int> q;
+    int rc = vortex_positions(n_vort, seed, min_sep, px, py, q);
+    if (rc) return rc;
+    double S = 0.0;
+    for (int j = 0; j < n_vort; ++j) S += q[j] * px[j];
+    double *dx = nullptr, *dy = nullptr;
+    int* dq = nullptr;
+    const size_t nv = (size_t)std::max(n_vort, 1);
+    VK_CUDA_TRY(cudaMalloc(&dx, sizeof(double) * nv));
+    VK_CUDA_TRY(cudaMalloc(&dy, sizeof(double) * nv));
+    VK_CUDA_TRY(cudaMalloc(&dq, sizeof(int) * nv));
+    if (n_vort > 0) {
+      VK_CUDA_TRY(cudaMemcpyAsync(dx, px.data(), sizeof(double) * n_vort, cudaMemcpyHostToDevice, st_));
+      VK_CUDA_TRY(cudaMemcpyAsync(dy, py.data(), sizeof(double) * n_vort, cudaMemcpyHostToDevice, st_));
+      VK_CUDA_TRY(cudaMemcpyAsync(dq, q.data(), sizeof(int) * n_vort, cudaMemcpyHostToDevice, st_));
+    }
+    launch_raw("k_ic_vortices", k_ic_vortices, 152 * 8, 256, 0, (double2*)stage64_, nx_, ny_, (const double*)dx,
+               (const double*)dy, (const int*)dq, n_vort, xi0, S);
+    if (std::is_same<T, double>::value)
+      VK_CUDA_TRY(cudaMemcpyAsync(psi_, stage64_, n2_ * sizeof(double2), cudaMemcpyDeviceToDevice, st_));
+    else
+      launch_simple("k_from_f64", k_from_f64<T>, (const double2*)stage64_, psi_, n2_);
+    rc = sync_check();
+    cudaFree(dx);
+    cudaFree(dy);
+    cudaFree(dq);
+    if (rc) return rc;
+    if (pos_out)
+      for (int j = 0; j < n_vort; ++j) {
+        pos_out[2 * j] = px[j];
+        pos_out[2 * j + 1] = py[j];
+      }
+    return set_psi_on_device();
+  }
+  int set_psi_on_device() {
     fwd2d(psi_, kpsi_, p_.otoc != 0);
     if (p_.otoc) {
       inv2d(kpsi_, psi_, true);

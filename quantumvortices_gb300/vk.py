@@ -103,6 +103,7 @@ def load_library(path: str | None = None) -> C.CDLL:
         "vk_write_wf": (C.c_int, [C.c_char_p, C.c_int32, C.c_double, C.c_double, C.c_int32, C.c_int32, dp]),
         "vk_read_wf": (C.c_int, [C.c_char_p, C.c_int32, C.c_int32, C.POINTER(C.c_int32), dp, dp, dp]),
         "vk_ic_vortices": (C.c_int, [C.c_int32, C.c_int32, C.c_int32, C.c_uint64, C.c_double, C.c_double, dp, dp]),
+        "vk_set_psi_vortices": (C.c_int, [vp, C.c_int32, C.c_uint64, C.c_double, C.c_double, dp]),
         "vk_ens_init": (C.c_int, [C.POINTER(VkParams), C.c_int32, C.POINTER(vp)]),
         "vk_ens_finalize": (C.c_int, [vp]),
         "vk_ens_set_psi": (C.c_int, [vp, C.c_int32, dp]),
@@ -257,6 +258,14 @@ class GPESolver:
         a = np.ascontiguousarray(psi, dtype=np.complex128)
         assert a.shape == (self.ny, self.nx)
         _check(self.lib.vk_set_psi(self._h, _dptr(a.view(np.float64))), "vk_set_psi")
+
+    def set_psi_vortices(self, n_vort: int, seed: int, xi0: float | None = None, min_sep: float = 0.0):
+        """Seeded vortex state computed on the GPU (same as ic_vortices), then set_psi."""
+        if xi0 is None:
+            xi0 = math.sqrt(2.0) * 2.0 * math.pi / self.nx
+        pos = np.empty((max(n_vort, 1), 2))
+        _check(self.lib.vk_set_psi_vortices(self._h, n_vort, seed, xi0, min_sep, _dptr(pos)), "vk_set_psi_vortices")
+        return pos[:n_vort]
 
     def set_kpsi(self, kpsi: np.ndarray) -> None:
         a = np.ascontiguousarray(kpsi, dtype=np.complex128)

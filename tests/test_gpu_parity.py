@@ -153,3 +153,27 @@ def test_kernel_launch_count_and_timing():
     assert {"k_x1", "k_y1", "k_x2", "k_y2_rk4"} <= set(t)
     assert t["k_x2"][1] == 8
     s.close()
+
+
+def test_device_vortex_ic_matches_host():
+    n = 128
+    p = vk.params_for(n, otoc=False)
+    psi_h, pos_h = vk.ic_vortices(n, n, 16, seed=21, min_sep=0.3)
+    with vk.GPESolver(p) as s:
+        pos_d = s.set_psi_vortices(16, seed=21, min_sep=0.3)
+        assert np.array_equal(pos_d, pos_h)
+        assert rel(s.get_psi(), psi_h) < 1e-13
+
+
+def test_4096_fp32_vs_fp64_with_1024_vortices():
+    """configs[3] second part: one 4096^2 field with 1024 vortices, FP32 bulk
+    against plain FP64 after 100 RK4 steps."""
+    n = 4096
+    out = {}
+    for prec in (vk.VK_PREC_FP64, vk.VK_PREC_FP32):
+        with vk.GPESolver(vk.params_for(n, dt=5e-4, precision=prec)) as s:
+            s.set_psi_vortices(1024, seed=5, min_sep=4 * np.sqrt(2) * 2 * np.pi / n)
+            s.gpe_rk4(100)
+            out[prec] = s.get_psi()
+    assert np.isfinite(out[vk.VK_PREC_FP64]).all()
+    assert rel(out[vk.VK_PREC_FP32], out[vk.VK_PREC_FP64]) < 1e-5
