@@ -155,6 +155,23 @@ int vk_ens_report(void* ens, char* buf, int32_t cap);
 int vk_ens_get_stream(void* ens, void** stream);
 int vk_ens_kernel_launches(void* ens, int64_t* count);
 
+/* Learned ARGLE warm-start network (new, no reference counterpart).  A
+ * periodic conv encoder-decoder (levels, channels base*2^l, 3x3 convs) on
+ * h x w grids with BF16 weights/activations and FP32 accumulation; every
+ * convolution (forward, data and weight gradient) runs on tcgen05 tensor
+ * cores.  Tensors passed in are DEVICE FP32 planar arrays: input [3][h][w]
+ * (Re/Im of the phase ansatz, signed vortex-charge density), output and
+ * target [2][h][w] (Re/Im correction).  Parameters are one FP32 vector,
+ * per conv W[cout][9][cin] then b[cout]. */
+int vk_nn_create(int32_t h, int32_t w, int32_t base, int32_t levels, uint64_t seed, void** net);
+int vk_nn_destroy(void* net);
+int vk_nn_num_params(void* net, int64_t* n);
+int vk_nn_get_params(void* net, float* host, int64_t n);
+int vk_nn_set_params(void* net, const float* host, int64_t n);
+int vk_nn_forward(void* net, const float* in_dev, float* out_dev, void* stream);
+int vk_nn_loss_grad(void* net, const float* in_dev, const float* target_dev, double* loss_out, float* grad_host);
+int vk_nn_train_step(void* net, const float* in_dev, const float* target_dev, float lr, double* loss_out);
+
 /* Per-kernel timing.  Between vk_timing_begin and vk_timing_end every kernel
  * this context launches is bracketed by CUDA events on the context's stream;
  * vk_timing_end synchronises and returns, per kernel tag (NUL-terminated,

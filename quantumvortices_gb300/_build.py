@@ -14,8 +14,9 @@ PKG = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(PKG, "csrc")
 OUT_DIR = os.path.join(PKG, "_build")
 LIB = os.path.join(PKG, "libvk.so")
+DRIVER = os.path.join(PKG, "vikshobha_gb300")
 
-CU_SRCS = ["vk_f64.cu", "vk_f32.cu", "vk_common.cu", "vk_noalloc.cu", "vk_ens.cu"]
+CU_SRCS = ["vk_f64.cu", "vk_f32.cu", "vk_common.cu", "vk_noalloc.cu", "vk_ens.cu", "vk_nn.cu"]
 CPP_SRCS = ["vk_api.cpp", "vk_host.cpp"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC,-fopenmp",
@@ -66,6 +67,9 @@ def build(verbose: bool = False, jobs: int | None = None) -> str:
             list(ex.map(_run, cmds))
     if cmds or not os.path.exists(LIB):
         _run([nvcc, *ARCH, "-shared", "-o", LIB, *objs, "-Xcompiler", "-fopenmp", "-lgomp"])
+    drv_src = os.path.join(CSRC, "vk_driver.cpp")
+    if not os.path.exists(DRIVER) or os.path.getmtime(DRIVER) < max(os.path.getmtime(drv_src), os.path.getmtime(LIB)):
+        _run([cxx, "-O2", "-std=c++17", "-o", DRIVER, drv_src, "-L" + PKG, "-lvk", "-Wl,-rpath,$ORIGIN"])
     if verbose:
         print("built", LIB)
     return LIB

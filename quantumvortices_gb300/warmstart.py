@@ -1,0 +1,296 @@
+"""Learned ARGLE warm-start (new; the reference has no machine learning).
+
+A conv encoder-decoder (libvk's tcgen05 BF16 kernels, vk_nn_*) maps the
+seeded vortex phase ansatz plus a signed vortex-charge density to a
+correction of the ansatz; ARGLE (vk_argle) then continues from the
+corrected field.  Training data are generated by the solver itself:
+each sample is (ansatz, ARGLE-relaxed state).
+"""
+from __future__ import annotations
+
+import ctypes as C
+import math
+import time
+
+import numpy as np
+
+from . import vk
+
+
+class WarmStartNet:
+    def __init__(self, h: int, w: int, base: int = 32, levels: int = 4, seed: int = 1):
+        self.lib = vk.load_library()
+        L = self.lib
+        dp, vp = C.POINTER(C.c_double), C.c_void_p
+        fp = C.POINTER(C.c_float)
+        for name, res, args in [
+            ("vk_nn_create", C.c_int, [C.c_int32, C.c_int32, C.c_int32, C.c_int32, C.c_uint64, C.POINTER(vp)]),
+            ("vk_nn_destroy", C.c_int, [vp]),
+            ("vk_nn_num_params", C.c_int, [vp, C.POINTER(C.c_int64)]),
+            ("vk_nn_get_params", C.c_int, [vp, fp, C.c_int64]),
+            ("vk_nn_set_params", C.c_int, [vp, fp, C.c_int64]),
+            ("vk_nn_forward", C.c_int, [vp, C.c_void_p, C.c_void_p, vp]),
+            ("vk_nn_loss_grad", C.c_int, [vp, C.c_void_p, C.c_void_p, dp, fp]),
+            ("vk_nn_train_step", C.c_int, [vp, C.c_void_p, C.c_void_p, C.c_float, dp]),
+        ]:
+            f = getattr(L, name)
+            f.restype, f.argtypes = res, args
+        self.h, self.w, self.base, self.levels = h, w, base, levels
+        hnd = C.c_void_p()
+        vk._check(L.vk_nn_create(h, w, base, levels, seed, C.byref(hnd)), "vk_nn_create")
+        self._h = hnd
+        n = C.c_int64()
+        vk._check(L.vk_nn_num_params(self._h, C.byref(n)), "vk_nn_num_params")
+        self.nparam = int(n.value)
+
+    def close(self):
+        if getattr(self, "_h", None) is not None and self._h.value:
+            vk._check(self.lib.vk_nn_destroy(self._h), "vk_nn_destroy")
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def get_params(self) -> np.ndarray:
+        a = np.empty(self.nparam, dtype=np.float32)
+        vk._check(self.lib.vk_nn_get_params(self._h, a.ctypes.data_as(C.POINTER(C.c_float)), self.nparam), "get")
+        return a
+
+    def set_params(self, a: np.ndarray) -> None:
+        a = np.ascontiguousarray(a, dtype=np.float32)
+        vk._check(self.lib.vk_nn_set_params(self._h, a.ctypes.data_as(C.POINTER(C.c_float)), self.nparam), "set")
+
+    def forward(self, inp_dev, out_dev) -> None:
+        """inp_dev/out_dev: torch CUDA float32 tensors [3,h,w] / [2,h,w]."""
+        vk._check(self.lib.vk_nn_forward(self._h, inp_dev.data_ptr(), out_dev.data_ptr(), None), "vk_nn_forward")
+
+    def loss_grad(self, inp_dev, tgt_dev):
+        loss = C.c_double()
+        g = np.empty(self.nparam, dtype=np.float32)
+        vk._check(self.lib.vk_nn_loss_grad(self._h, inp_dev.data_ptr(), tgt_dev.data_ptr(), C.byref(loss),
+                                           g.ctypes.data_as(C.POINTER(C.c_float))), "vk_nn_loss_grad")
+        return float(loss.value), g
+
+    def train_step(self, inp_dev, tgt_dev, lr: float, want_loss: bool = False):
+        loss = C.c_double()
+        vk._check(self.lib.vk_nn_train_step(self._h, inp_dev.data_ptr(), tgt_dev.data_ptr(), lr,
+                                            C.byref(loss) if want_loss else None), "vk_nn_train_step")
+        return float(loss.value) if want_loss else None
+
+
+def features(n: int, pos: np.ndarray, psi_ansatz: np.ndarray, width: float) -> np.ndarray:
+    """[3, n, n]: Re/Im of the ansatz and a signed vortex-charge density
+    (periodic Gaussians of the given width, + for the first half of `pos`)."""
+    nv = len(pos)
+    x = np.arange(n) * 2 * np.pi / n
+    X, Y = np.meshgrid(x, x)
+    q = np.zeros((n, n))
+    for j in range(nv):
+        dx = (X - pos[j, 0] + np.pi) % (2 * np.pi) - np.pi
+        dy = (Y - pos[j, 1] + np.pi) % (2 * np.pi) - np.pi
+        q += (1.0 if j < nv // 2 else -1.0) * np.exp(-(dx * dx + dy * dy) / (2 * width * width))
+    return np.stack([psi_ansatz.real, psi_ansatz.imag, q]).astype(np.float32)
+
+
+def _torch():
+    import torch  # device memory and plumbing only; the network runs in libvk
+    return torch
+
+
+def features_device(n: int, pos: np.ndarray, psi_ansatz, width: float):
+    """features() on the GPU with torch tensors (psi_ansatz: complex numpy)."""
+    torch = _torch()
+    nv = len(pos)
+    x = torch.arange(n, device="cuda", dtype=torch.float32) * (2 * math.pi / n)
+    q = torch.zeros((n, n), device="cuda", dtype=torch.float32)
+    if nv:
+        px = torch.tensor(pos[:, 0], device="cuda", dtype=torch.float32)[:, None]
+        py = torch.tensor(pos[:, 1], device="cuda", dtype=torch.float32)[:, None]
+        sg = torch.tensor([1.0 if j < nv // 2 else -1.0 for j in range(nv)], device="cuda")[:, None, None]
+        dx = torch.remainder(x[None, :] - px + math.pi, 2 * math.pi) - math.pi   # [nv, n] along x
+        dy = torch.remainder(x[None, :] - py + math.pi, 2 * math.pi) - math.pi   # [nv, n] along y
+        gx = torch.exp(-dx * dx / (2 * width * width))
+        gy = torch.exp(-dy * dy / (2 * width * width))
+        q = (sg * gy[:, :, None] * gx[:, None, :]).sum(0)
+    a = torch.from_numpy(np.stack([psi_ansatz.real, psi_ansatz.imag]).astype(np.float32)).cuda()
+    return torch.cat([a, q[None]], 0).contiguous()
+
+
+class DataGen:
+    """Solver-generated training pairs: (features, relaxed - ansatz)."""
+
+    def __init__(self, n: int, relax_steps: int = 1000, dt: float = 1e-3, precision: int = vk.VK_PREC_FP32):
+        self.n, self.relax, self.dt = n, relax_steps, dt
+        self.params = vk.params_for(n, dt=dt, precision=precision, otoc=True)
+        self.solver = vk.GPESolver(self.params)
+        dx = 2 * math.pi / n
+        self.xi0 = math.sqrt(2.0) * dx
+        self.width = 2.0 * self.xi0
+
+    def ansatz(self, nv: int, seed: int):
+        pos = self.solver.set_psi_vortices(nv, seed, self.xi0, min_sep=4 * self.xi0)
+        return pos, self.solver.get_psi()
+
+    def sample(self, nv: int, seed: int):
+        torch = _torch()
+        pos, psi0 = self.ansatz(nv, seed)
+        self.solver.argle(self.relax)
+        # relaxed state = F^-1[kpsi] (psi itself is one step behind after ARGLE)
+        kpsi = self.solver.get_kpsi()
+        relaxed = np.fft.ifft2(kpsi.T)
+        feat = features_device(self.n, pos, psi0, self.width)
+        tgt = torch.from_numpy(np.stack([(relaxed - psi0).real, (relaxed - psi0).imag]).astype(np.float32)).cuda()
+        return feat, tgt
+
+    def close(self):
+        self.solver.close()
+
+
+def vortex_count(rng) -> int:
+    return int(rng.integers(4, 65)) * 2  # 8..128, even (neutral)
+
+
+def train(net: WarmStartNet, gen: DataGen, n_train: int, epochs: int, lr: float, seed0: int = 10_000,
+          log=print):
+    """Generates n_train samples (seeds seed0..seed0+n_train-1) and trains."""
+    torch = _torch()
+    rng = np.random.default_rng(seed0)
+    data = []
+    t0 = time.perf_counter()
+    for i in range(n_train):
+        data.append(gen.sample(vortex_count(rng), seed0 + i))
+    torch.cuda.synchronize()
+    tgen = time.perf_counter() - t0
+    log(f"generated {n_train} ARGLE-relaxed {gen.n}^2 samples in {tgen:.1f} s")
+    t0 = time.perf_counter()
+    hist = []
+    order = np.arange(n_train)
+    for ep in range(epochs):
+        rng.shuffle(order)
+        tot = 0.0
+        for k, i in enumerate(order):
+            l = net.train_step(data[i][0], data[i][1], lr * (0.5 ** ep), want_loss=(k % 16 == 0))
+            if l is not None:
+                tot += l
+        hist.append(tot / max(1, (n_train + 15) // 16))
+        log(f"epoch {ep}: mean sampled loss {hist[-1]:.4e}")
+    torch.cuda.synchronize()
+    return {"gen_s": tgen, "train_s": time.perf_counter() - t0, "loss": hist}
+
+
+def steps_to(solver: vk.GPESolver, target: float, max_steps: int, chunk: int = 10):
+    """ARGLE in chunks until the last-step residual <= target; returns
+    (steps, residual).  Residual = ||kpsi_new-kpsi_old||/(dt ||kpsi_old||)."""
+    steps, r = 0, float("inf")
+    while steps < max_steps:
+        r = solver.argle(chunk)
+        steps += chunk
+        if r <= target:
+            break
+    return steps, r
+
+
+def _timed_argle(gen: DataGen, psi, steps: int) -> float:
+    torch = _torch()
+    gen.solver.set_psi(psi)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    gen.solver.argle(steps)
+    return time.perf_counter() - t0
+
+
+def evaluate(net: WarmStartNet, gen: DataGen, seeds, log=print):
+    """Plain ARGLE from the ansatz vs ARGLE from the network's warm start.
+    Target residual per seed: what plain ARGLE reaches after gen.relax steps
+    (the configured relaxation length).  Times are wall times of one
+    vk_argle call of the needed length (warm start: plus the network)."""
+    torch = _torch()
+    rng = np.random.default_rng(12345)
+    out = []
+    s = gen.solver
+    n = gen.n
+    corr = torch.empty((2, n, n), device="cuda", dtype=torch.float32)
+    for seed in seeds:
+        nv = vortex_count(rng)
+        pos, psi0 = gen.ansatz(nv, seed)
+        r_target = s.argle(gen.relax)
+        e_plain = s.diagnostics_gpe().etot
+        gen.ansatz(nv, seed)
+        k_plain, _ = steps_to(s, r_target, gen.relax)
+        feat = features_device(n, pos, psi0, gen.width)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        net.forward(feat, corr)
+        c = corr.cpu().numpy()
+        t_net = time.perf_counter() - t0
+        warm = psi0 + (c[0] + 1j * c[1])
+        s.set_psi(warm)
+        k_warm, r_warm = steps_to(s, r_target, 4 * gen.relax)
+        t_plain = _timed_argle(gen, psi0, k_plain)
+        t_warm = _timed_argle(gen, warm, k_warm) + t_net
+        s.set_psi(warm)
+        s.argle(gen.relax)
+        e_warm = s.diagnostics_gpe().etot
+        # energy criterion: steps until E <= plain's energy after gen.relax steps
+        s.set_psi(warm)
+        k_e, chunk = 0, max(10, gen.relax // 20)
+        while k_e < 4 * gen.relax:
+            s.argle(chunk)
+            k_e += chunk
+            if s.diagnostics_gpe().etot <= e_plain:
+                break
+        out.append({"seed": int(seed), "nv": nv, "r_target": r_target, "plain_steps": k_plain,
+                    "warm_steps": k_warm, "warm_reached": bool(r_warm <= r_target), "plain_s": t_plain,
+                    "warm_s": t_warm, "net_s": t_net, "energy_plain": e_plain, "energy_warm_same_steps": e_warm,
+                    "warm_steps_to_plain_energy": k_e})
+        log(out[-1])
+    return out
+
+
+def summarize(rows):
+    ps = np.array([r["plain_steps"] for r in rows], float)
+    ws = np.array([r["warm_steps"] for r in rows], float)
+    pt = np.array([r["plain_s"] for r in rows])
+    wt = np.array([r["warm_s"] for r in rows])
+    de = np.array([abs(r["energy_warm_same_steps"] - r["energy_plain"]) / abs(r["energy_plain"]) for r in rows])
+    return {"seeds": len(rows), "plain_steps_mean": float(ps.mean()), "warm_steps_mean": float(ws.mean()),
+            "iterations_saved_frac": float(1 - ws.sum() / ps.sum()), "plain_s_mean": float(pt.mean()),
+            "warm_s_mean": float(wt.mean()), "time_ratio_warm_over_plain": float(wt.sum() / pt.sum()),
+            "reached_frac": float(np.mean([r["warm_reached"] for r in rows])),
+            "rel_energy_diff_same_steps_mean": float(de.mean()),
+            "warm_steps_to_plain_energy_mean": float(np.mean([r["warm_steps_to_plain_energy"] for r in rows]))}
+
+
+def main(argv=None):
+    import argparse
+    import json
+    ap = argparse.ArgumentParser(description="train and evaluate the learned ARGLE warm start")
+    ap.add_argument("--n", type=int, default=512)
+    ap.add_argument("--relax", type=int, default=1000)
+    ap.add_argument("--train", type=int, default=512)
+    ap.add_argument("--eval", type=int, default=32)
+    ap.add_argument("--epochs", type=int, default=3)
+    ap.add_argument("--base", type=int, default=32)
+    ap.add_argument("--levels", type=int, default=4)
+    ap.add_argument("--lr", type=float, default=1e-3)
+    ap.add_argument("--out", default=None)
+    a = ap.parse_args(argv)
+    gen = DataGen(a.n, a.relax)
+    net = WarmStartNet(a.n, a.n, a.base, a.levels, seed=1)
+    tr = train(net, gen, a.train, a.epochs, a.lr)
+    held = list(range(900_000, 900_000 + a.eval))  # disjoint from the training seeds
+    rows = evaluate(net, gen, held)
+    res = {"config": vars(a), "train": tr, "summary": summarize(rows), "rows": rows}
+    print(json.dumps(res["summary"]))
+    if a.out:
+        with open(a.out, "w") as f:
+            json.dump(res, f, indent=1)
+    net.close()
+    gen.close()
+
+
+if __name__ == "__main__":
+    main()

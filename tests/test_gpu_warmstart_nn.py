@@ -1,0 +1,65 @@
+"""tcgen05 BF16 network kernels (forward, data and weight gradients) against
+the CPU restatement oracle/nn_oracle.py, which mirrors the BF16 rounding
+points; tolerances are relative L2: output 1e-2, gradient 2e-2 (BF16)."""
+import numpy as np
+import pytest
+
+from oracle import nn_oracle
+from quantumvortices_gb300.warmstart import WarmStartNet
+
+pytestmark = pytest.mark.gpu
+
+
+def rel(a, b):
+    return float(np.linalg.norm(a - b) / np.linalg.norm(b))
+
+
+def _data(h, seed=0):
+    torch = pytest.importorskip("torch")
+    rng = np.random.default_rng(seed)
+    inp = rng.standard_normal((3, h, h)).astype(np.float32)
+    tgt = (0.3 * rng.standard_normal((2, h, h))).astype(np.float32)
+    return inp, tgt, torch.from_numpy(inp).cuda(), torch.from_numpy(tgt).cuda()
+
+
+@pytest.mark.parametrize("h,base,levels", [(32, 16, 2), (64, 16, 3), (64, 32, 4)])
+def test_forward_matches_oracle(h, base, levels):
+    torch = pytest.importorskip("torch")
+    net = WarmStartNet(h, h, base, levels, seed=3)
+    inp, tgt, di, dt = _data(h)
+    out = torch.empty((2, h, h), dtype=torch.float32, device="cuda")
+    net.forward(di, out)
+    ref, _ = nn_oracle.forward(net.get_params().astype(np.float64), inp.astype(np.float64), base, levels)
+    assert rel(out.cpu().numpy(), ref) < 1e-2
+    net.close()
+
+
+@pytest.mark.parametrize("h,base,levels", [(32, 16, 2), (64, 16, 3)])
+def test_gradient_matches_oracle(h, base, levels):
+    net = WarmStartNet(h, h, base, levels, seed=5)
+    inp, tgt, di, dt = _data(h, seed=1)
+    loss, g = net.loss_grad(di, dt)
+    rloss, rg = nn_oracle.loss_grad(net.get_params().astype(np.float64), inp.astype(np.float64),
+                                    tgt.astype(np.float64), base, levels)
+    assert abs(loss - rloss) <= 1e-2 * rloss
+    assert rel(g, rg) < 2e-2
+    # per layer
+    o = 0
+    for ci, co, _ in nn_oracle.layers(base, levels):
+        n = co * 9 * ci
+        assert rel(g[o:o + n], rg[o:o + n]) < 5e-2, (ci, co)
+        o += n + co
+    net.close()
+
+
+def test_training_reduces_loss():
+    """Adam on a learnable map (half of the first two input channels)."""
+    torch = pytest.importorskip("torch")
+    net = WarmStartNet(64, 64, 16, 3, seed=7)
+    inp, _, di, _ = _data(64, seed=2)
+    dt = (0.5 * di[:2]).contiguous()
+    l0 = net.train_step(di, dt, 2e-3, want_loss=True)
+    for _ in range(150):
+        last = net.train_step(di, dt, 2e-3, want_loss=True)
+    assert last < 0.3 * l0, (l0, last)
+    net.close()

@@ -228,3 +228,28 @@ def test_vortex_count_of_seeded_state():
     o = Oracle(n)
     o.set_psi(psi0, otoc=False)
     assert o.count_vortices() == (4, 4)
+
+
+def test_nn_oracle_gradient_by_finite_differences():
+    """The CPU restatement of the warm-start network: exact-arithmetic
+    gradient against central differences."""
+    from oracle import nn_oracle as nn
+    nn.EXACT = True
+    try:
+        base, levels, H = 16, 2, 8
+        rng = np.random.default_rng(0)
+        n = sum(co * 9 * ci + co for ci, co, _ in nn.layers(base, levels))
+        params = rng.standard_normal(n) * 0.2
+        inp = rng.standard_normal((3, H, H))
+        tgt = rng.standard_normal((2, H, H))
+        loss, g = nn.loss_grad(params, inp, tgt, base, levels)
+        idx = rng.choice(n, 12, replace=False)
+        for i in idx:
+            e = np.zeros(n)
+            e[i] = 1e-6
+            lp, _ = nn.loss_grad(params + e, inp, tgt, base, levels)
+            lm, _ = nn.loss_grad(params - e, inp, tgt, base, levels)
+            fd = (lp - lm) / 2e-6
+            assert abs(fd - g[i]) <= 1e-5 * max(1.0, abs(fd)), (i, fd, g[i])
+    finally:
+        nn.EXACT = False
