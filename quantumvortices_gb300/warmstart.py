@@ -178,7 +178,28 @@ def train(net: WarmStartNet, gen: DataGen, n_train: int, epochs: int, lr: float,
         hist.append(tot / max(1, (n_train + 15) // 16))
         log(f"epoch {ep}: mean sampled loss {hist[-1]:.4e}")
     torch.cuda.synchronize()
-    return {"gen_s": tgen, "train_s": time.perf_counter() - t0, "loss": hist}
+    ts = time.perf_counter() - t0
+    fl = train_flops(net)
+    return {"gen_s": tgen, "train_s": ts, "loss": hist, "flops_per_step": fl,
+            "tensor_tflops": fl * n_train * epochs / ts / 1e12}
+
+
+def train_flops(net: WarmStartNet) -> float:
+    """Multiply-add FLOPs of one training step's convolutions (forward, data
+    and weight gradients; the first layer has no data gradient)."""
+    b, L = net.base, net.levels
+    convs = [(3, b, 0), (b, b, 0)]
+    for lv in range(1, L):
+        convs += [(b << (lv - 1), b << lv, lv), (b << lv, b << lv, lv)]
+    for lv in range(L - 2, -1, -1):
+        convs += [(b << (lv + 1), b << lv, lv), (b << lv, b << lv, lv)]
+    convs.append((b, 2, 0))
+    tot = 0.0
+    for i, (ci, co, lv) in enumerate(convs):
+        npix = (net.h >> lv) * (net.w >> lv)
+        f = 2.0 * npix * 9 * ci * co
+        tot += f * (2 if i == 0 else 3)
+    return tot
 
 
 def steps_to(solver: vk.GPESolver, target: float, max_steps: int, chunk: int = 10):
@@ -202,11 +223,23 @@ def _timed_argle(gen: DataGen, psi, steps: int) -> float:
     return time.perf_counter() - t0
 
 
+def _grand(d) -> float:
+    """The functional ARGLE descends: E - Omega N = etot - echem in the
+    reference's normalisation (etot = egrad + eintr alone is not monotone
+    under ARGLE, because the norm is free)."""
+    return d.etot - d.echem
+
+
 def evaluate(net: WarmStartNet, gen: DataGen, seeds, log=print):
     """Plain ARGLE from the ansatz vs ARGLE from the network's warm start.
-    Target residual per seed: what plain ARGLE reaches after gen.relax steps
-    (the configured relaxation length).  Times are wall times of one
-    vk_argle call of the needed length (warm start: plus the network)."""
+
+    Residual criterion: the residual plain ARGLE reaches after gen.relax
+    steps (the configured relaxation length); both starts run ARGLE in
+    chunks of 10 until they reach it.  Times are wall times of one vk_argle
+    call of the needed length (warm start: plus the network and its copy).
+    Energy criterion: the ARGLE functional E - Omega N after gen.relax steps
+    from either start, and the steps the warm start needs to reach plain
+    ARGLE's value (chunks of gen.relax // 20, capped at 4 * gen.relax)."""
     torch = _torch()
     rng = np.random.default_rng(12345)
     out = []
@@ -217,7 +250,8 @@ def evaluate(net: WarmStartNet, gen: DataGen, seeds, log=print):
         nv = vortex_count(rng)
         pos, psi0 = gen.ansatz(nv, seed)
         r_target = s.argle(gen.relax)
-        e_plain = s.diagnostics_gpe().etot
+        d = s.diagnostics_gpe()
+        e_plain, f_plain = d.etot, _grand(d)
         gen.ansatz(nv, seed)
         k_plain, _ = steps_to(s, r_target, gen.relax)
         feat = features_device(n, pos, psi0, gen.width)
@@ -233,19 +267,20 @@ def evaluate(net: WarmStartNet, gen: DataGen, seeds, log=print):
         t_warm = _timed_argle(gen, warm, k_warm) + t_net
         s.set_psi(warm)
         s.argle(gen.relax)
-        e_warm = s.diagnostics_gpe().etot
-        # energy criterion: steps until E <= plain's energy after gen.relax steps
+        d = s.diagnostics_gpe()
+        e_warm, f_warm = d.etot, _grand(d)
         s.set_psi(warm)
-        k_e, chunk = 0, max(10, gen.relax // 20)
-        while k_e < 4 * gen.relax:
+        k_f, chunk = 0, max(10, gen.relax // 20)
+        while k_f < 4 * gen.relax:
             s.argle(chunk)
-            k_e += chunk
-            if s.diagnostics_gpe().etot <= e_plain:
+            k_f += chunk
+            if _grand(s.diagnostics_gpe()) <= f_plain:
                 break
         out.append({"seed": int(seed), "nv": nv, "r_target": r_target, "plain_steps": k_plain,
                     "warm_steps": k_warm, "warm_reached": bool(r_warm <= r_target), "plain_s": t_plain,
                     "warm_s": t_warm, "net_s": t_net, "energy_plain": e_plain, "energy_warm_same_steps": e_warm,
-                    "warm_steps_to_plain_energy": k_e})
+                    "grand_plain": f_plain, "grand_warm_same_steps": f_warm,
+                    "warm_steps_to_plain_grand": k_f})
         log(out[-1])
     return out
 
@@ -256,12 +291,17 @@ def summarize(rows):
     pt = np.array([r["plain_s"] for r in rows])
     wt = np.array([r["warm_s"] for r in rows])
     de = np.array([abs(r["energy_warm_same_steps"] - r["energy_plain"]) / abs(r["energy_plain"]) for r in rows])
+    dg = np.array([(r["grand_warm_same_steps"] - r["grand_plain"]) / abs(r["grand_plain"]) for r in rows])
+    kf = np.array([r["warm_steps_to_plain_grand"] for r in rows], float)
     return {"seeds": len(rows), "plain_steps_mean": float(ps.mean()), "warm_steps_mean": float(ws.mean()),
             "iterations_saved_frac": float(1 - ws.sum() / ps.sum()), "plain_s_mean": float(pt.mean()),
             "warm_s_mean": float(wt.mean()), "time_ratio_warm_over_plain": float(wt.sum() / pt.sum()),
+            "time_ratio_median": float(np.median(wt / pt)),
             "reached_frac": float(np.mean([r["warm_reached"] for r in rows])),
             "rel_energy_diff_same_steps_mean": float(de.mean()),
-            "warm_steps_to_plain_energy_mean": float(np.mean([r["warm_steps_to_plain_energy"] for r in rows]))}
+            "rel_grand_diff_same_steps_mean": float(dg.mean()),
+            "grand_lower_frac": float(np.mean(dg <= 0)),
+            "warm_steps_to_plain_grand_median": float(np.median(kf))}
 
 
 def main(argv=None):
