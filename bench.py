@@ -143,6 +143,13 @@ def kernel_flops(tag, n, K):
     return None if rows is None else rows * f
 
 
+def precision_errors(d32, d64):
+    """FP32-bulk diagnostics against the FP64 path's (same state, same steps)."""
+    return {"rel_err_energy": abs(d32.etot - d64.etot) / abs(d64.etot),
+            "rel_err_norm": abs(d32.norm - d64.norm) / abs(d64.norm),
+            "rel_l2_err_spectra": float(np.linalg.norm(d32.spec - d64.spec) / np.linalg.norm(d64.spec))}
+
+
 def fp64_peak_tflops(torch):
     """FP64 throughput of cuBLAS DGEMM (4096^3) on this GPU, TFLOP/s."""
     a = torch.randn(4096, 4096, dtype=torch.float64, device="cuda")
@@ -199,13 +206,20 @@ def ensemble_bench(torch, K, W, S):
         s64.set_psi(psi)
         s64.gpe_rk4(100)
         ref = s64.get_psi()
+        d64 = s64.diagnostics_gpe()
         s64.close()
-        errs[f"member{m}_{n}"] = float(np.linalg.norm(ens.get_psi(m) - ref) / np.linalg.norm(ref))
+        got = ens.get_psi(m)
+        ev = vk.GPESolver(vk.params_for(n, dt=5e-4, precision=vk.VK_PREC_FP64, otoc=False))
+        ev.set_psi(got)  # diagnostics of the member's state, evaluated in FP64
+        d32 = ev.diagnostics_gpe()
+        ev.close()
+        errs[f"member{m}_{n}"] = {"rel_l2_psi": float(np.linalg.norm(got - ref) / np.linalg.norm(ref)),
+                                  **precision_errors(d32, d64)}
     report = ens.report
     ens.close()
     return {"value": pts * S * K / (ms * 1e-3), "unit": UNIT, "members": "192 x 256^2 + 48 x 512^2",
             "grid_points": pts, "ms_per_rk4_step": ms / (K * S), "gpu_launches": launches,
-            "rel_l2_psi_vs_fp64_after_100_steps": errs, "autotune": report}
+            "errors_vs_fp64_after_100_steps": errs, "autotune": report}
 
 
 def grid4096_bench(torch, steps=5):
@@ -215,7 +229,7 @@ def grid4096_bench(torch, steps=5):
     n = 4096
     xi0 = math.sqrt(2) * 2 * math.pi / n
     out = {}
-    psis = {}
+    psis, diags = {}, {}
     for nm, prec in (("fp64", vk.VK_PREC_FP64), ("fp32", vk.VK_PREC_FP32)):
         s = vk.GPESolver(vk.params_for(n, dt=5e-4, precision=prec))
         s.set_psi_vortices(1024, 11, xi0, min_sep=4 * xi0)
@@ -231,10 +245,12 @@ def grid4096_bench(torch, steps=5):
         s.set_psi_vortices(1024, 11, xi0, min_sep=4 * xi0)
         s.gpe_rk4(100)
         psis[nm] = s.get_psi()
+        diags[nm] = s.diagnostics_gpe()
         s.close()
     a, b = psis["fp32"], psis["fp64"]
     out["unit"] = UNIT
     out["rel_l2_psi_fp32_vs_fp64_after_100_steps"] = float(np.linalg.norm(a - b) / np.linalg.norm(b))
+    out.update(precision_errors(diags["fp32"], diags["fp64"]))
     return out
 
 
@@ -329,10 +345,12 @@ def run_ours(args, rank, world, local_rank):
         s32.set_psi(psi0)
         s32.gpe_rk4(100)
         a = s32.get_psi()
+        d32 = s32.diagnostics_gpe()
         s64 = vk.GPESolver(p)
         s64.set_psi(psi0)
         s64.gpe_rk4(100)
         b = s64.get_psi()
+        d64 = s64.diagnostics_gpe()
         s32.timing_begin()
         s32.gpe_rk4(S)
         per32 = s32.timing_end()
@@ -340,6 +358,7 @@ def run_ours(args, rank, world, local_rank):
         s64.close()
         fp32 = {"value": world * n * n * S * K / (ms32 * 1e-3), "unit": UNIT, "ms_per_step": ms32 / K,
                 "rel_l2_psi_vs_fp64_after_100_steps": float(np.linalg.norm(a - b) / np.linalg.norm(b)),
+                **precision_errors(d32, d64),
                 "kernel_ms": {k: round(v[0] / v[1], 5) for k, v in per32.items()}}
 
     ens = None if args.no_ensemble else ensemble_bench(torch, K, W, S)

@@ -73,6 +73,34 @@ __device__ __forceinline__ int kwn(int i, int n) { return i < n / 2 ? i : i - n;
 // Row index of logical row l when only |kx| <= K rows are processed.
 __device__ __forceinline__ int pruned_row(int l, int K, int n) { return l <= K ? l : n - (2 * K + 1 - l); }
 
+// Stage NR rows of L values into shared memory (pitch LP, padded index):
+// s[r][k] = fetch(r, k).  Every thread holds PER = NR*L/NT elements; the
+// global loads of a batch are issued before any of them is stored, so a
+// thread has up to 16 loads in flight instead of one load per round trip.
+template <typename T, int L, int NR, int NT, int LP, class F>
+__device__ __forceinline__ void stage_rows(cplx<T>* __restrict__ s, F fetch) {
+  constexpr int PER = NR * L / NT;
+  static_assert(NR * L % NT == 0, "threads tile the rows");
+  // FP64 passes are DFMA-bound and short of registers: one element at a time
+  constexpr int BMAX = sizeof(T) == 4 ? 16 : 1;
+  constexpr int B = PER < BMAX ? PER : BMAX;
+  constexpr int UNR = sizeof(T) == 4 ? PER / B : 1;
+#pragma unroll UNR
+  for (int q0 = 0; q0 < PER; q0 += B) {
+    cplx<T> v[B];
+#pragma unroll
+    for (int j = 0; j < B; ++j) {
+      const int e = threadIdx.x + (q0 + j) * NT;
+      v[j] = fetch(e / L, e % L);
+    }
+#pragma unroll
+    for (int j = 0; j < B; ++j) {
+      const int e = threadIdx.x + (q0 + j) * NT;
+      s[(e / L) * LP + pidx(e % L)] = v[j];
+    }
+  }
+}
+
 // Scalars shared by the passes (by value in the launch).
 struct StepConsts {
   int nx, ny;        // grid
@@ -111,10 +139,7 @@ __global__ void __launch_bounds__(GeoX<T, L>::NT, GeoX<T, L>::MINB) k_xfwd(const
   extern __shared__ __align__(16) unsigned char smraw[];
   C* s = reinterpret_cast<C*>(smraw);
   const int y0 = blockIdx.x * G::R;
-  for (int e = threadIdx.x; e < G::R * L; e += G::NT) {
-    const int r = e / L, x = e % L;
-    s[r * G::LP + pidx(x)] = src[(size_t)(y0 + r) * L + x];
-  }
+  stage_rows<T, L, G::R, G::NT, G::LP>(s, [&](int r, int x) { return src[(size_t)(y0 + r) * L + x]; });
   __syncthreads();
   fft_rows<T, L, G::R, G::NT, -1>(s, tw);
   for (int e = threadIdx.x; e < G::R * L; e += G::NT) {
@@ -134,10 +159,7 @@ __global__ void __launch_bounds__(GeoY<T, L>::NT, GeoY<T, L>::MINB) k_yfwd(const
   extern __shared__ __align__(16) unsigned char smraw[];
   C* s = reinterpret_cast<C*>(smraw);
   const int x0 = blockIdx.x * G::R;
-  for (int e = threadIdx.x; e < G::R * L; e += G::NT) {
-    const int r = e / L, y = e % L;
-    s[r * G::LP + pidx(y)] = src[(size_t)(x0 + r) * L + y];
-  }
+  stage_rows<T, L, G::R, G::NT, G::LP>(s, [&](int r, int y) { return src[(size_t)(x0 + r) * L + y]; });
   __syncthreads();
   fft_rows<T, L, G::R, G::NT, -1>(s, tw);
   for (int e = threadIdx.x; e < G::R * L; e += G::NT) {
@@ -164,10 +186,7 @@ __global__ void __launch_bounds__(GeoY<T, L>::NT, GeoY<T, L>::MINB) k_yinv(const
   extern __shared__ __align__(16) unsigned char smraw[];
   C* s = reinterpret_cast<C*>(smraw);
   const int x0 = blockIdx.x * G::R;
-  for (int e = threadIdx.x; e < G::R * L; e += G::NT) {
-    const int r = e / L, y = e % L;
-    s[r * G::LP + pidx(y)] = src[(size_t)(x0 + r) * L + y];
-  }
+  stage_rows<T, L, G::R, G::NT, G::LP>(s, [&](int r, int y) { return src[(size_t)(x0 + r) * L + y]; });
   __syncthreads();
   fft_rows<T, L, G::R, G::NT, +1>(s, tw);
   for (int e = threadIdx.x; e < G::R * L; e += G::NT) {
@@ -183,12 +202,11 @@ __device__ __forceinline__ void xinv_body(const cplx<T>* __restrict__ src, cplx<
                                                      const cplx<T>* __restrict__ tw, T scale, int K, const int tile, cplx<T>* __restrict__ s) {
   typedef cplx<T> C;
   const int y0 = tile * G::R;
-  for (int e = threadIdx.x; e < G::R * L; e += G::NT) {
-    const int r = e / L, k = e % L;
+  stage_rows<T, L, G::R, G::NT, G::LP>(s, [&](int r, int k) {
     C v = mkc<T>(T(0), T(0));
     if (!PRUNE || k <= K || k >= L - K) v = src[(size_t)(y0 + r) * L + k];
-    s[r * G::LP + pidx(k)] = v;
-  }
+    return v;
+  });
   __syncthreads();
   fft_rows<T, L, G::R, G::NT, +1>(s, tw);
   for (int e = threadIdx.x; e < G::R * L; e += G::NT) {
@@ -230,12 +248,11 @@ __device__ __forceinline__ void x1_body(const cplx<T>* __restrict__ Ta, cplx<T>*
   const int y0 = tile * G::R;
   const int ny = c.ny, K = c.K;
   if (FROM_T) {
-    for (int e = threadIdx.x; e < G::R * L; e += G::NT) {
-      const int r = e / L, k = e % L;
+    stage_rows<T, L, G::R, G::NT, G::LP>(s, [&](int r, int k) {
       C v = mkc<T>(T(0), T(0));
       if (!PRUNE || k <= K || k >= L - K) v = Ta[(size_t)(y0 + r) * L + k];
-      s[r * G::LP + pidx(k)] = v;
-    }
+      return v;
+    });
     __syncthreads();
     fft_rows<T, L, G::R, G::NT, +1>(s, tw);
     const T scale = T(c.scale);
@@ -246,10 +263,7 @@ __device__ __forceinline__ void x1_body(const cplx<T>* __restrict__ Ta, cplx<T>*
       psi[(size_t)(y0 + r) * L + x] = v;
     }
   } else {
-    for (int e = threadIdx.x; e < G::R * L; e += G::NT) {
-      const int r = e / L, x = e % L;
-      s[r * G::LP + pidx(x)] = psi[(size_t)(y0 + r) * L + x];
-    }
+    stage_rows<T, L, G::R, G::NT, G::LP>(s, [&](int r, int x) { return psi[(size_t)(y0 + r) * L + x]; });
   }
   __syncthreads();
   // rho for row pairs: z_p(x) = rho(x, y0+2p) + i rho(x, y0+2p+1), into row p.
@@ -304,12 +318,11 @@ __device__ __forceinline__ void y1_body(const cplx<T>* __restrict__ Tb, cplx<T>*
   typedef cplx<T> C;
   const int l0 = tile * G::R;
   const int K = c.K;
-  for (int e = threadIdx.x; e < G::R * L; e += G::NT) {
-    const int r = e / L, y = e % L;
+  stage_rows<T, L, G::R, G::NT, G::LP>(s, [&](int r, int y) {
     C v = mkc<T>(T(0), T(0));
     if (l0 + r <= K) v = Tb[(size_t)(l0 + r) * L + y];
-    s[r * G::LP + pidx(y)] = v;
-  }
+    return v;
+  });
   __syncthreads();
   fft_rows<T, L, G::R, G::NT, -1>(s, tw);
   for (int e = threadIdx.x; e < G::R * L; e += G::NT) {
@@ -347,8 +360,7 @@ __device__ __forceinline__ void x2_body(const cplx<T>* __restrict__ Tc, const cp
   const int K = c.K, ny = c.ny, pk = c.pk;
   constexpr int NPAIR = G::R / 2;
   // Z_p(k) = A(k) + i B(k) with the Hermitian extension to negative k.
-  for (int e = threadIdx.x; e < NPAIR * L; e += G::NT) {
-    const int p = e / L, k = e % L;
+  stage_rows<T, L, NPAIR, G::NT, G::LP>(s, [&](int p, int k) {
     C v = mkc<T>(T(0), T(0));
     const size_t ra = (size_t)(y0 + 2 * p) * pk, rb = ra + pk;
     if (k <= K) {
@@ -359,8 +371,8 @@ __device__ __forceinline__ void x2_body(const cplx<T>* __restrict__ Tc, const cp
       // conj(a) + i conj(b)
       v = mkc<T>(a.x + b.y, b.x - a.y);
     }
-    s[p * G::LP + pidx(k)] = v;
-  }
+    return v;
+  });
   __syncthreads();
   fft_rows<T, L, NPAIR, G::NT, +1, G::NT>(s, tw);
   constexpr int PER = G::R * L / G::NT;
@@ -429,12 +441,11 @@ __device__ __forceinline__ void y2_rk4_body(const cplx<T>* __restrict__ Td, cplx
   const int l0 = tile * G::R;
   const int K = c.K, nx = c.nx;
   const int nrow = 2 * K + 1;
-  for (int e = threadIdx.x; e < G::R * L; e += G::NT) {
-    const int r = e / L, y = e % L;
+  stage_rows<T, L, G::R, G::NT, G::LP>(s, [&](int r, int y) {
     C v = mkc<T>(T(0), T(0));
     if (l0 + r < nrow) v = Td[(size_t)pruned_row(l0 + r, K, nx) * L + y];
-    s[r * G::LP + pidx(y)] = v;
-  }
+    return v;
+  });
   __syncthreads();
   fft_rows<T, L, G::R, G::NT, -1>(s, tw);
   // Stage coefficients with the reference's evaluation order:
@@ -444,38 +455,57 @@ __device__ __forceinline__ void y2_rk4_body(const cplx<T>* __restrict__ Td, cplx
   const T c1 = T(STAGE == 3 ? c.dt : c.dt * 0.5);
   const T pr = T(c.prefac_re), pi_ = T(c.prefac_im);
   const T al = T(c.alpha), om = T(c.omega);
-  for (int e = threadIdx.x; e < G::R * L; e += G::NT) {
-    const int r = e / L, ky = e % L;
-    if (l0 + r >= nrow) continue;
-    const int kxi = pruned_row(l0 + r, K, nx);
-    const int k1 = kwn(kxi, nx), k2 = kwn(ky, L);
-    const int ksq = k1 * k1 + k2 * k2;
-    const size_t gi = (size_t)kxi * L + ky;
-    C nw = mkc<T>(T(0), T(0));
-    if (ksq <= c.k2max) {
-      const C ps = kpsi[gi];
-      const C nh = s[r * G::LP + pidx(ky)];
-      const T kin = al * T(ksq) - (om - T(c.g * c.rho_bg));
-      const C t = mkc<T>(kin * ps.x + nh.x, kin * ps.y + nh.y);
-      const C rhs = mkc<T>(pr * t.x - pi_ * t.y, pr * t.y + pi_ * t.x);
-      if (STAGE == 1) {
-        str1[gi] = ps;
-        str2[gi] = mkc<T>(c2 * rhs.x, c2 * rhs.y);
-        nw = mkc<T>(ps.x + c1 * rhs.x, ps.y + c1 * rhs.y);
-      } else {
-        const C s1 = str1[gi];
-        C s2 = str2[gi];
-        s2 = mkc<T>(s2.x + c2 * rhs.x, s2.y + c2 * rhs.y);
-        if (STAGE < 4) {
-          str2[gi] = s2;
-          nw = mkc<T>(s1.x + c1 * rhs.x, s1.y + c1 * rhs.y);
-        } else {
-          nw = mkc<T>(s1.x + s2.x, s1.y + s2.y);
-        }
+  // batches of B elements per thread: all loads of a batch before any use
+  constexpr int PER = G::R * L / G::NT;
+  constexpr int B = sizeof(T) == 4 ? (PER < 8 ? PER : 8) : 1;
+  constexpr int UNR = sizeof(T) == 4 ? PER / B : 1;
+#pragma unroll UNR
+  for (int q0 = 0; q0 < PER; q0 += B) {
+    C ps[B], s1v[B], s2v[B];
+#pragma unroll
+    for (int j = 0; j < B; ++j) {
+      const int e = threadIdx.x + (q0 + j) * G::NT;
+      const int r = e / L, ky = e % L;
+      const bool act = l0 + r < nrow;
+      const size_t gi = act ? (size_t)pruned_row(l0 + r, K, nx) * L + ky : 0;
+      ps[j] = act ? kpsi[gi] : mkc<T>(T(0), T(0));
+      if (STAGE > 1) {
+        s1v[j] = act ? str1[gi] : mkc<T>(T(0), T(0));
+        s2v[j] = act ? str2[gi] : mkc<T>(T(0), T(0));
       }
     }
-    kpsi[gi] = nw;
-    s[r * G::LP + pidx(ky)] = nw;
+#pragma unroll
+    for (int j = 0; j < B; ++j) {
+      const int e = threadIdx.x + (q0 + j) * G::NT;
+      const int r = e / L, ky = e % L;
+      if (l0 + r >= nrow) continue;
+      const int kxi = pruned_row(l0 + r, K, nx);
+      const int k1 = kwn(kxi, nx), k2 = kwn(ky, L);
+      const int ksq = k1 * k1 + k2 * k2;
+      const size_t gi = (size_t)kxi * L + ky;
+      C nw = mkc<T>(T(0), T(0));
+      if (ksq <= c.k2max) {
+        const C nh = s[r * G::LP + pidx(ky)];
+        const T kin = al * T(ksq) - (om - T(c.g * c.rho_bg));
+        const C t = mkc<T>(kin * ps[j].x + nh.x, kin * ps[j].y + nh.y);
+        const C rhs = mkc<T>(pr * t.x - pi_ * t.y, pr * t.y + pi_ * t.x);
+        if (STAGE == 1) {
+          str1[gi] = ps[j];
+          str2[gi] = mkc<T>(c2 * rhs.x, c2 * rhs.y);
+          nw = mkc<T>(ps[j].x + c1 * rhs.x, ps[j].y + c1 * rhs.y);
+        } else {
+          const C s2 = mkc<T>(s2v[j].x + c2 * rhs.x, s2v[j].y + c2 * rhs.y);
+          if (STAGE < 4) {
+            str2[gi] = s2;
+            nw = mkc<T>(s1v[j].x + c1 * rhs.x, s1v[j].y + c1 * rhs.y);
+          } else {
+            nw = mkc<T>(s1v[j].x + s2.x, s1v[j].y + s2.y);
+          }
+        }
+      }
+      kpsi[gi] = nw;
+      s[r * G::LP + pidx(ky)] = nw;
+    }
   }
   __syncthreads();
   fft_rows<T, L, G::R, G::NT, +1>(s, tw);
@@ -509,19 +539,28 @@ __device__ __forceinline__ void y2_argle_body(const cplx<T>* __restrict__ Td, cp
   __shared__ double red[3][512];
   const int x0 = tile * G::R;
   const int nx = c.nx;
-  for (int e = threadIdx.x; e < G::R * L; e += G::NT) {
-    const int r = e / L, y = e % L;
-    s[r * G::LP + pidx(y)] = Td[(size_t)(x0 + r) * L + y];
-  }
+  stage_rows<T, L, G::R, G::NT, G::LP>(s, [&](int r, int y) { return Td[(size_t)(x0 + r) * L + y]; });
   __syncthreads();
   fft_rows<T, L, G::R, G::NT, -1>(s, tw);
   const T al = T(c.alpha), om = T(c.omega), dt = T(c.dt);
   double dsum = 0.0, osum = 0.0, nsum = 0.0;
-  for (int e = threadIdx.x; e < G::R * L; e += G::NT) {
+  constexpr int PER = G::R * L / G::NT;
+  constexpr int B = sizeof(T) == 4 ? (PER < 8 ? PER : 8) : 1;
+#pragma unroll 1
+  for (int q0 = 0; q0 < PER; q0 += B) {
+  C oldv[B];
+#pragma unroll
+  for (int j = 0; j < B; ++j) {
+    const int e = threadIdx.x + (q0 + j) * G::NT;
+    oldv[j] = kpsi[(size_t)(x0 + e / L) * L + e % L];
+  }
+#pragma unroll
+  for (int j = 0; j < B; ++j) {
+    const int e = threadIdx.x + (q0 + j) * G::NT;
     const int r = e / L, ky = e % L;
     const int k1 = kwn(x0 + r, nx), k2 = kwn(ky, L);
     const size_t gi = (size_t)(x0 + r) * L + ky;
-    const C old = kpsi[gi];
+    const C old = oldv[j];
     const C nh = s[r * G::LP + pidx(ky)];
     const T omb = om - T(c.g * c.rho_bg);
     const C t1 = mkc<T>(nh.x + omb * old.x, nh.y + omb * old.y);
@@ -537,6 +576,7 @@ __device__ __forceinline__ void y2_argle_body(const cplx<T>* __restrict__ Td, cp
       osum += (double)old.x * old.x + (double)old.y * old.y;
       nsum += (double)nw.x * nw.x + (double)nw.y * nw.y;
     }
+  }
   }
   if (RESID) {
     red[0][threadIdx.x] = dsum;

@@ -20,6 +20,7 @@
 #include <cstdint>
 #include <cstring>
 #include <string>
+#include <type_traits>
 #include <vector>
 #include "../../include/vk.h"
 #include "vk_solver.h"
@@ -33,85 +34,144 @@ typedef __nv_bfloat16 bf16;
 __device__ __forceinline__ int wrapi(int v, int n) { return v < 0 ? v + n : (v >= n ? v - n : v); }
 
 // ------------------------------------------------------------------ conv --
-// One CTA = 128 output pixels x BN channels.  CK = K columns per chunk.
+// Implicit-GEMM convolution, one CTA = 128 output pixels x BN output
+// channels (channel block blockIdx.y).  The reduction index kk = tap*Cin + ci
+// runs over 9*Cin in chunks of 64 (a chunk may span taps; the tail is
+// zero-filled), which is also the row layout of the weights [co][tap][ci], so
+// a weight tile is 64 contiguous values per output channel.  Operand tiles
+// stream through an S-stage shared-memory ring with cp.async (16-byte
+// vectors, 8 channels of one pixel); thread 0 issues the chunk's four
+// K = 16 MMAs and commits them to the stage's mbarrier, which frees the stage
+// for the copies S - 1 chunks ahead.  Every wait is bounded.
+constexpr int kConvStages = 3;
+
 template <int BN>
 __global__ void __launch_bounds__(128) k_conv(const bf16* __restrict__ in, int H, int W, int Cin,
-                                              const bf16* __restrict__ wgt, const float* __restrict__ bias, int relu,
-                                              bf16* __restrict__ out_bf, float* __restrict__ out_f, int nout,
-                                              int* __restrict__ err) {
+                                              const bf16* __restrict__ wgt, const float* __restrict__ bias,
+                                              int cout, int relu, bf16* __restrict__ out_bf, int ldo,
+                                              float* __restrict__ out_f, int nout, int* __restrict__ err) {
+  constexpr int S = kConvStages;
+  constexpr int ABYTES = 128 * 64 * 2, BBYTES = BN * 64 * 2, STAGE = ABYTES + BBYTES;
   extern __shared__ __align__(1024) unsigned char sm[];
-  const int CK = Cin < 64 ? Cin : 64;
-  unsigned char* sA = sm;                        // 128 x CK
-  unsigned char* sB = sm + 128 * 64 * 2;         // BN x CK
-  __shared__ __align__(8) uint64_t bar;
+  __shared__ __align__(8) uint64_t bar[S];
   __shared__ uint32_t tslot;
   const int tid = threadIdx.x, warp = tid >> 5;
   const int npix = H * W;
-  const int p0 = blockIdx.x * 128;
+  const int p0 = blockIdx.x * 128, n0 = blockIdx.y * BN;
+  const int KT = 9 * Cin, nck = (KT + 63) / 64;
   constexpr uint32_t NCOL = BN < 32 ? 32 : BN;
   if (warp == 0) tc::tmem_alloc(&tslot, NCOL);
-  if (tid == 0) tc::mbar_init(&bar);
+  if (tid < S) tc::mbar_init(&bar[tid]);
   tc::fence_before();
   __syncthreads();
   tc::fence_after();
   const uint32_t taddr = tslot;
   const uint32_t idesc = tc::idesc_bf16(128, BN);
-  uint32_t phase = 0;
-  bool first = true;
-  const int vpr = CK / 8;  // 16-byte vectors per tile row
-  for (int tap = 0; tap < 9; ++tap) {
-    const int dy = tap / 3 - 1, dx = tap % 3 - 1;
-    for (int c0 = 0; c0 < Cin; c0 += CK) {
-      for (int i = tid; i < 128 * vpr; i += 128) {
-        const int r = i / vpr, kv = i % vpr;
-        const int p = p0 + r;
-        uint4 v = make_uint4(0, 0, 0, 0);
-        if (p < npix) {
-          const int y = p / W, x = p % W;
-          const int src = wrapi(y + dy, H) * W + wrapi(x + dx, W);
-          v = *reinterpret_cast<const uint4*>(in + (size_t)src * Cin + c0 + 8 * kv);
-        }
-        *reinterpret_cast<uint4*>(sA + tc::tile_off(r, 8 * kv, CK)) = v;
-      }
-      for (int i = tid; i < BN * vpr; i += 128) {
-        const int r = i / vpr, kv = i % vpr;
-        const uint4 v = *reinterpret_cast<const uint4*>(wgt + ((size_t)r * 9 + tap) * Cin + c0 + 8 * kv);
-        *reinterpret_cast<uint4*>(sB + tc::tile_off(r, 8 * kv, CK)) = v;
-      }
-      tc::fence_async_smem();
-      tc::fence_before();
-      __syncthreads();
-      tc::fence_after();
-      if (tid == 0) {
-        for (int j = 0; j < CK / 16; ++j) {
-          const uint64_t ad = tc::smem_desc(tc::smem_u32(sA) + j * 256, 128, (CK / 8) * 128);
-          const uint64_t bd = tc::smem_desc(tc::smem_u32(sB) + j * 256, 128, (CK / 8) * 128);
-          tc::mma(taddr, ad, bd, idesc, first ? 0u : 1u);
-          first = false;
-        }
-        tc::commit(&bar);
-      }
-      tc::mbar_wait(&bar, phase, err);
-      phase ^= 1;
-      tc::fence_after();
-    }
+  // this thread's A vectors: column kv = tid & 7 of rows tid/8 + 16 j
+  const int kv = tid & 7;
+  int py[8], px[8];
+  bool pin[8];
+#pragma unroll
+  for (int j = 0; j < 8; ++j) {
+    const int p = p0 + (tid >> 3) + 16 * j;
+    pin[j] = p < npix;
+    py[j] = pin[j] ? p / W : 0;
+    px[j] = pin[j] ? p % W : 0;
   }
-  // epilogue
-  const int r = 32 * warp + (tid & 31);
-  const int p = p0 + r;
-  for (int c0 = 0; c0 < BN; c0 += (BN < 32 ? 16 : 32)) {
-    float v[32];
-    const uint32_t ta = taddr + ((uint32_t)(32 * warp) << 16) + c0;
-    if (BN < 32) tc::tmem_ld16(ta, v);
-    else tc::tmem_ld32(ta, v);
-    const int nc = BN < 32 ? 16 : 32;
-    if (p < npix) {
-      for (int j = 0; j < nc; ++j) {
-        const int c = c0 + j;
-        float a = v[j] + (bias ? bias[c] : 0.f);
-        if (relu) a = fmaxf(a, 0.f);
-        if (out_bf) out_bf[(size_t)p * BN + c] = __float2bfloat16(a);
-        if (out_f && c < nout) out_f[(size_t)p * nout + c] = a;
+  auto load_chunk = [&](int i, int buf) {
+    unsigned char* sA = sm + buf * STAGE;
+    unsigned char* sB = sA + ABYTES;
+    const int kk = i * 64 + 8 * kv;
+    const bool kin = kk < KT;
+    const int tap = kin ? kk / Cin : 0, ci = kin ? kk - tap * Cin : 0;
+    const int dy = tap / 3 - 1, dx = tap % 3 - 1;
+#pragma unroll
+    for (int j = 0; j < 8; ++j) {
+      const int r = (tid >> 3) + 16 * j;
+      const bool ok = kin && pin[j];
+      const int src = ok ? wrapi(py[j] + dy, H) * W + wrapi(px[j] + dx, W) : 0;
+      tc::cp_async16<true>(sA + (r >> 3) * 1024 + kv * 128 + (r & 7) * 16, in + (size_t)src * Cin + ci, ok ? 16u : 0u);
+    }
+#pragma unroll
+    for (int j = 0; j < (BN * 8 + 127) / 128; ++j) {
+      const int r = (tid >> 3) + 16 * j;
+      if (r < BN) {
+        const bf16* src = kin ? wgt + (size_t)(n0 + r) * KT + kk : wgt;
+        tc::cp_async16<false>(sB + (r >> 3) * 1024 + kv * 128 + (r & 7) * 16, src, kin ? 16u : 0u);
+      }
+    }
+  };
+#pragma unroll
+  for (int s0 = 0; s0 < S - 1; ++s0) {
+    if (s0 < nck) load_chunk(s0, s0);
+    tc::cp_async_commit();
+  }
+  bool ok = true;
+  int issued = 0;  // chunks whose MMAs were issued (same count in every thread)
+  for (int i = 0; i < nck; ++i) {
+    tc::cp_async_wait<S - 2>();
+    tc::fence_async_smem();
+    tc::fence_before();
+    if (!__syncthreads_and(ok)) { ok = false; break; }
+    tc::fence_after();
+    ++issued;
+    if (tid == 0) {
+      const uint32_t a0 = tc::smem_u32(sm + (i % S) * STAGE);
+#pragma unroll
+      for (int j = 0; j < 4; ++j) {
+        const uint64_t ad = tc::smem_desc(a0 + j * 256, 128, 1024);
+        const uint64_t bd = tc::smem_desc(a0 + ABYTES + j * 256, 128, 1024);
+        tc::mma(taddr, ad, bd, idesc, (i > 0 || j > 0) ? 1u : 0u);
+      }
+      tc::commit(&bar[i % S]);
+    }
+    const int jn = i + S - 1;
+    if (jn < nck) {
+      if (i >= 1) ok = tc::mbar_wait(&bar[(i - 1) % S], ((i - 1) / S) & 1, err) && ok;
+      if (ok) load_chunk(jn, jn % S);
+    }
+    tc::cp_async_commit();
+  }
+  // drain: own copies, then the last issued MMAs (bounded; also after a timeout)
+  tc::cp_async_wait<0>();
+  if (issued > 0) ok = tc::mbar_wait(&bar[(issued - 1) % S], ((issued - 1) / S) & 1, err) && ok;
+  tc::fence_after();
+  if (__syncthreads_and(ok)) {
+    const int r = 32 * warp + (tid & 31);
+    const int p = p0 + r;
+    constexpr int NC = BN < 32 ? 16 : 32;
+#pragma unroll 1
+    for (int c0 = 0; c0 < BN; c0 += NC) {
+      float v[32];
+      const uint32_t ta = taddr + ((uint32_t)(32 * warp) << 16) + c0;
+      if (NC == 16) tc::tmem_ld16(ta, v);
+      else tc::tmem_ld32(ta, v);
+      if (p < npix) {
+#pragma unroll
+        for (int j = 0; j < NC; ++j) {
+          const int c = n0 + c0 + j;
+          float a = v[j] + ((bias && c < cout) ? bias[c] : 0.f);
+          if (relu) a = fmaxf(a, 0.f);
+          v[j] = a;
+        }
+        if (out_bf) {
+#pragma unroll
+          for (int q = 0; q < NC / 8; ++q) {
+            uint4 w;
+            __nv_bfloat162 h0 = __floats2bfloat162_rn(v[8 * q + 0], v[8 * q + 1]);
+            __nv_bfloat162 h1 = __floats2bfloat162_rn(v[8 * q + 2], v[8 * q + 3]);
+            __nv_bfloat162 h2 = __floats2bfloat162_rn(v[8 * q + 4], v[8 * q + 5]);
+            __nv_bfloat162 h3 = __floats2bfloat162_rn(v[8 * q + 6], v[8 * q + 7]);
+            w.x = *reinterpret_cast<uint32_t*>(&h0);
+            w.y = *reinterpret_cast<uint32_t*>(&h1);
+            w.z = *reinterpret_cast<uint32_t*>(&h2);
+            w.w = *reinterpret_cast<uint32_t*>(&h3);
+            *reinterpret_cast<uint4*>(out_bf + (size_t)p * ldo + n0 + c0 + 8 * q) = w;
+          }
+        }
+        if (out_f)
+          for (int j = 0; j < NC; ++j)
+            if (n0 + c0 + j < nout) out_f[(size_t)p * nout + n0 + c0 + j] = v[j];
       }
     }
   }
@@ -120,78 +180,195 @@ __global__ void __launch_bounds__(128) k_conv(const bf16* __restrict__ in, int H
   if (warp == 0) tc::tmem_dealloc(taddr, NCOL);
 }
 
-// Weight gradient: rows m = tap*Cin + ci (tile of 128), columns = BN output
-// channels, reduction over this CTA's pixel range (chunks of 64 pixels).
-template <int BN>
+// 8x8 transpose of 16-bit values: r[i] holds 8 channels of pixel i; on
+// return t[c] holds channel c of pixels 0..7 (both as 4 x u32 pairs).
+__device__ __forceinline__ void transpose8x8(const uint4 (&r)[8], uint4 (&t)[8]) {
+#pragma unroll
+  for (int j = 0; j < 4; ++j) {
+    uint32_t lo[4], hi[4];
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      const uint32_t x = (&r[2 * k].x)[j], y = (&r[2 * k + 1].x)[j];
+      lo[k] = __byte_perm(x, y, 0x5410);
+      hi[k] = __byte_perm(x, y, 0x7632);
+    }
+    t[2 * j] = make_uint4(lo[0], lo[1], lo[2], lo[3]);
+    t[2 * j + 1] = make_uint4(hi[0], hi[1], hi[2], hi[3]);
+  }
+}
+
+// Weight gradient dW[m][co] (m = tap*Cin + ci) += sum over this CTA's pixel
+// range of in[q + off(tap)][ci] * dy[q][co]: rows m in a tile of 128,
+// columns BN = all output channels, reduction over pixels in chunks of 64.
+// Both operands are channel-contiguous in memory and pixel-contiguous in
+// the K-major tiles, so each thread loads 8x8 blocks (8 pixels x 16 bytes),
+// transposes them in registers and stores one 128-byte core matrix.  The
+// loads run DEPTH chunks ahead of the tensor core (register sets), and the
+// MMA tiles are double-buffered.  With db != nullptr the CTAs of the first
+// row tile also reduce the bias gradient db[co] += sum_q dy[q][co] (co < nb)
+// from the dy blocks they already hold.
+template <int BN, int DEPTH>
 __global__ void __launch_bounds__(128) k_wgrad(const bf16* __restrict__ in, const bf16* __restrict__ dy, int H, int W,
                                                int Cin, int pix_per_cta, float* __restrict__ dW,
-                                               int* __restrict__ err) {
+                                               float* __restrict__ db, int nb, int* __restrict__ err) {
+  constexpr int ABYTES = 128 * 64 * 2, STAGE = ABYTES + BN * 64 * 2;
+  constexpr int NBB = (BN + 127) / 128;  // B blocks per thread
   extern __shared__ __align__(1024) unsigned char sm[];
-  unsigned char* sA = sm;                 // 128 x 64
-  unsigned char* sB = sm + 128 * 64 * 2;  // BN x 64
-  __shared__ __align__(8) uint64_t bar;
+  __shared__ __align__(8) uint64_t bar[2];
   __shared__ uint32_t tslot;
   const int tid = threadIdx.x, warp = tid >> 5;
   const int npix = H * W, M = 9 * Cin;
   const int m0 = blockIdx.x * 128;
   const int q0 = blockIdx.y * pix_per_cta, q1 = min(npix, q0 + pix_per_cta);
+  const int nck = q1 > q0 ? (q1 - q0 + 63) / 64 : 0;
+  const bool do_bias = db != nullptr && blockIdx.x == 0;
   constexpr uint32_t NCOL = BN < 32 ? 32 : BN;
   if (warp == 0) tc::tmem_alloc(&tslot, NCOL);
-  if (tid == 0) tc::mbar_init(&bar);
+  if (tid < 2) tc::mbar_init(&bar[tid]);
   tc::fence_before();
   __syncthreads();
   tc::fence_after();
   const uint32_t taddr = tslot;
   const uint32_t idesc = tc::idesc_bf16(128, BN);
-  uint32_t phase = 0;
-  bool first = true;
-  for (int k0 = q0; k0 < q1; k0 += 64) {
-    for (int i = tid; i < 128 * 64; i += 128) {
-      const int r = i % 128, k = i / 128;
-      const int m = m0 + r, q = k0 + k;
-      bf16 v = __float2bfloat16(0.f);
-      if (m < M && q < q1) {
-        const int tap = m / Cin, ci = m % Cin;
-        const int y = q / W, x = q % W;
-        const int src = wrapi(y + tap / 3 - 1, H) * W + wrapi(x + tap % 3 - 1, W);
-        v = in[(size_t)src * Cin + ci];
+  // A block of this thread: rows m0 + 8*rb .. +7 (one tap), pixels 8*kb .. +7
+  const int rb = tid >> 3, kb = tid & 7;
+  const int mA = m0 + 8 * rb;
+  const bool rowok = mA < M;
+  const int tap = rowok ? mA / Cin : 0, ci0 = rowok ? mA - tap * Cin : 0;
+  const int ty = tap / 3 - 1, tx = tap % 3 - 1;
+  uint4 ra[DEPTH][8], rbv[DEPTH][NBB][8];
+  float bsum[NBB][8];
+#pragma unroll
+  for (int b = 0; b < NBB; ++b)
+#pragma unroll
+    for (int c = 0; c < 8; ++c) bsum[b][c] = 0.f;
+  auto load_regs = [&](int i, auto slot_c) {
+    constexpr int SL = decltype(slot_c)::value;
+    const int qb = q0 + i * 64 + 8 * kb;
+#pragma unroll
+    for (int e = 0; e < 8; ++e) {
+      const int q = qb + e;
+      uint4 v = make_uint4(0, 0, 0, 0);
+      if (rowok && q < q1) {
+        const int y = q / W, x = q - y * W;
+        const int src = wrapi(y + ty, H) * W + wrapi(x + tx, W);
+        v = *reinterpret_cast<const uint4*>(in + (size_t)src * Cin + ci0);
       }
-      *reinterpret_cast<bf16*>(sA + tc::tile_off(r, k, 64)) = v;
+      ra[SL][e] = v;
     }
-    for (int i = tid; i < BN * 64; i += 128) {
-      const int c = i % BN, k = i / BN;
-      const int q = k0 + k;
-      const bf16 v = q < q1 ? dy[(size_t)q * BN + c] : __float2bfloat16(0.f);
-      *reinterpret_cast<bf16*>(sB + tc::tile_off(c, k, 64)) = v;
+#pragma unroll
+    for (int b = 0; b < NBB; ++b) {
+      const int cb = (tid + 128 * b) >> 3;
+#pragma unroll
+      for (int e = 0; e < 8; ++e) {
+        const int q = qb + e;
+        uint4 v = make_uint4(0, 0, 0, 0);
+        if (cb < BN / 8 && q < q1) v = *reinterpret_cast<const uint4*>(dy + (size_t)q * BN + 8 * cb);
+        rbv[SL][b][e] = v;
+      }
     }
+  };
+  auto store_regs = [&](int buf, auto slot_c) {
+    constexpr int SL = decltype(slot_c)::value;
+    unsigned char* sA = sm + buf * STAGE;
+    unsigned char* sB = sA + ABYTES;
+    uint4 t[8];
+    transpose8x8(ra[SL], t);
+#pragma unroll
+    for (int c = 0; c < 8; ++c) *reinterpret_cast<uint4*>(sA + rb * 1024 + kb * 128 + c * 16) = t[c];
+#pragma unroll
+    for (int b = 0; b < NBB; ++b) {
+      const int cb = (tid + 128 * b) >> 3;
+      if (cb < BN / 8) {
+        if (do_bias) {
+#pragma unroll
+          for (int e = 0; e < 8; ++e) {
+            const __nv_bfloat162* h = reinterpret_cast<const __nv_bfloat162*>(&rbv[SL][b][e]);
+#pragma unroll
+            for (int c = 0; c < 4; ++c) {
+              const float2 f = __bfloat1622float2(h[c]);
+              bsum[b][2 * c] += f.x;
+              bsum[b][2 * c + 1] += f.y;
+            }
+          }
+        }
+        transpose8x8(rbv[SL][b], t);
+#pragma unroll
+        for (int c = 0; c < 8; ++c) *reinterpret_cast<uint4*>(sB + cb * 1024 + kb * 128 + c * 16) = t[c];
+      }
+    }
+  };
+  bool ok = true;
+  int issued = 0;
+  // one chunk: free its tile buffer, fill it from the register set, issue its MMAs, prefetch
+  auto step = [&](int i, auto slot_c) -> bool {
+    const int buf = i & 1;
+    if (i >= 2) ok = tc::mbar_wait(&bar[buf], ((i - 2) >> 1) & 1, err) && ok;
+    if (ok) store_regs(buf, slot_c);
     tc::fence_async_smem();
     tc::fence_before();
-    __syncthreads();
+    if (!__syncthreads_and(ok)) { ok = false; return false; }
     tc::fence_after();
+    ++issued;
     if (tid == 0) {
+      const uint32_t a0 = tc::smem_u32(sm + buf * STAGE);
+#pragma unroll
       for (int j = 0; j < 4; ++j) {
-        const uint64_t ad = tc::smem_desc(tc::smem_u32(sA) + j * 256, 128, 8 * 128);
-        const uint64_t bd = tc::smem_desc(tc::smem_u32(sB) + j * 256, 128, 8 * 128);
-        tc::mma(taddr, ad, bd, idesc, first ? 0u : 1u);
-        first = false;
+        const uint64_t ad = tc::smem_desc(a0 + j * 256, 128, 1024);
+        const uint64_t bd = tc::smem_desc(a0 + ABYTES + j * 256, 128, 1024);
+        tc::mma(taddr, ad, bd, idesc, (i > 0 || j > 0) ? 1u : 0u);
       }
-      tc::commit(&bar);
+      tc::commit(&bar[buf]);
     }
-    tc::mbar_wait(&bar, phase, err);
-    phase ^= 1;
-    tc::fence_after();
+    if (i + DEPTH < nck) load_regs(i + DEPTH, slot_c);
+    return true;
+  };
+  using S0 = std::integral_constant<int, 0>;
+  using S1 = std::integral_constant<int, DEPTH - 1>;
+  if (nck > 0) load_regs(0, S0());
+  if (DEPTH == 2 && nck > 1) load_regs(1, S1());
+  if (DEPTH == 2) {
+    for (int i = 0; i < nck; i += 2) {
+      if (!step(i, S0())) break;
+      if (i + 1 < nck && !step(i + 1, S1())) break;
+    }
+  } else {
+    for (int i = 0; i < nck; ++i)
+      if (!step(i, S0())) break;
   }
-  const int r = 32 * warp + (tid & 31);
-  const int m = m0 + r;
-  if (q1 > q0) {  // CTA-uniform: every warp runs the collective TMEM loads
-    for (int c0 = 0; c0 < BN; c0 += (BN < 32 ? 16 : 32)) {
+  if (issued > 0) ok = tc::mbar_wait(&bar[(issued - 1) & 1], ((issued - 1) >> 1) & 1, err) && ok;
+  tc::fence_after();
+  if (__syncthreads_and(ok) && issued > 0) {  // CTA-uniform: every warp runs the TMEM loads
+    const int r = 32 * warp + (tid & 31);
+    const int m = m0 + r;
+    constexpr int NC = BN < 32 ? 16 : 32;
+#pragma unroll 1
+    for (int c0 = 0; c0 < BN; c0 += NC) {
       float v[32];
       const uint32_t ta = taddr + ((uint32_t)(32 * warp) << 16) + c0;
-      if (BN < 32) tc::tmem_ld16(ta, v);
+      if (NC == 16) tc::tmem_ld16(ta, v);
       else tc::tmem_ld32(ta, v);
-      const int nc = BN < 32 ? 16 : 32;
       if (m < M)
-        for (int j = 0; j < nc; ++j) atomicAdd(&dW[(size_t)m * BN + c0 + j], v[j]);
+#pragma unroll
+        for (int j = 0; j < NC; j += 4)
+          atomicAdd(reinterpret_cast<float4*>(&dW[(size_t)m * BN + c0 + j]), make_float4(v[j], v[j + 1], v[j + 2], v[j + 3]));
+    }
+    if (do_bias) {
+#pragma unroll
+      for (int b = 0; b < NBB; ++b) {
+        const int cb = (tid + 128 * b) >> 3;
+#pragma unroll
+        for (int c = 0; c < 8; ++c) {
+          float x = bsum[b][c];
+          x += __shfl_xor_sync(0xffffffffu, x, 1);
+          x += __shfl_xor_sync(0xffffffffu, x, 2);
+          x += __shfl_xor_sync(0xffffffffu, x, 4);
+          bsum[b][c] = x;
+        }
+        if (kb == 0 && cb < BN / 8)
+          for (int c = 0; c < 8; ++c)
+            if (8 * cb + c < nb) atomicAdd(&db[8 * cb + c], bsum[b][c]);
+      }
     }
   }
   tc::fence_before();
@@ -249,22 +426,6 @@ __global__ void k_add(const bf16* __restrict__ a, const bf16* __restrict__ b, bf
 __global__ void k_relu_bwd(const bf16* __restrict__ y, const bf16* __restrict__ d, bf16* __restrict__ o, size_t n) {
   for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
     o[i] = __bfloat162float(y[i]) > 0.f ? d[i] : __float2bfloat16(0.f);
-}
-// bias gradient: db[c] += sum_p d[p][c] for the cout real channels (stride cs)
-__global__ void k_bias_grad(const bf16* __restrict__ d, int npix, int cs, int cout, float* __restrict__ db) {
-  for (int c = blockIdx.x; c < cout; c += gridDim.x) {
-    float s = 0.f;
-    for (int p = threadIdx.x; p < npix; p += blockDim.x) s += __bfloat162float(d[(size_t)p * cs + c]);
-    __shared__ float red[256];
-    red[threadIdx.x] = s;
-    __syncthreads();
-    for (int o = blockDim.x / 2; o > 0; o >>= 1) {
-      if ((int)threadIdx.x < o) red[threadIdx.x] += red[threadIdx.x + o];
-      __syncthreads();
-    }
-    if (threadIdx.x == 0) atomicAdd(&db[c], red[0]);
-    __syncthreads();
-  }
 }
 // MSE loss on the head output (FP32 [p][nout]) against planar targets
 // [nout][p]; writes the BF16 gradient [p][cpad] and accumulates the loss.
@@ -490,53 +651,58 @@ class Net {
   }
 
   // ---- launches
-  void conv(const Tensor& in, const Conv& cv, const bf16* w, int cout_p, const float* bias, int relu, bf16* out_bf,
+  // Convolution of `in` with weights w (rows [cout_p][9*in.c]); output
+  // channels split into blocks of BN so that small levels still fill the GPU.
+  void conv(const Tensor& in, const bf16* w, int cout_p, int cout, const float* bias, int relu, bf16* out_bf,
             float* out_f32, int nout) {
     const int npix = in.h * in.w;
-    const int grid = (npix + 127) / 128;
-    const size_t smem = 128 * 64 * 2 + (size_t)cout_p * 64 * 2;
-    switch (cout_p) {
-      case 16: launch_conv<16>(grid, smem, in, w, bias, relu, out_bf, out_f32, nout); break;
-      case 32: launch_conv<32>(grid, smem, in, w, bias, relu, out_bf, out_f32, nout); break;
-      case 64: launch_conv<64>(grid, smem, in, w, bias, relu, out_bf, out_f32, nout); break;
-      case 128: launch_conv<128>(grid, smem, in, w, bias, relu, out_bf, out_f32, nout); break;
-      default: launch_conv<256>(grid, smem, in, w, bias, relu, out_bf, out_f32, nout); break;
+    const int tiles = (npix + 127) / 128;
+    int bn = std::min(cout_p, 128);
+    while (bn > 32 && tiles * (cout_p / bn) < 2 * 152) bn /= 2;
+    const dim3 grid(tiles, cout_p / bn);
+    switch (bn) {
+      case 16: launch_conv<16>(grid, in, w, bias, cout, relu, out_bf, cout_p, out_f32, nout); break;
+      case 32: launch_conv<32>(grid, in, w, bias, cout, relu, out_bf, cout_p, out_f32, nout); break;
+      case 64: launch_conv<64>(grid, in, w, bias, cout, relu, out_bf, cout_p, out_f32, nout); break;
+      default: launch_conv<128>(grid, in, w, bias, cout, relu, out_bf, cout_p, out_f32, nout); break;
     }
-    (void)cv;
   }
   template <int BN>
-  void launch_conv(int grid, size_t smem, const Tensor& in, const bf16* w, const float* bias, int relu, bf16* ob,
-                   float* of, int nout) {
+  void launch_conv(dim3 grid, const Tensor& in, const bf16* w, const float* bias, int cout, int relu, bf16* ob,
+                   int ldo, float* of, int nout) {
+    const size_t smem = (size_t)kConvStages * (128 * 64 * 2 + BN * 64 * 2);
     static bool attr = false;
     if (!attr) {
-      cudaFuncSetAttribute(k_conv<BN>, cudaFuncAttributeMaxDynamicSharedMemorySize, 128 * 64 * 2 + 256 * 64 * 2);
+      cudaFuncSetAttribute(k_conv<BN>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
       attr = true;
     }
-    k_conv<BN><<<grid, 128, smem, st>>>(in.d, in.h, in.w, in.c, w, bias, relu, ob, of, nout, err);
+    k_conv<BN><<<grid, 128, smem, st>>>(in.d, in.h, in.w, in.c, w, bias, cout, relu, ob, ldo, of, nout, err);
   }
-  void wgrad(const Tensor& in, const bf16* dy, int coutp, float* out) {
+  // dW GEMM (and, with db, the bias gradient of the nb real channels).
+  void wgrad(const Tensor& in, const bf16* dy, int coutp, float* out, float* db, int nb) {
     const int npix = in.h * in.w, M = 9 * in.c;
     const int mt = (M + 127) / 128;
-    int ppc = 4096;
-    while ((npix + ppc - 1) / ppc * mt < 2 * 152 && ppc > 256) ppc /= 2;
+    int ppc = 8192;
+    while ((npix + ppc - 1) / ppc * mt < 4 * 152 && ppc > 512) ppc /= 2;
     dim3 grid(mt, (npix + ppc - 1) / ppc);
-    const size_t smem = 128 * 64 * 2 + (size_t)coutp * 64 * 2;
+    const size_t smem = 2 * (128 * 64 * 2 + (size_t)coutp * 64 * 2);
     cudaMemsetAsync(out, 0, sizeof(float) * (size_t)M * coutp, st);
     switch (coutp) {
-      case 16: launch_wgrad<16>(grid, smem, in, dy, ppc, out); break;
-      case 32: launch_wgrad<32>(grid, smem, in, dy, ppc, out); break;
-      case 64: launch_wgrad<64>(grid, smem, in, dy, ppc, out); break;
-      case 128: launch_wgrad<128>(grid, smem, in, dy, ppc, out); break;
-      default: launch_wgrad<256>(grid, smem, in, dy, ppc, out); break;
+      case 16: launch_wgrad<16, 2>(grid, smem, in, dy, ppc, out, db, nb); break;
+      case 32: launch_wgrad<32, 2>(grid, smem, in, dy, ppc, out, db, nb); break;
+      case 64: launch_wgrad<64, 2>(grid, smem, in, dy, ppc, out, db, nb); break;
+      case 128: launch_wgrad<128, 2>(grid, smem, in, dy, ppc, out, db, nb); break;
+      default: launch_wgrad<256, 1>(grid, smem, in, dy, ppc, out, db, nb); break;
     }
   }
-  template <int BN> void launch_wgrad(dim3 grid, size_t smem, const Tensor& in, const bf16* dy, int ppc, float* out) {
+  template <int BN, int DEPTH>
+  void launch_wgrad(dim3 grid, size_t smem, const Tensor& in, const bf16* dy, int ppc, float* out, float* db, int nb) {
     static bool attr = false;
     if (!attr) {
-      cudaFuncSetAttribute(k_wgrad<BN>, cudaFuncAttributeMaxDynamicSharedMemorySize, 128 * 64 * 2 + 256 * 64 * 2);
+      cudaFuncSetAttribute(k_wgrad<BN, DEPTH>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
       attr = true;
     }
-    k_wgrad<BN><<<grid, 128, smem, st>>>(in.d, dy, in.h, in.w, in.c, ppc, out, err);
+    k_wgrad<BN, DEPTH><<<grid, 128, smem, st>>>(in.d, dy, in.h, in.w, in.c, ppc, out, db, nb, err);
   }
   static int blocks(size_t n) { return (int)std::min<size_t>((n + 255) / 256, 152 * 16); }
 
@@ -548,9 +714,9 @@ class Net {
     const Tensor* cur = &x0;
     for (int l = 0; l < levels; ++l) {
       const Conv& c1 = convs[ci++];
-      conv(*cur, c1, c1.wb, c1.coutp, param + c1.boff, 1, a[l].d, nullptr, 0);
+      conv(*cur, c1.wb, c1.coutp, c1.cout, param + c1.boff, 1, a[l].d, nullptr, 0);
       const Conv& c2 = convs[ci++];
-      conv(a[l], c2, c2.wb, c2.coutp, param + c2.boff, 1, s[l].d, nullptr, 0);
+      conv(a[l], c2.wb, c2.coutp, c2.cout, param + c2.boff, 1, s[l].d, nullptr, 0);
       if (l + 1 < levels) {
         k_pool<<<blocks(p[l].n()), 256, 0, st>>>(s[l].d, p[l].d, s[l].h, s[l].w, s[l].c);
         cur = &p[l];
@@ -560,14 +726,14 @@ class Net {
     for (int l = levels - 2; l >= 0; --l) {
       k_up<<<blocks(u[l].n()), 256, 0, st>>>(dec->d, u[l].d, u[l].h, u[l].w, u[l].c);
       const Conv& c1 = convs[ci++];
-      conv(u[l], c1, c1.wb, c1.coutp, param + c1.boff, 1, c[l].d, nullptr, 0);
+      conv(u[l], c1.wb, c1.coutp, c1.cout, param + c1.boff, 1, c[l].d, nullptr, 0);
       k_add<<<blocks(e[l].n()), 256, 0, st>>>(c[l].d, s[l].d, e[l].d, e[l].n());
       const Conv& c2 = convs[ci++];
-      conv(e[l], c2, c2.wb, c2.coutp, param + c2.boff, 1, d[l].d, nullptr, 0);
+      conv(e[l], c2.wb, c2.coutp, c2.cout, param + c2.boff, 1, d[l].d, nullptr, 0);
       dec = &d[l];
     }
     const Conv& hd = convs[ci++];
-    conv(*dec, hd, hd.wb, hd.coutp, param + hd.boff, 0, nullptr, out_f, 2);
+    conv(*dec, hd.wb, hd.coutp, hd.cout, param + hd.boff, 0, nullptr, out_f, 2);
   }
 
   // Backward of conv `cv` whose input is `in` and (post-activation) output
@@ -579,17 +745,16 @@ class Net {
       k_relu_bwd<<<blocks(nout), 256, 0, st>>>(out, dpost, dpre_scratch, nout);
       dpre = dpre_scratch;
     }
-    wgrad(in, dpre, cv.coutp, wscratch);
+    wgrad(in, dpre, cv.coutp, wscratch, grad + cv.boff, cv.cout);
     k_wgrad_scatter<<<blocks((size_t)cv.cout * 9 * cv.cin), 256, 0, st>>>(wscratch, cv.cout, cv.cin, cv.coutp,
                                                                           cv.cinp, grad + cv.woff);
-    k_bias_grad<<<std::min(cv.cout, 256), 256, 0, st>>>(dpre, in.h * in.w, cv.coutp, cv.cout, grad + cv.boff);
     if (din) {
       Tensor dp;
       dp.d = const_cast<bf16*>(dpre);
       dp.h = in.h;
       dp.w = in.w;
       dp.c = cv.coutp;
-      conv(dp, cv, cv.wt, cv.cinp, nullptr, 0, din, nullptr, 0);
+      conv(dp, cv.wt, cv.cinp, cv.cinp, nullptr, 0, din, nullptr, 0);
     }
   }
 

@@ -79,6 +79,18 @@ __device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, int* e
   return done != 0;
 }
 
+// Asynchronous 16-byte global -> shared copies (zero-filled when nbytes = 0).
+// CA keeps the line in L1 (operands re-read by neighbouring taps).
+template <bool CA>
+__device__ __forceinline__ void cp_async16(void* dst, const void* src, uint32_t nbytes) {
+  if (CA)
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 16, %2;" ::"r"(smem_u32(dst)), "l"(src), "r"(nbytes));
+  else
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;" ::"r"(smem_u32(dst)), "l"(src), "r"(nbytes));
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;"); }
+template <int N> __device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;" ::"n"(N)); }
+
 // 32 consecutive FP32 accumulator columns of this thread's TMEM lane.
 __device__ __forceinline__ void tmem_ld32(uint32_t taddr, float* out) {
   uint32_t v[32];
