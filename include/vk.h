@@ -75,6 +75,7 @@ typedef struct vk_namelist {
   double gp_mass_part, ppotd, ppotv0, ppotthick;
   int32_t maxiter, fsteps, ssteps, gsteps;  /* &tparam */
   int32_t nrst, sprst;                      /* &ckprst */
+  int32_t strst, ststeps;                   /* &ckprst strst, &tparam ststeps (-DGPSTS) */
 } vk_namelist;
 
 /* Replaces: the namelist reads + MPI_BCAST block (src/driver.f90:147-334).
@@ -194,6 +195,29 @@ int vk_timing_end(void* ctx, int32_t cap, char* tags, double* total_ms, int64_t*
  * array: calls that overlap on the GPU race.  Work is queued on `stream`
  * (a cudaStream_t; NULL = legacy default stream) and is not synchronised. */
 int vk_fft2d_forward_noalloc(const double* psi_dev, double* kpsi_dev, int32_t nx, int32_t ny, void* stream);
+
+/* ---- spatio-temporal spectra (the -DGPSTS path) ----
+ * Replaces: sts_gpe (src/diagnostics.f90:636-695), called every ststeps
+ * (src/solve.f90:139-144), which appends kpsi(:,kx=0) and the kpsi plane to
+ * files, and the offline post-processor Run/CompSTS/driver.f90:132-265,
+ * which Hann-windows each mode's time series (w = (1-cos(2 pi t/(Nt-1)))/2),
+ * transforms it along time (FFTW forward), and forms
+ *   sts1d[w][ky]   = stsnorm |X(kx=0, ky, w)|^2
+ *   sts2d[w][m]    = sum over nint(|k|) = m of stsnorm |X(k, w)|^2, m = 0..nx/3
+ * with stsnorm = (1/Nt)^2 (1/(nx ny))^2.  Here the planes stay on the GPU in
+ * a ring of nt records (nt * nx * ny * 16 bytes) and the transform and the
+ * shell sums run there. */
+/* Allocates the ring for nt records (nt a power of two, 16..4096). */
+int vk_sts_begin(void* ctx, int32_t nt);
+/* Appends the current kpsi (as FP64) to the ring; VK_E_STATE when full. */
+int vk_sts_record(void* ctx);
+/* Number of records held. */
+int vk_sts_count(void* ctx, int32_t* n);
+/* With the ring full: sts1d[nt*ny] (row w = 0..nt-1), sts2d[nt*(nx/3+1)].
+ * Consumes the records (the ring is empty afterwards). */
+int vk_sts_spectra(void* ctx, double* sts1d, double* sts2d);
+/* Frees the ring. */
+int vk_sts_end(void* ctx);
 
 /* Thread-local message for the last failing call on this thread. */
 const char* vk_last_error(void);

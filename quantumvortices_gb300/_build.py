@@ -16,7 +16,7 @@ OUT_DIR = os.path.join(PKG, "_build")
 LIB = os.path.join(PKG, "libvk.so")
 DRIVER = os.path.join(PKG, "vikshobha_gb300")
 
-CU_SRCS = ["vk_f64.cu", "vk_f32.cu", "vk_common.cu", "vk_noalloc.cu", "vk_ens.cu", "vk_nn.cu"]
+CU_SRCS = ["vk_f64.cu", "vk_f32.cu", "vk_common.cu", "vk_noalloc.cu", "vk_ens.cu", "vk_nn.cu", "vk_sts.cu"]
 CPP_SRCS = ["vk_api.cpp", "vk_host.cpp"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC,-fopenmp",

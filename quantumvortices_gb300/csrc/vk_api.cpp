@@ -16,6 +16,7 @@ struct Ctx {
   uint32_t magic;
   vk_params p;
   vk::SolverBase* s;
+  vk::StsBase* sts = nullptr;  // spatio-temporal spectra ring (vk_sts_begin)
 };
 constexpr uint32_t kMagic = 0x56494b53u;  // "VIKS"
 
@@ -67,6 +68,8 @@ extern "C" int vk_init(const vk_params* p, void** ctx) {
 extern "C" int vk_finalize(void* ctx) {
   Ctx* c = as_ctx(ctx);
   if (!c) return VK_E_INVALID;
+  delete c->sts;
+  c->sts = nullptr;
   delete c->s;
   c->s = nullptr;
   c->magic = 0;
@@ -181,4 +184,58 @@ extern "C" int vk_set_psi_vortices(void* ctx, int32_t n_vort, uint64_t seed, dou
                                    double* pos_out) {
   VK_CTX_OR_FAIL(ctx);
   return c->s->set_psi_vortices(n_vort, seed, xi0, min_sep, pos_out);
+}
+
+// ---- spatio-temporal spectra (sts_gpe + Run/CompSTS post-processing) ----
+
+extern "C" int vk_sts_begin(void* ctx, int32_t nt) {
+  VK_CTX_OR_FAIL(ctx);
+  if (!pow2_in_range(nt)) {
+    set_error("vk_sts_begin: nt must be a power of two in [16, 4096]");
+    return VK_E_INVALID;
+  }
+  delete c->sts;
+  c->sts = nullptr;
+  int st = VK_OK;
+  c->sts = vk::make_sts(c->p.nx, c->p.ny, nt, c->s->stream(), &st);
+  return st;
+}
+
+extern "C" int vk_sts_record(void* ctx) {
+  VK_CTX_OR_FAIL(ctx);
+  if (!c->sts) {
+    set_error("vk_sts_record: no record ring (call vk_sts_begin first)");
+    return VK_E_STATE;
+  }
+  return c->sts->record(c->s);
+}
+
+extern "C" int vk_sts_count(void* ctx, int32_t* n) {
+  VK_CTX_OR_FAIL(ctx);
+  if (!n) {
+    set_error("vk_sts_count: null output");
+    return VK_E_INVALID;
+  }
+  *n = c->sts ? c->sts->count() : 0;
+  return VK_OK;
+}
+
+extern "C" int vk_sts_spectra(void* ctx, double* sts1d, double* sts2d) {
+  VK_CTX_OR_FAIL(ctx);
+  if (!sts1d || !sts2d) {
+    set_error("vk_sts_spectra: null output");
+    return VK_E_INVALID;
+  }
+  if (!c->sts) {
+    set_error("vk_sts_spectra: no record ring (call vk_sts_begin first)");
+    return VK_E_STATE;
+  }
+  return c->sts->spectra(sts1d, sts2d);
+}
+
+extern "C" int vk_sts_end(void* ctx) {
+  VK_CTX_OR_FAIL(ctx);
+  delete c->sts;
+  c->sts = nullptr;
+  return VK_OK;
 }

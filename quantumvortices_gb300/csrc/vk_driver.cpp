@@ -14,10 +14,14 @@
 //   data/gpobj_{pos,vel,frc}_<i>.dat_nrst0, egpobj, momgpobj  (particles)
 //   data/gp{pos,vel,f0ext}_ckp.dat_nrst0     every fsteps (gppart_checkpoint)
 //   run_info.dat                             wall time
+// With --sts NT (the -DGPSTS build), every ststeps (sts_gpe):
+//   data/sts_time.dat_nrst0, data/sts1d/kpsi_x0_nrst0.dat, data/sts2d/kpsi_nrst0p1.dat
+// and every NT records the Run/CompSTS spectra data/sts1d_kx0_nrst<strst>.dat,
+// data/sts2d_nrst<strst>.dat (computed on the GPU).
 // Text files use Fortran's E15.6 edit descriptor.  Output points between
 // which no file is written are stepped with one vk_gpe_rk4 call.
 //
-// Usage: vikshobha_gb300 [--argle] [--fp32] [--no-otoc] [--steps N]
+// Usage: vikshobha_gb300 [--argle] [--fp32] [--no-otoc] [--steps N] [--sts NT]
 #include <chrono>
 #include <cmath>
 #include <cstdio>
@@ -73,6 +77,20 @@ void mkdirs() {
   for (const char* d : dirs) mkdir(d, 0755);
 }
 
+// One Fortran sequential-unformatted record (4-byte length markers) appended.
+void append_record(const std::string& path, const void* data, size_t bytes) {
+  FILE* f = std::fopen(path.c_str(), "ab");
+  if (!f) {
+    std::fprintf(stderr, "cannot open %s\n", path.c_str());
+    std::exit(1);
+  }
+  const uint32_t m = (uint32_t)bytes;
+  std::fwrite(&m, 4, 1, f);
+  std::fwrite(data, 1, bytes, f);
+  std::fwrite(&m, 4, 1, f);
+  std::fclose(f);
+}
+
 bool file_exists(const std::string& p) {
   struct stat st;
   return stat(p.c_str(), &st) == 0;
@@ -112,13 +130,15 @@ void read_particle_file(const std::string& path, int np, std::vector<double>& ou
 int main(int argc, char** argv) {
   bool argle = false, fp32 = false, otoc = true;
   long steps_override = -1;
+  int sts_nt = 0;  // -DGPSTS path: records per spatio-temporal spectrum (0 = off)
   for (int i = 1; i < argc; ++i) {
     if (!std::strcmp(argv[i], "--argle")) argle = true;
     else if (!std::strcmp(argv[i], "--fp32")) fp32 = true;
     else if (!std::strcmp(argv[i], "--no-otoc")) otoc = false;
     else if (!std::strcmp(argv[i], "--steps") && i + 1 < argc) steps_override = std::atol(argv[++i]);
+    else if (!std::strcmp(argv[i], "--sts") && i + 1 < argc) sts_nt = std::atoi(argv[++i]);
     else {
-      std::fprintf(stderr, "usage: %s [--argle] [--fp32] [--no-otoc] [--steps N]\n", argv[0]);
+      std::fprintf(stderr, "usage: %s [--argle] [--fp32] [--no-otoc] [--steps N] [--sts NT]\n", argv[0]);
       return 2;
     }
   }
@@ -131,6 +151,7 @@ int main(int argc, char** argv) {
   const long maxiter = steps_override >= 0 ? steps_override : nl.maxiter;
   const int fsteps = nl.fsteps > 0 ? nl.fsteps : 1 << 30, gsteps = nl.gsteps > 0 ? nl.gsteps : 1 << 30;
   const int ssteps = nl.ssteps > 0 ? nl.ssteps : 1 << 30;
+  const int ststeps = sts_nt > 0 ? (nl.ststeps > 0 ? nl.ststeps : 20) : 1 << 30;
   const int nx = p.nx, ny = p.ny, np = p.n_particles;
   const int nshell = vk_nshell(nx);
   std::printf(" VIKSHOBHA 2D GPE on one GPU: Nx %d Ny %d dt %g %s %s\n", nx, ny, p.dt, argle ? "ARGLE" : "RK4",
@@ -155,8 +176,49 @@ int main(int argc, char** argv) {
   }
   std::vector<double> sc(10), spec(6 * (size_t)(nshell + 1));
   std::vector<double> ppos(2 * (size_t)std::max(np, 1)), pvel(ppos.size()), pfrc(ppos.size());
-  int fldpoint = 0, spcpoint = 0;
+  int fldpoint = 0, spcpoint = 0, stspoint = 0, stsfile = nl.strst;
   double time = 0.0;
+
+  // sts_gpe (src/diagnostics.f90:636-695): time, the kx = 0 line and the
+  // plane of kpsi appended to files; the same record goes to the GPU ring, and
+  // every sts_nt records the spectra of Run/CompSTS/driver.f90 are written
+  // (sts1d_kx0 / sts2d text files, one line per frequency).
+  std::vector<double> kbuf;
+  if (sts_nt > 0) {
+    mkdir("data/sts1d", 0755);
+    mkdir("data/sts2d", 0755);
+    kbuf.resize(2 * (size_t)nx * ny);
+    check(vk_sts_begin(ctx, sts_nt), "vk_sts_begin");
+  }
+  auto sts = [&](double t) {
+    append_line("data/sts_time.dat_nrst" + nrs, {t});
+    check(vk_get_kpsi(ctx, kbuf.data()), "vk_get_kpsi");
+    append_record("data/sts1d/kpsi_x0_nrst" + nrs + ".dat", kbuf.data(), sizeof(double) * 2 * ny);
+    append_record("data/sts2d/kpsi_nrst" + nrs + "p1.dat", kbuf.data(), sizeof(double) * 2 * (size_t)nx * ny);
+    check(vk_sts_record(ctx), "vk_sts_record");
+    int32_t cnt = 0;
+    check(vk_sts_count(ctx, &cnt), "vk_sts_count");
+    if (cnt == sts_nt) {
+      const int nsh = nx / 3 + 1;
+      std::vector<double> s1((size_t)sts_nt * ny), s2((size_t)sts_nt * nsh);
+      check(vk_sts_spectra(ctx, s1.data(), s2.data()), "vk_sts_spectra");
+      const std::string id = std::to_string(stsfile++);
+      FILE* f1 = std::fopen(("data/sts1d_kx0_nrst" + id + ".dat").c_str(), "w");
+      FILE* f2 = std::fopen(("data/sts2d_nrst" + id + ".dat").c_str(), "w");
+      for (int w = 0; w < sts_nt; ++w) {
+        if (f1) {
+          for (int j = 0; j < ny; ++j) std::fprintf(f1, " %24.16E", s1[(size_t)w * ny + j]);
+          std::fprintf(f1, "\n");
+        }
+        if (f2) {
+          for (int j = 0; j < nsh; ++j) std::fprintf(f2, " %24.16E", s2[(size_t)w * nsh + j]);
+          std::fprintf(f2, "\n");
+        }
+      }
+      if (f1) std::fclose(f1);
+      if (f2) std::fclose(f2);
+    }
+  };
 
   auto io_fields = [&](int n, double t) {
     const std::string f = "data/wf/wf" + std::to_string(n) + "p1.dat";
@@ -229,13 +291,15 @@ int main(int argc, char** argv) {
   // solve (src/solve.f90:414-523) with nrst = 0 after restart_from_argle_data
   io_fields(fldpoint, time);
   diagnostics(spcpoint, 0, time);
+  if (sts_nt > 0) sts(time);  // src/solve.f90:96-98 (nrst = 0)
   double residual = 0.0;
   long itime = 0;
   while (itime < maxiter) {
     // advance to the next output point in one call
     long next = maxiter;
     const long nf = (itime / fsteps + 1) * (long)fsteps, ng = (itime / gsteps + 1) * (long)gsteps;
-    next = std::min(next, std::min(nf, ng));
+    const long nst = (itime / ststeps + 1) * (long)ststeps;
+    next = std::min(next, std::min(std::min(nf, ng), nst));
     const int n = (int)(next - itime);
     if (argle) check(vk_argle(ctx, n, &residual), "vk_argle");
     else check(vk_gpe_rk4(ctx, n), "vk_gpe_rk4");
@@ -253,6 +317,10 @@ int main(int argc, char** argv) {
         std::fprintf(stderr, "norm blew up at step %ld (norm = %g)\n", itime, sc[6]);
         return 3;
       }
+    }
+    if (itime % ststeps == 0) {  // src/solve.f90:139-144
+      ++stspoint;
+      sts(time);
     }
   }
   check(vk_finalize(ctx), "vk_finalize");

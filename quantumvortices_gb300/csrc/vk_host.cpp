@@ -173,6 +173,8 @@ extern "C" int vk_read_namelists(const char* parameter_txt, const char* paramete
   get(nl, "tparam", "gsteps", [&](double x) { out->gsteps = (int32_t)x; });
   get(nl, "ckprst", "nrst", [&](double x) { out->nrst = (int32_t)x; });
   get(nl, "ckprst", "sprst", [&](double x) { out->sprst = (int32_t)x; });
+  get(nl, "ckprst", "strst", [&](double x) { out->strst = (int32_t)x; });
+  get(nl, "tparam", "ststeps", [&](double x) { out->ststeps = (int32_t)x; });
   get(nl, "gpparam", "xi", [&](double x) { out->xi = x; });
   get(nl, "gpparam", "csound", [&](double x) { out->csound = x; });
   get(nl, "gpparam", "rho_avg", [&](double x) { out->rho_avg = x; });

@@ -30,6 +30,9 @@ class SolverBase {
   // Ensemble support: copy this field's device view (a Field<T>), query and
   // update the state flags around batched steps.
   virtual int field_view(void* out, size_t size) = 0;
+  // Copies kpsi (all nx*ny modes) as FP64 into dst (device double2), on
+  // this solver's stream.
+  virtual int snapshot_kpsi_f64(void* dst) = 0;
   virtual bool kpsi_is_masked() const = 0;
   virtual void mark_rk4_done() = 0;
 };
@@ -52,6 +55,16 @@ class EnsembleBase {
 };
 EnsembleBase* make_ensemble_f64(const vk_params* p, int n, int* status);
 EnsembleBase* make_ensemble_f32(const vk_params* p, int n, int* status);
+
+// Spatio-temporal spectra recorder (vk_sts.cu).
+class StsBase {
+ public:
+  virtual ~StsBase() {}
+  virtual int record(SolverBase* s) = 0;
+  virtual int count() const = 0;
+  virtual int spectra(double* sts1d, double* sts2d) = 0;
+};
+StsBase* make_sts(int nx, int ny, int nt, void* stream, int* status);
 
 // Host helpers shared by both precisions (vk_host.cpp).
 void twiddle_table(int n, double* out_interleaved);      // exp(-2 pi i k/n), k < n

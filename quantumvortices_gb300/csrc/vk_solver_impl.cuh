@@ -204,6 +204,10 @@ class Solver : public SolverBase {
     std::memcpy(out, &f, sizeof(f));
     return VK_OK;
   }
+  int snapshot_kpsi_f64(void* dst) override {
+    launch_simple("k_to_f64", k_to_f64<T>, (const C*)kpsi_, (double2*)dst, n2_);
+    return check_launch();
+  }
   bool kpsi_is_masked() const override { return kpsi_masked_; }
   void mark_rk4_done() override {
     kpsi_masked_ = true;

@@ -58,7 +58,7 @@ class VkNamelist(C.Structure):
         ("gp_n_obj", C.c_int32),
         ("gp_mass_part", C.c_double), ("ppotd", C.c_double), ("ppotv0", C.c_double), ("ppotthick", C.c_double),
         ("maxiter", C.c_int32), ("fsteps", C.c_int32), ("ssteps", C.c_int32), ("gsteps", C.c_int32),
-        ("nrst", C.c_int32), ("sprst", C.c_int32),
+        ("nrst", C.c_int32), ("sprst", C.c_int32), ("strst", C.c_int32), ("ststeps", C.c_int32),
     ]
 
 
@@ -112,6 +112,11 @@ def load_library(path: str | None = None) -> C.CDLL:
         "vk_ens_report": (C.c_int, [vp, C.c_char_p, C.c_int32]),
         "vk_ens_get_stream": (C.c_int, [vp, C.POINTER(vp)]),
         "vk_ens_kernel_launches": (C.c_int, [vp, C.POINTER(C.c_int64)]),
+        "vk_sts_begin": (C.c_int, [vp, C.c_int32]),
+        "vk_sts_record": (C.c_int, [vp]),
+        "vk_sts_count": (C.c_int, [vp, C.POINTER(C.c_int32)]),
+        "vk_sts_spectra": (C.c_int, [vp, dp, dp]),
+        "vk_sts_end": (C.c_int, [vp]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(lib, name)
@@ -338,6 +343,33 @@ class GPESolver:
         n = C.c_int64()
         _check(self.lib.vk_kernel_launches(self._h, C.byref(n)), "vk_kernel_launches")
         return int(n.value)
+
+    # spatio-temporal spectra (sts_gpe + the Run/CompSTS post-processor)
+    def sts_begin(self, nt: int) -> None:
+        """Device ring for nt kpsi records (nt a power of two, 16..4096)."""
+        self._sts_nt = int(nt)
+        _check(self.lib.vk_sts_begin(self._h, int(nt)), "vk_sts_begin")
+
+    def sts_record(self) -> None:
+        """Appends the current kpsi (sts_gpe, every ststeps)."""
+        _check(self.lib.vk_sts_record(self._h), "vk_sts_record")
+
+    @property
+    def sts_count(self) -> int:
+        n = C.c_int32()
+        _check(self.lib.vk_sts_count(self._h, C.byref(n)), "vk_sts_count")
+        return int(n.value)
+
+    def sts_spectra(self):
+        """(sts1d[nt, ny], sts2d[nt, nx//3 + 1]) of the full ring; consumes it."""
+        nt = self._sts_nt
+        a = np.empty((nt, self.ny))
+        b = np.empty((nt, self.nx // 3 + 1))
+        _check(self.lib.vk_sts_spectra(self._h, _dptr(a), _dptr(b)), "vk_sts_spectra")
+        return a, b
+
+    def sts_end(self) -> None:
+        _check(self.lib.vk_sts_end(self._h), "vk_sts_end")
 
 
 class Ensemble:

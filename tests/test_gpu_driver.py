@@ -81,3 +81,41 @@ def test_driver_argle_with_particles(tmp_path):
     assert (tmp_path / "data/gpobj_frc_2.dat_nrst0").exists()
     eg = (tmp_path / "data/egpobj.dat_nrst0").read_text().splitlines()
     assert len(eg) == 3 and all(re.fullmatch(f"({E156}){{4}}", ln) for ln in eg)
+
+
+def _read_records(path, rec_len):
+    """Fortran sequential-unformatted records of complex128."""
+    raw = open(path, "rb").read()
+    out, i = [], 0
+    while i < len(raw):
+        m = int(np.frombuffer(raw[i:i + 4], dtype=np.int32)[0])
+        assert m == rec_len * 16
+        out.append(np.frombuffer(raw[i + 4:i + 4 + m], dtype=np.complex128))
+        assert int(np.frombuffer(raw[i + 4 + m:i + 8 + m], dtype=np.int32)[0]) == m
+        i += m + 8
+    return np.array(out)
+
+
+def test_driver_sts_path(tmp_path):
+    """--sts NT: the sts_gpe record files every ststeps and, once NT records
+    are held, the spectra of Run/CompSTS (checked against the oracle fed
+    with the driver's own record files)."""
+    from oracle import sts_oracle
+    n, dt, nt, ststeps = 64, 1e-3, 16, 3
+    _write_inputs(tmp_path, n, dt, maxiter=(nt - 1) * ststeps, fsteps=1000, gsteps=1000, ssteps=1000)
+    txt = (tmp_path / "parameter.txt").read_text().replace("gsteps=1000\n", f"gsteps=1000\nststeps={ststeps}\n")
+    (tmp_path / "parameter.txt").write_text(txt)
+    r = subprocess.run([_build.DRIVER, "--sts", str(nt)], cwd=tmp_path, capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0, r.stderr
+    t = (tmp_path / "data/sts_time.dat_nrst0").read_text().split()
+    assert len(t) == nt and abs(float(t[-1]) - (nt - 1) * ststeps * dt) < 1e-9
+    line = _read_records(tmp_path / "data/sts1d/kpsi_x0_nrst0.dat", n)
+    plane = _read_records(tmp_path / "data/sts2d/kpsi_nrst0p1.dat", n * n)
+    assert line.shape == (nt, n) and plane.shape == (nt, n * n)
+    assert np.array_equal(line, plane[:, :n])            # kx = 0 is the first row of kpsi[kx][ky]
+    r1, r2 = sts_oracle.spectra(plane.reshape(nt, n, n))
+    g1 = np.loadtxt(tmp_path / "data/sts1d_kx0_nrst0.dat")
+    g2 = np.loadtxt(tmp_path / "data/sts2d_nrst0.dat")
+    assert g1.shape == r1.shape and g2.shape == r2.shape
+    assert np.abs(g1 - r1).max() <= 1e-12 * np.abs(r1).max()
+    assert np.abs(g2 - r2).max() <= 1e-12 * np.abs(r2).max()

@@ -46,15 +46,16 @@ def test_params_mapping():
 
 def test_namelist_parsing(tmp_path):
     a = tmp_path / "parameter.txt"
-    a.write_text("! Parameters\n&ckprst\nnrst = 0   ! restart\nsprst = 0\n/\n&resolution\nNx=256\nNy=128\n"
-                 "Nz=64\n/\n&tparam\ndt_fix=1.0d-3  ! step\nmaxiter=400000\nfsteps=1000\nssteps=1000\n"
-                 "gsteps=100\n/\n")
+    a.write_text("! Parameters\n&ckprst\nnrst = 0   ! restart\nsprst = 0\nstrst = 2\n/\n&resolution\nNx=256\n"
+                 "Ny=128\nNz=64\n/\n&tparam\ndt_fix=1.0d-3  ! step\nmaxiter=400000\nfsteps=1000\nssteps=1000\n"
+                 "gsteps=100\nststeps=20     ! kpsi 1d-line output frequency\n/\n")
     b = tmp_path / "parameter_gpe.txt"
     b.write_text("&gpparam\nxi=1.0d0 !\ncsound=1.0d0 !\nrho_avg=1.0d0 !\ndisp_factor=0.0d0 !\n/\n"
                  "&gpparticle\ngp_N_obj = 16 !\ngp_mass_part = 100.0d0 !\nppotd = 2.0d0\nppotV0 = 10.0d0 !\n/\n"
                  "&gpotoc\nk_otoc_gp = 1.8d0 !\neps_otoc_gp = 1.0d0-4 !\n/\n")
     nl = vk.read_namelists(str(a), str(b))
     assert (nl.nx, nl.ny, nl.maxiter, nl.fsteps, nl.gsteps) == (256, 128, 400000, 1000, 100)
+    assert (nl.strst, nl.ststeps) == (2, 20)
     assert nl.dt_fix == 1e-3 and nl.gp_n_obj == 16 and nl.ppotv0 == 10.0
     p = vk.derive_params(nl)
     dx = 2 * math.pi / 256
