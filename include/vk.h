@@ -64,6 +64,21 @@ typedef struct vk_params {
   int32_t reserved[8];
 } vk_params;
 
+/* Compile-time branches of the reference, selected at run time
+ * (vk_set_variant).  Only the ones listed as built are accepted. */
+#define VK_VAR_FRCDISP 1 /* -DGPE_FRCDISP: gpe_rhs hypo/hyperviscosity and
+                            random-phase shell forcing (src/gpe.f90:623-658) */
+typedef struct vk_variant {
+  int32_t flags;                      /* VK_VAR_* bits                      */
+  int32_t pad;
+  double vishypo_gp, vishype_gp;      /* &gphypvis (src/driver.f90:68)       */
+  double famp_gp, kf1_gp, kf2_gp;     /* &gpforceparam, kf after *kdx
+                                         (src/driver.f90:67, :384-387)       */
+  uint64_t seed;                      /* counter-based stream of the forcing
+                                         phases (stands in for RANDOM_NUMBER) */
+  int32_t reserved[8];
+} vk_variant;
+
 /* Raw namelist values (src/driver.f90:52-79) -> vk_params, restating
  * set_grid (src/mod_grid.f90:63-101) and src/driver.f90:360-396. */
 typedef struct vk_namelist {
@@ -195,6 +210,16 @@ int vk_timing_end(void* ctx, int32_t cap, char* tags, double* total_ms, int64_t*
  * array: calls that overlap on the GPU race.  Work is queued on `stream`
  * (a cudaStream_t; NULL = legacy default stream) and is not synchronised. */
 int vk_fft2d_forward_noalloc(const double* psi_dev, double* kpsi_dev, int32_t nx, int32_t ny, void* stream);
+
+/* Selects the compile-time branches of v->flags for this context (0 = the
+ * plain equations).  With VK_VAR_FRCDISP every RK4 right-hand side
+ * (gpe_rhs, src/gpe.f90:609-669) becomes
+ *   prefac((alpha k^2 - Omega) kpsi + N^) - vishypo k^-16 kpsi (k != 0)
+ *   - vishype k^16 kpsi + famp exp(i 2 pi u)   (kf1^2 <= k^2 <= kf2^2),
+ * then the 2/3 mask; u is uniform [0,1) from (seed, RHS evaluation count,
+ * mode kx*ny + ky) -- the reference draws RANDOM_NUMBER per mode and RHS.
+ * Not with particles.  Unbuilt flags return VK_E_INVALID. */
+int vk_set_variant(void* ctx, const vk_variant* v);
 
 /* ---- spatio-temporal spectra (the -DGPSTS path) ----
  * Replaces: sts_gpe (src/diagnostics.f90:636-695), called every ststeps

@@ -53,6 +53,8 @@ def lib() -> C.CDLL:
             ("vko_particles_set", None, [vp, dp, dp, dp]), ("vko_particles_get", None, [vp, dp, dp, dp]),
             ("vko_particle_forces", None, [vp, dp]),
             ("vko_count_vortices", None, [vp, ip, ip]), ("vko_set_threads", None, [C.c_int32]),
+            ("vko_set_frcdisp", None, [vp, C.c_int32, C.c_double, C.c_double, C.c_double, C.c_double,
+                                       C.c_double, C.c_uint64]),
         ]:
             f = getattr(L, name)
             f.restype = res
@@ -151,6 +153,10 @@ class Oracle:
         frc = np.zeros((P, 2))
         lib().vko_particle_forces(self._h, _d(frc))
         return frc
+
+    def set_frcdisp(self, on=True, vishypo=0.0, vishype=0.0, famp=0.0, kf1=0.0, kf2=0.0, seed=1):
+        """-DGPE_FRCDISP terms of gpe_rhs (gpe.f90:623-658)."""
+        lib().vko_set_frcdisp(self._h, int(on), vishypo, vishype, famp, kf1, kf2, seed)
 
     def count_vortices(self):
         a, b = C.c_int32(), C.c_int32()

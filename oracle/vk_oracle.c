@@ -55,7 +55,25 @@ struct vko_state {
   double *pos, *vel, *frc, *f0ext, *tpos, *tvel, *ku[4], *kq[4], *shortrange;
   double gpfrcpart[2];
   double gpdeltaE, gpr0obj; /* set by shortrange_repulsion (gpe_particle.f90:395-396) */
+  /* -DGPE_FRCDISP (gpe.f90:623-658): hypo/hyperviscosity, random-phase forcing */
+  int frcdisp;
+  double vishypo, vishype, famp, kf1, kf2;
+  uint64_t seed, ctr; /* forcing phases: uniform(seed, ctr, mode), ctr = RHS evaluations so far */
 };
+
+/* Counter-based uniform [0,1) for the forcing phases: the GPU kernels use
+ * the same definition (SplitMix64 finaliser of seed, counter and mode).  It
+ * stands in for the reference's RANDOM_NUMBER, whose stream is compiler
+ * dependent: parity with the reference is statistical for the forcing. */
+static inline uint64_t mix64(uint64_t z) {
+  z += 0x9E3779B97F4A7C15ull;
+  z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+  z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+  return z ^ (z >> 31);
+}
+static inline double frc_uniform(uint64_t seed, uint64_t ctr, uint64_t mode) {
+  return (double)(mix64(mix64(seed ^ (ctr * 0xD1B54A32D192ED03ull)) + mode) >> 11) * (1.0 / 9007199254740992.0);
+}
 
 /* ---------------------------------------------------------------- grid -- */
 
@@ -487,9 +505,35 @@ static void gpe_rhs(vko_state* s) {
     for (int ky = 0; ky < ny; ++ky) {
       size_t i = (size_t)kx * ny + ky;
       s->nlin[i] = cmul(prefac, cadd(s->tmp1[i], s->nlin[i]));
+      if (s->frcdisp) { /* -DGPE_FRCDISP, :623-658 */
+        const int k1 = s->kwn1[kx], k2 = s->kwn2[ky];
+        const int ksqr = k1 * k1 + k2 * k2;
+        const double kr2 = (double)k1 * k1 + (double)k2 * k2;
+        const double x2 = kr2 * kr2, x4 = x2 * x2, x8 = x4 * x4; /* kradius2**8 */
+        if (ksqr != 0) s->nlin[i] = csub(s->nlin[i], crmul(s->vishypo * (1.0 / x8), s->kpsi[i]));
+        s->nlin[i] = csub(s->nlin[i], crmul(s->vishype * x8, s->kpsi[i]));
+        if ((double)ksqr >= s->kf1 * s->kf1 && (double)ksqr <= s->kf2 * s->kf2) {
+          const double ran = 2.0 * PI * frc_uniform(s->seed, s->ctr, i);
+          s->nlin[i].re += s->famp * cos(ran);
+          s->nlin[i].im += s->famp * sin(ran);
+        }
+      }
       if (masked(s, s->kwn1[kx], s->kwn2[ky])) s->nlin[i].re = s->nlin[i].im = 0.0;
     }
   }
+  if (s->frcdisp) ++s->ctr;
+}
+
+void vko_set_frcdisp(vko_state* s, int32_t on, double vishypo, double vishype, double famp, double kf1,
+                     double kf2, uint64_t seed) {
+  s->frcdisp = on;
+  s->vishypo = vishypo;
+  s->vishype = vishype;
+  s->famp = famp;
+  s->kf1 = kf1;
+  s->kf2 = kf2;
+  s->seed = seed;
+  s->ctr = 0;
 }
 
 /* One RK4 stage update (gpe.f90:366-387, 401-421, 435-455, 469-489). */

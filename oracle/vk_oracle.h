@@ -77,6 +77,10 @@ void vko_particles_get(const vko_state* s, double* pos, double* vel, double* frc
 /* Force on every particle at the current state (translate_particle_potential(i)
  * for i=1..P, diagnostics.f90:528-533); frc[p][d]. */
 void vko_particle_forces(vko_state* s, double* frc);
+/* -DGPE_FRCDISP (gpe.f90:623-658): hypo/hyperviscosity and random-phase
+ * forcing in the shell kf1^2 <= k^2 <= kf2^2 (phases from frc_uniform). */
+void vko_set_frcdisp(vko_state* s, int32_t on, double vishypo, double vishype, double famp, double kf1,
+                     double kf2, uint64_t seed);
 
 /* Signed plaquette winding count on the physical grid (new component). */
 void vko_count_vortices(const vko_state* s, int32_t* n_plus, int32_t* n_minus);

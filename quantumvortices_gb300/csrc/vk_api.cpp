@@ -239,3 +239,12 @@ extern "C" int vk_sts_end(void* ctx) {
   c->sts = nullptr;
   return VK_OK;
 }
+
+extern "C" int vk_set_variant(void* ctx, const vk_variant* v) {
+  VK_CTX_OR_FAIL(ctx);
+  if (!v) {
+    set_error("vk_set_variant: null variant");
+    return VK_E_INVALID;
+  }
+  return c->s->set_variant(v);
+}

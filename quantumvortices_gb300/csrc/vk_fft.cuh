@@ -116,6 +116,40 @@ template <int DIR, typename C> __device__ __forceinline__ void dft16(C* v) {
   }
 }
 
+// 32-point DFT in registers: even/odd DFT16 and one radix-2 layer with the
+// W32^k rotations, k = 0..15 (cos and sin of k*pi/16).
+template <int DIR, typename C> __device__ __forceinline__ void dft32(C* v) {
+  typedef decltype(v[0].x) T;
+  C e[16], o[16];
+#pragma unroll
+  for (int i = 0; i < 16; ++i) { e[i] = v[2 * i]; o[i] = v[2 * i + 1]; }
+  dft16<DIR>(e);
+  dft16<DIR>(o);
+  const T c1 = T(0.98078528040323044912618223613424), s1 = T(0.19509032201612826784828486847702);  // pi/16
+  const T c2 = T(0.92387953251128675612818318939679), s2 = T(0.38268343236508977172845998403040);  // pi/8
+  const T c3 = T(0.83146961230254523707878837761791), s3 = T(0.55557023301960222474283081394853);  // 3pi/16
+  o[1] = rotc<DIR>(o[1], c1, s1);
+  o[2] = rotc<DIR>(o[2], c2, s2);
+  o[3] = rotc<DIR>(o[3], c3, s3);
+  o[4] = rot45<DIR>(o[4]);
+  o[5] = rotc<DIR>(o[5], s3, c3);
+  o[6] = rotc<DIR>(o[6], s2, c2);
+  o[7] = rotc<DIR>(o[7], s1, c1);
+  o[8] = rot90<DIR>(o[8]);
+  o[9] = rot90<DIR>(rotc<DIR>(o[9], c1, s1));
+  o[10] = rot90<DIR>(rotc<DIR>(o[10], c2, s2));
+  o[11] = rot90<DIR>(rotc<DIR>(o[11], c3, s3));
+  o[12] = rot135<DIR>(o[12]);
+  o[13] = rot90<DIR>(rotc<DIR>(o[13], s3, c3));
+  o[14] = rot90<DIR>(rotc<DIR>(o[14], s2, c2));
+  o[15] = rot90<DIR>(rotc<DIR>(o[15], s1, c1));
+#pragma unroll
+  for (int k = 0; k < 16; ++k) {
+    v[k] = cadd(e[k], o[k]);
+    v[k + 16] = csub(e[k], o[k]);
+  }
+}
+
 template <int RAD, int DIR, typename C> __device__ __forceinline__ void dft(C* v) {
   if (RAD == 2) dft2<DIR>(v[0], v[1]);
   else if (RAD == 4) dft4<DIR>(v[0], v[1], v[2], v[3]);
@@ -202,16 +236,60 @@ __device__ __forceinline__ void run_stages(cplx<T>* s, const cplx<T>* tw, RadixL
 
 __host__ __device__ constexpr int plan_maxrad(int e) { return e >= 16 ? 16 : (e >= 8 ? 8 : 4); }
 
+// 1024-point transform of NR rows with one warp per row (FP32): the
+// four-step split 1024 = 32 x 32 inside the warp.  Lane l holds x[l + 32 j]
+// (j = 0..31), does a DFT32 over j, multiplies by W1024^(l k2), and the warp
+// transposes through the row's own shared-memory slots (pitch 33); lane k2
+// then does a DFT32 over l and writes X[k2 + 32 k1] in natural order.  Only
+// __syncwarp between the phases: no block-wide barriers inside the
+// transform.
+template <typename T, int L, int NR, int DIR>
+__device__ __forceinline__ void fft_rows_warp(cplx<T>* s, const cplx<T>* __restrict__ tw) {
+  static_assert(L == 1024, "four-step 32 x 32");
+  typedef cplx<T> C;
+  const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+  if (w < NR) {
+    C* row = s + w * padded(L);
+    C v[32];
+#pragma unroll
+    for (int j = 0; j < 32; ++j) v[j] = row[pidx(l + 32 * j)];
+    dft32<DIR>(v);
+#pragma unroll
+    for (int k2 = 1; k2 < 32; ++k2) {
+      C t = __ldg(tw + l * k2);
+      if (DIR > 0) t.y = -t.y;
+      v[k2] = cmul(v[k2], t);
+    }
+    __syncwarp();
+#pragma unroll
+    for (int k2 = 0; k2 < 32; ++k2) row[k2 * 33 + l] = v[k2];
+    __syncwarp();
+#pragma unroll
+    for (int n1 = 0; n1 < 32; ++n1) v[n1] = row[l * 33 + n1];
+    dft32<DIR>(v);
+    __syncwarp();
+#pragma unroll
+    for (int k1 = 0; k1 < 32; ++k1) row[pidx(l + 32 * k1)] = v[k1];
+  }
+  __syncthreads();
+}
+
 // In-place FFT of the first NR rows of s by threads [0, NTA) of a block of
 // NTB threads; every thread must call it.  The plan's largest radix is the
 // number of points per thread (NR*L/NTA), capped at 16.  The caller must
 // __syncthreads() after filling s; on return s holds the natural-order
 // transform and the block is synchronised.  DIR = -1 forward, +1 inverse.
+// FP32 1024-point rows with at least a warp per row (and every thread of
+// the block active) take the warp-per-row transform instead.
 template <typename T, int L, int NR, int NTA, int DIR, int NTB = NTA>
 __device__ __forceinline__ void fft_rows(cplx<T>* s, const cplx<T>* __restrict__ tw) {
-  constexpr int E = NR * L / NTA;
-  static_assert(E >= 4, "at least four points per thread");
-  run_stages<T, L, NR, NTA, DIR, 1, NTB>(s, tw, typename PlanFor<L, plan_maxrad(E)>::type());
+  if constexpr (sizeof(T) == 4 && L == 1024 && NTA == NTB && NTA >= 32 * NR) {
+    fft_rows_warp<T, L, NR, DIR>(s, tw);
+  } else {
+    constexpr int E = NR * L / NTA;
+    static_assert(E >= 4, "at least four points per thread");
+    run_stages<T, L, NR, NTA, DIR, 1, NTB>(s, tw, typename PlanFor<L, plan_maxrad(E)>::type());
+  }
 }
 
 }  // namespace vk

@@ -45,15 +45,18 @@ inline void ensure_smem_attr(const void* fn, size_t dyn_bytes) {
 // Launch geometry.  x passes (rows y, GeoX) hold R >= 2 rows per CTA so two
 // real rows can share one complex FFT; y passes (rows kx, GeoY) hold R rows.
 // NT = R*L/16 threads: full-height transforms run radix-16 stages, the
-// half-height paired transforms radix-8 stages on the same threads.
+// half-height paired transforms radix-8 stages on the same threads.  FP32
+// at L = 1024 uses one warp per row (NT = 32 R) and the warp-per-row
+// transform of vk_fft.cuh (sizes chosen by a sweep on GB300).
 // MINB is the CTAs per SM the register budget is sized for.
 template <typename T, int L> struct GeoX;
 template <typename T, int L> struct GeoY;
-#define VK_GEO(KIND, TT, LL, RR, MB)                                         \
+#define VK_GEOE(KIND, TT, LL, RR, MB, EE)                                    \
   template <> struct KIND<TT, LL> {                                          \
     static constexpr int L = LL, R = RR, LP = padded(LL), MINB = MB;         \
-    static constexpr int NT = RR * LL / 16;                                  \
+    static constexpr int NT = RR * LL / EE;                                  \
   };
+#define VK_GEO(KIND, TT, LL, RR, MB) VK_GEOE(KIND, TT, LL, RR, MB, 16)
 VK_GEO(GeoX, double, 16, 16, 4) VK_GEO(GeoX, double, 32, 16, 4) VK_GEO(GeoX, double, 64, 16, 4)
 VK_GEO(GeoX, double, 128, 8, 4) VK_GEO(GeoX, double, 256, 4, 4) VK_GEO(GeoX, double, 512, 2, 4)
 VK_GEO(GeoX, double, 1024, 2, 4) VK_GEO(GeoX, double, 2048, 2, 2) VK_GEO(GeoX, double, 4096, 2, 1)
@@ -62,11 +65,12 @@ VK_GEO(GeoY, double, 128, 2, 8) VK_GEO(GeoY, double, 256, 1, 8) VK_GEO(GeoY, dou
 VK_GEO(GeoY, double, 1024, 1, 8) VK_GEO(GeoY, double, 2048, 1, 4) VK_GEO(GeoY, double, 4096, 1, 2)
 VK_GEO(GeoX, float, 16, 16, 4) VK_GEO(GeoX, float, 32, 16, 4) VK_GEO(GeoX, float, 64, 16, 4)
 VK_GEO(GeoX, float, 128, 8, 4) VK_GEO(GeoX, float, 256, 4, 4) VK_GEO(GeoX, float, 512, 2, 8)
-VK_GEO(GeoX, float, 1024, 2, 4) VK_GEO(GeoX, float, 2048, 2, 2) VK_GEO(GeoX, float, 4096, 2, 1)
+VK_GEOE(GeoX, float, 1024, 4, 2, 32) VK_GEO(GeoX, float, 2048, 2, 2) VK_GEO(GeoX, float, 4096, 2, 1)
 VK_GEO(GeoY, float, 16, 16, 4) VK_GEO(GeoY, float, 32, 8, 8) VK_GEO(GeoY, float, 64, 4, 8)
 VK_GEO(GeoY, float, 128, 2, 8) VK_GEO(GeoY, float, 256, 1, 8) VK_GEO(GeoY, float, 512, 1, 8)
-VK_GEO(GeoY, float, 1024, 1, 8) VK_GEO(GeoY, float, 2048, 1, 4) VK_GEO(GeoY, float, 4096, 1, 2)
+VK_GEOE(GeoY, float, 1024, 2, 4, 32) VK_GEO(GeoY, float, 2048, 1, 4) VK_GEO(GeoY, float, 4096, 1, 2)
 #undef VK_GEO
+#undef VK_GEOE
 
 __device__ __forceinline__ int kwn(int i, int n) { return i < n / 2 ? i : i - n; }
 
@@ -116,7 +120,27 @@ struct StepConsts {
   // 0 on the plain FP64 path (the reference's arithmetic); Omega/g on the
   // FP32 path, where it removes the large cancelling g psi / Omega kpsi pair.
   double rho_bg;
+  // -DGPE_FRCDISP (frc != 0): hypo/hyperviscosity and random-phase forcing
+  // in the RK4 right-hand side; the phase counter lives on the device.
+  int frc;
+  double vishypo, vishype, famp, kf1sq, kf2sq;
+  unsigned long long seed;
+  const unsigned long long* rng_ctr;
 };
+
+// Counter-based uniform [0,1) of the forcing phases (SplitMix64 finaliser of
+// seed, RHS-evaluation counter and mode index); the oracle defines the same.
+__host__ __device__ __forceinline__ unsigned long long vk_mix64(unsigned long long z) {
+  z += 0x9E3779B97F4A7C15ull;
+  z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+  z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+  return z ^ (z >> 31);
+}
+__host__ __device__ __forceinline__ double vk_frc_uniform(unsigned long long seed, unsigned long long ctr,
+                                                          unsigned long long mode) {
+  return (double)(vk_mix64(vk_mix64(seed ^ (ctr * 0xD1B54A32D192ED03ull)) + mode) >> 11) *
+         (1.0 / 9007199254740992.0);
+}
 
 // Device view of one field's buffers and constants (ensemble work items
 // index an array of these).
@@ -455,6 +479,7 @@ __device__ __forceinline__ void y2_rk4_body(const cplx<T>* __restrict__ Td, cplx
   const T c1 = T(STAGE == 3 ? c.dt : c.dt * 0.5);
   const T pr = T(c.prefac_re), pi_ = T(c.prefac_im);
   const T al = T(c.alpha), om = T(c.omega);
+  const unsigned long long rctr = c.frc ? *c.rng_ctr : 0ull;
   // batches of B elements per thread: all loads of a batch before any use
   constexpr int PER = G::R * L / G::NT;
   constexpr int B = sizeof(T) == 4 ? (PER < 8 ? PER : 8) : 1;
@@ -488,7 +513,22 @@ __device__ __forceinline__ void y2_rk4_body(const cplx<T>* __restrict__ Td, cplx
         const C nh = s[r * G::LP + pidx(ky)];
         const T kin = al * T(ksq) - (om - T(c.g * c.rho_bg));
         const C t = mkc<T>(kin * ps[j].x + nh.x, kin * ps[j].y + nh.y);
-        const C rhs = mkc<T>(pr * t.x - pi_ * t.y, pr * t.y + pi_ * t.x);
+        C rhs = mkc<T>(pr * t.x - pi_ * t.y, pr * t.y + pi_ * t.x);
+        if (c.frc) {  // src/gpe.f90:623-658, in the reference's order
+          const double kr2 = (double)ksq;
+          const double x2 = kr2 * kr2, x4 = x2 * x2, x8 = x4 * x4;  // kradius2**8
+          if (ksq != 0) {
+            const T a = T(c.vishypo * (1.0 / x8));
+            rhs = mkc<T>(rhs.x - a * ps[j].x, rhs.y - a * ps[j].y);
+          }
+          const T b = T(c.vishype * x8);
+          rhs = mkc<T>(rhs.x - b * ps[j].x, rhs.y - b * ps[j].y);
+          if (kr2 >= c.kf1sq && kr2 <= c.kf2sq) {
+            double sn, cs;
+            sincos(2.0 * 3.14159265358979323846 * vk_frc_uniform(c.seed, rctr, gi), &sn, &cs);
+            rhs = mkc<T>(rhs.x + T(c.famp * cs), rhs.y + T(c.famp * sn));
+          }
+        }
         if (STAGE == 1) {
           str1[gi] = ps[j];
           str2[gi] = mkc<T>(c2 * rhs.x, c2 * rhs.y);

@@ -33,6 +33,8 @@ class SolverBase {
   // Copies kpsi (all nx*ny modes) as FP64 into dst (device double2), on
   // this solver's stream.
   virtual int snapshot_kpsi_f64(void* dst) = 0;
+  // Compile-time branches of the reference selected at run time.
+  virtual int set_variant(const vk_variant* v) = 0;
   virtual bool kpsi_is_masked() const = 0;
   virtual void mark_rk4_done() = 0;
 };

@@ -51,6 +51,10 @@ template <typename T> __global__ void k_to_f64(const cplx<T>* __restrict__ in, d
   for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
     out[i] = make_double2((double)in[i].x, (double)in[i].y);
 }
+// One more right-hand side evaluated: advance the forcing-phase counter
+// (templated so each precision's translation unit has its own symbol).
+template <typename T> __global__ void k_rng_bump(unsigned long long* c) { *c += 1ull; }
+
 template <typename T> __global__ void k_scale_two(cplx<T>* __restrict__ a, cplx<T>* __restrict__ b, size_t n,
                                                   const double* __restrict__ sums, double factor_num) {
   // renormalisation: s = sqrt(Nparticle / norm), norm = factor * sum|kpsi|^2
@@ -119,6 +123,10 @@ class Solver : public SolverBase {
     const int maxblk = std::max(nx_, ny_);
     VK_CUDA_TRY(cudaMalloc(&part_, sizeof(double) * 3 * (size_t)maxblk));
     VK_CUDA_TRY(cudaMalloc(&sums_, sizeof(double) * 8));
+    VK_CUDA_TRY(cudaMalloc(&rngc_, sizeof(unsigned long long)));
+    VK_CUDA_TRY(cudaMemset(rngc_, 0, sizeof(unsigned long long)));
+    c_.frc = 0;
+    c_.rng_ctr = rngc_;
     // twiddle tables
     int trc = upload_twiddles(nx_, &twx_);
     if (trc) return trc;
@@ -203,6 +211,31 @@ class Solver : public SolverBase {
     f.twx = twx_; f.twy = twy_; f.c = c_;
     std::memcpy(out, &f, sizeof(f));
     return VK_OK;
+  }
+  int set_variant(const vk_variant* v) override {
+    if (v->flags & ~VK_VAR_FRCDISP) {
+      set_error("vk_set_variant: only VK_VAR_FRCDISP is built");
+      return VK_E_INVALID;
+    }
+    const double vals[] = {v->vishypo_gp, v->vishype_gp, v->famp_gp, v->kf1_gp, v->kf2_gp};
+    for (double x : vals)
+      if (!std::isfinite(x)) {
+        set_error("vk_set_variant: non-finite parameter");
+        return VK_E_INVALID;
+      }
+    c_.frc = (v->flags & VK_VAR_FRCDISP) ? 1 : 0;
+    c_.vishypo = v->vishypo_gp;
+    c_.vishype = v->vishype_gp;
+    c_.famp = v->famp_gp;
+    c_.kf1sq = v->kf1_gp * v->kf1_gp;
+    c_.kf2sq = v->kf2_gp * v->kf2_gp;
+    c_.seed = v->seed;
+    // the captured step graphs bake the constants in: capture again
+    if (g_rk4_) cudaGraphExecDestroy(g_rk4_);
+    if (g_argle_) cudaGraphExecDestroy(g_argle_);
+    g_rk4_ = g_argle_ = nullptr;
+    VK_CUDA_TRY(cudaMemsetAsync(rngc_, 0, sizeof(unsigned long long), st_));
+    return sync_check();
   }
   int snapshot_kpsi_f64(void* dst) override {
     launch_simple("k_to_f64", k_to_f64<T>, (const C*)kpsi_, (double2*)dst, n2_);
@@ -302,6 +335,7 @@ class Solver : public SolverBase {
         x2(+1, true);
       }
       y2_rk4(stage);
+      if (c_.frc) launch_raw("k_rng_bump", k_rng_bump<T>, 1, 1, 0, rngc_);
       if (np_ > 0) launch_raw("k_part_update", k_part_update, 1, 32, 0, ps_, pc_, stage);
     }
   }
@@ -742,6 +776,8 @@ class Solver : public SolverBase {
     if (stage64_) cudaFree(stage64_);
     if (part_) cudaFree(part_);
     if (sums_) cudaFree(sums_);
+    if (rngc_) cudaFree(rngc_);
+    rngc_ = nullptr;
     if (st_) cudaStreamDestroy(st_);
     psi_ = kpsi_ = str1_ = str2_ = Ta_ = Td_ = Tb_ = Tc_ = twx_ = twy_ = nullptr;
     st_ = nullptr;
@@ -772,6 +808,7 @@ class Solver : public SolverBase {
   bool timing_ = false;
   bool graphs_ok_ = true;
   cudaGraphExec_t g_rk4_ = nullptr, g_argle_ = nullptr;
+  unsigned long long* rngc_ = nullptr;  // forcing-phase counter (RHS evaluations)
   int64_t g_rk4_n_ = 0, g_argle_n_ = 0;
   cudaError_t launch_err_ = cudaSuccess;
   const char* launch_err_tag_ = nullptr;

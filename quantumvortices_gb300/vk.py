@@ -62,6 +62,19 @@ class VkNamelist(C.Structure):
     ]
 
 
+VK_VAR_FRCDISP = 1
+
+
+class VkVariant(C.Structure):
+    """vk_variant: run-time selection of the reference's compile-time branches."""
+    _fields_ = [
+        ("flags", C.c_int32), ("pad", C.c_int32),
+        ("vishypo_gp", C.c_double), ("vishype_gp", C.c_double),
+        ("famp_gp", C.c_double), ("kf1_gp", C.c_double), ("kf2_gp", C.c_double),
+        ("seed", C.c_uint64), ("reserved", C.c_int32 * 8),
+    ]
+
+
 class VkError(RuntimeError):
     pass
 
@@ -112,6 +125,7 @@ def load_library(path: str | None = None) -> C.CDLL:
         "vk_ens_report": (C.c_int, [vp, C.c_char_p, C.c_int32]),
         "vk_ens_get_stream": (C.c_int, [vp, C.POINTER(vp)]),
         "vk_ens_kernel_launches": (C.c_int, [vp, C.POINTER(C.c_int64)]),
+        "vk_set_variant": (C.c_int, [vp, C.POINTER(VkVariant)]),
         "vk_sts_begin": (C.c_int, [vp, C.c_int32]),
         "vk_sts_record": (C.c_int, [vp]),
         "vk_sts_count": (C.c_int, [vp, C.POINTER(C.c_int32)]),
@@ -343,6 +357,16 @@ class GPESolver:
         n = C.c_int64()
         _check(self.lib.vk_kernel_launches(self._h, C.byref(n)), "vk_kernel_launches")
         return int(n.value)
+
+    def set_variant(self, frcdisp: bool = False, vishypo: float = 0.0, vishype: float = 0.0, famp: float = 0.0,
+                    kf1: float = 0.0, kf2: float = 0.0, seed: int = 1) -> None:
+        """-DGPE_FRCDISP: hypo/hyperviscosity and random-phase shell forcing in
+        every RK4 right-hand side (src/gpe.f90:623-658); kf in units of kdx."""
+        v = VkVariant()
+        v.flags = VK_VAR_FRCDISP if frcdisp else 0
+        v.vishypo_gp, v.vishype_gp, v.famp_gp, v.kf1_gp, v.kf2_gp = vishypo, vishype, famp, kf1, kf2
+        v.seed = seed
+        _check(self.lib.vk_set_variant(self._h, C.byref(v)), "vk_set_variant")
 
     # spatio-temporal spectra (sts_gpe + the Run/CompSTS post-processor)
     def sts_begin(self, nt: int) -> None:

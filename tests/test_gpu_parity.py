@@ -131,6 +131,32 @@ def test_fp32_bulk_error_vs_fp64_oracle():
     s.close()
 
 
+@pytest.mark.parametrize("n", [512, 1024, 2048])
+def test_fp32_forward_fft(n):
+    """The FP32 transforms (1024: the warp-per-row four-step transform)
+    against numpy's FP64 FFT: relative L2 <= 1e-6."""
+    p = vk.params_for(n, precision=vk.VK_PREC_FP32, otoc=False)
+    psi0, _ = vk.ic_vortices(n, n, 8, seed=2)
+    with vk.GPESolver(p) as s:
+        s.set_psi(psi0)
+        ref = np.fft.fft2(psi0).T                      # transposed Fourier layout [kx][ky]
+        assert rel(s.get_kpsi(), ref) < 1e-6
+        s.set_kpsi(ref)                                # F^-1 through the FP32 inverse passes
+        assert rel(s.get_psi(), psi0) < 1e-6
+
+
+def test_fp32_1024_rk4_vs_fp64():
+    """FP32 bulk at 1024^2 (warp-per-row transforms) against the FP64 path
+    after 100 RK4 steps: relative L2 <= 5e-6."""
+    out = {}
+    for prec in (vk.VK_PREC_FP64, vk.VK_PREC_FP32):
+        with vk.GPESolver(vk.params_for(1024, dt=5e-4, precision=prec)) as s:
+            s.set_psi_vortices(64, seed=1, min_sep=4 * np.sqrt(2) * 2 * np.pi / 1024)
+            s.gpe_rk4(100)
+            out[prec] = s.get_psi()
+    assert rel(out[vk.VK_PREC_FP32], out[vk.VK_PREC_FP64]) < 5e-6
+
+
 def test_state_errors():
     p = vk.params_for(32)
     s = vk.GPESolver(p)
