@@ -66,14 +66,19 @@ typedef struct vk_params {
 
 /* Compile-time branches of the reference, selected at run time
  * (vk_set_variant).  Only the ones listed as built are accepted. */
-#define VK_VAR_FRCDISP 1 /* -DGPE_FRCDISP: gpe_rhs hypo/hyperviscosity and
-                            random-phase shell forcing (src/gpe.f90:623-658) */
+#define VK_VAR_FRCDISP 1     /* -DGPE_FRCDISP: gpe_rhs hypo/hyperviscosity and
+                                random-phase shell forcing (src/gpe.f90:623-658) */
+#define VK_VAR_ADVECTION 2   /* -DGPE_ADVECTION: ARGLE Taylor-Green advection
+                                (src/gpe.f90:78-81, 93-96, 115-131)         */
+#define VK_VAR_COUNTERFLOW 4 /* -DGPE_COUNTERFLOW: ARGLE constant counterflow
+                                (src/gpe.f90:78-81, 93-96, 135-145)         */
 typedef struct vk_variant {
   int32_t flags;                      /* VK_VAR_* bits                      */
   int32_t pad;
   double vishypo_gp, vishype_gp;      /* &gphypvis (src/driver.f90:68)       */
   double famp_gp, kf1_gp, kf2_gp;     /* &gpforceparam, kf after *kdx
                                          (src/driver.f90:67, :384-387)       */
+  double vnx, vny;                    /* &gpcounterflow (src/driver.f90:61)  */
   uint64_t seed;                      /* counter-based stream of the forcing
                                          phases (stands in for RANDOM_NUMBER) */
   int32_t reserved[8];
@@ -218,7 +223,13 @@ int vk_fft2d_forward_noalloc(const double* psi_dev, double* kpsi_dev, int32_t nx
  *   - vishype k^16 kpsi + famp exp(i 2 pi u)   (kf1^2 <= k^2 <= kf2^2),
  * then the 2/3 mask; u is uniform [0,1) from (seed, RHS evaluation count,
  * mode kx*ny + ky) -- the reference draws RANDOM_NUMBER per mode and RHS.
- * Not with particles.  Unbuilt flags return VK_E_INVALID. */
+ * With VK_VAR_ADVECTION or VK_VAR_COUNTERFLOW (one of them) every ARGLE step
+ * adds to N = -g P_G rho psi, with grad psi = F^-1[i k kpsi]:
+ *   advection   -i u.grad psi - (1/4)(1/alpha)|u|^2 psi,
+ *               u = (sin x cos y, -cos x sin y);
+ *   counterflow -i (vnx, vny).grad psi.
+ * The flow terms need nx <= 2048 (FP64) and no particles.  Unbuilt flags
+ * return VK_E_INVALID. */
 int vk_set_variant(void* ctx, const vk_variant* v);
 
 /* ---- spatio-temporal spectra (the -DGPSTS path) ----

@@ -55,6 +55,7 @@ def lib() -> C.CDLL:
             ("vko_count_vortices", None, [vp, ip, ip]), ("vko_set_threads", None, [C.c_int32]),
             ("vko_set_frcdisp", None, [vp, C.c_int32, C.c_double, C.c_double, C.c_double, C.c_double,
                                        C.c_double, C.c_uint64]),
+            ("vko_set_argle_flow", None, [vp, C.c_int32, C.c_double, C.c_double]),
         ]:
             f = getattr(L, name)
             f.restype = res
@@ -157,6 +158,10 @@ class Oracle:
     def set_frcdisp(self, on=True, vishypo=0.0, vishype=0.0, famp=0.0, kf1=0.0, kf2=0.0, seed=1):
         """-DGPE_FRCDISP terms of gpe_rhs (gpe.f90:623-658)."""
         lib().vko_set_frcdisp(self._h, int(on), vishypo, vishype, famp, kf1, kf2, seed)
+
+    def set_argle_flow(self, mode, vnx=0.0, vny=0.0):
+        """ARGLE flow terms (gpe.f90:78-146): 1 advection, 2 counterflow."""
+        lib().vko_set_argle_flow(self._h, int(mode), vnx, vny)
 
     def count_vortices(self):
         a, b = C.c_int32(), C.c_int32()

@@ -59,6 +59,9 @@ struct vko_state {
   int frcdisp;
   double vishypo, vishype, famp, kf1, kf2;
   uint64_t seed, ctr; /* forcing phases: uniform(seed, ctr, mode), ctr = RHS evaluations so far */
+  /* ARGLE flow terms: 1 = -DGPE_ADVECTION (Taylor-Green), 2 = -DGPE_COUNTERFLOW */
+  int flow;
+  double vnx, vny;
 };
 
 /* Counter-based uniform [0,1) for the forcing phases: the GPU kernels use
@@ -585,6 +588,17 @@ static double argle_step(vko_state* s) {
   const double alpha = s->p.alpha, g = s->p.gstrength, om = s->p.omega_chem, dt = s->p.dt;
   fft_inv(s, s->kpsi, s->psi); /* :42 */
   if (s->np > 0) translate_particle_potential(s, 0); /* :50-53 */
+  if (s->flow) { /* :78-81, 93-96: gradients of psi in physical space */
+    for (int kx = 0; kx < nx; ++kx)
+      for (int ky = 0; ky < ny; ++ky) {
+        size_t i = (size_t)kx * ny + ky;
+        cx ikx = {0.0, (double)s->kwn1[kx]}, iky = {0.0, (double)s->kwn2[ky]};
+        s->tmp1[i] = cmul(ikx, s->kpsi[i]);
+        s->tmp2[i] = cmul(iky, s->kpsi[i]);
+      }
+    fft_inv(s, s->tmp1, s->tmp1);
+    fft_inv(s, s->tmp2, s->tmp2);
+  }
   for (size_t i = 0; i < s->n2; ++i) { /* :56-60 */
     double a = cabs_f(s->psi[i]);
     s->nlin[i].re = a * a;
@@ -601,6 +615,18 @@ static double argle_step(vko_state* s) {
   for (size_t i = 0; i < s->n2; ++i) { /* :101-112 */
     cx t = cmul(crmul(-g, s->nlin[i]), s->psi[i]);
     if (s->np > 0) t = cadd(t, cmul(crmul(-1.0, s->trans_vobj[i]), s->psi[i]));
+    if (s->flow == 1) { /* :115-131, x = (i1-1) dx, y = (i2-1) dy */
+      const double x = (double)(i % (size_t)nx) * s->dx, y = (double)(i / (size_t)nx) * s->dy;
+      const double uadx = sin(x) * cos(y), uady = -cos(x) * sin(y);
+      cx v = cadd(crmul(uadx, s->tmp1[i]), crmul(uady, s->tmp2[i]));
+      cx miv = {v.im, -v.re}; /* -zi*(uadx*aa1+uady*aa2) */
+      t = cadd(t, miv);
+      t = csub(t, crmul((0.5 * 0.5) * (1.0 / alpha) * (uadx * uadx + uady * uady), s->psi[i]));
+    } else if (s->flow == 2) { /* :135-145 */
+      cx v = cadd(crmul(s->vnx, s->tmp1[i]), crmul(s->vny, s->tmp2[i]));
+      cx miv = {v.im, -v.re};
+      t = cadd(t, miv);
+    }
     s->nlin[i] = t;
   }
   fft_fwd(s, s->nlin, s->nlin); /* :170 */
@@ -632,6 +658,12 @@ static double argle_step(vko_state* s) {
     for (size_t i = 0; i < s->n2; ++i) s->kpsi[i] = crmul(f, s->kpsi[i]);
   }
   return sqrt(dsum) / (dt * sqrt(osum));
+}
+
+void vko_set_argle_flow(vko_state* s, int32_t mode, double vnx, double vny) {
+  s->flow = mode;
+  s->vnx = vnx;
+  s->vny = vny;
 }
 
 void vko_argle(vko_state* s, int32_t nsteps, double* residual) {

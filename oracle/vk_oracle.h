@@ -81,6 +81,9 @@ void vko_particle_forces(vko_state* s, double* frc);
  * forcing in the shell kf1^2 <= k^2 <= kf2^2 (phases from frc_uniform). */
 void vko_set_frcdisp(vko_state* s, int32_t on, double vishypo, double vishype, double famp, double kf1,
                      double kf2, uint64_t seed);
+/* ARGLE flow terms (gpe.f90:78-146): mode 1 = -DGPE_ADVECTION (Taylor-Green
+ * u = (sin x cos y, -cos x sin y)), 2 = -DGPE_COUNTERFLOW (u = (vnx, vny)). */
+void vko_set_argle_flow(vko_state* s, int32_t mode, double vnx, double vny);
 
 /* Signed plaquette winding count on the physical grid (new component). */
 void vko_count_vortices(const vko_state* s, int32_t* n_plus, int32_t* n_minus);

@@ -201,8 +201,9 @@ __global__ void __launch_bounds__(GeoY<T, L>::NT, GeoY<T, L>::MINB) k_yfwd(const
   }
 }
 
-// rows kx of src[kx][ky] -> F^-1_y -> dst[y][kx] (pitch nx).
-template <typename T, int L>
+// rows kx of src[kx][ky] -> F^-1_y -> dst[y][kx] (pitch nx).  DERIV: of
+// i*ky*src instead (the y-derivative, ARGLE flow terms).
+template <typename T, int L, bool DERIV = false>
 __global__ void __launch_bounds__(GeoY<T, L>::NT, GeoY<T, L>::MINB) k_yinv(const cplx<T>* __restrict__ src, cplx<T>* __restrict__ dst,
                                                      const cplx<T>* __restrict__ tw, int nx) {
   typedef GeoY<T, L> G;
@@ -210,7 +211,12 @@ __global__ void __launch_bounds__(GeoY<T, L>::NT, GeoY<T, L>::MINB) k_yinv(const
   extern __shared__ __align__(16) unsigned char smraw[];
   C* s = reinterpret_cast<C*>(smraw);
   const int x0 = blockIdx.x * G::R;
-  stage_rows<T, L, G::R, G::NT, G::LP>(s, [&](int r, int y) { return src[(size_t)(x0 + r) * L + y]; });
+  stage_rows<T, L, G::R, G::NT, G::LP>(s, [&](int r, int y) {
+    const C v = src[(size_t)(x0 + r) * L + y];
+    if (!DERIV) return v;
+    const T k = T(kwn(y, L));
+    return mkc<T>(-k * v.y, k * v.x);
+  });
   __syncthreads();
   fft_rows<T, L, G::R, G::NT, +1>(s, tw);
   for (int e = threadIdx.x; e < G::R * L; e += G::NT) {
@@ -455,8 +461,10 @@ __global__ void __launch_bounds__(GeoX<T, L>::NT, GeoX<T, L>::MINB) k_x2(const c
 // Y2 (RK4 stage STAGE = 1..4): rows |kx| <= K of Td: F_y -> N^ ->
 // rhs = prefac*((alpha k^2 - Omega) kpsi + N^), masked (src/gpe.f90:609-669)
 // then the stage update of src/gpe.f90:366-489; kpsi_new --F^-1_y--> Ta.
+// FRC: the -DGPE_FRCDISP terms (a separate instantiation, so the plain
+// kernel carries none of their registers).
 // ------------------------------------------------------------------------
-template <typename T, int L, class G, int STAGE>
+template <typename T, int L, class G, int STAGE, bool FRC = false>
 __device__ __forceinline__ void y2_rk4_body(const cplx<T>* __restrict__ Td, cplx<T>* __restrict__ kpsi,
                                                        cplx<T>* __restrict__ str1, cplx<T>* __restrict__ str2,
                                                        cplx<T>* __restrict__ Ta, const cplx<T>* __restrict__ tw,
@@ -479,7 +487,7 @@ __device__ __forceinline__ void y2_rk4_body(const cplx<T>* __restrict__ Td, cplx
   const T c1 = T(STAGE == 3 ? c.dt : c.dt * 0.5);
   const T pr = T(c.prefac_re), pi_ = T(c.prefac_im);
   const T al = T(c.alpha), om = T(c.omega);
-  const unsigned long long rctr = c.frc ? *c.rng_ctr : 0ull;
+  const unsigned long long rctr = FRC ? *c.rng_ctr : 0ull;
   // batches of B elements per thread: all loads of a batch before any use
   constexpr int PER = G::R * L / G::NT;
   constexpr int B = sizeof(T) == 4 ? (PER < 8 ? PER : 8) : 1;
@@ -514,7 +522,7 @@ __device__ __forceinline__ void y2_rk4_body(const cplx<T>* __restrict__ Td, cplx
         const T kin = al * T(ksq) - (om - T(c.g * c.rho_bg));
         const C t = mkc<T>(kin * ps[j].x + nh.x, kin * ps[j].y + nh.y);
         C rhs = mkc<T>(pr * t.x - pi_ * t.y, pr * t.y + pi_ * t.x);
-        if (c.frc) {  // src/gpe.f90:623-658, in the reference's order
+        if (FRC) {  // src/gpe.f90:623-658, in the reference's order
           const double kr2 = (double)ksq;
           const double x2 = kr2 * kr2, x4 = x2 * x2, x8 = x4 * x4;  // kradius2**8
           if (ksq != 0) {
@@ -555,13 +563,13 @@ __device__ __forceinline__ void y2_rk4_body(const cplx<T>* __restrict__ Td, cplx
   }
 }
 
-template <typename T, int L, int STAGE>
+template <typename T, int L, int STAGE, bool FRC = false>
 __global__ void __launch_bounds__(GeoY<T, L>::NT, GeoY<T, L>::MINB) k_y2_rk4(const cplx<T>* __restrict__ Td, cplx<T>* __restrict__ kpsi,
                                                        cplx<T>* __restrict__ str1, cplx<T>* __restrict__ str2,
                                                        cplx<T>* __restrict__ Ta, const cplx<T>* __restrict__ tw,
                                                        StepConsts c) {
   extern __shared__ __align__(16) unsigned char smraw[];
-  y2_rk4_body<T, L, GeoY<T, L>, STAGE>(Td, kpsi, str1, str2, Ta, tw, c, blockIdx.x, reinterpret_cast<cplx<T>*>(smraw));
+  y2_rk4_body<T, L, GeoY<T, L>, STAGE, FRC>(Td, kpsi, str1, str2, Ta, tw, c, blockIdx.x, reinterpret_cast<cplx<T>*>(smraw));
 }
 
 // ------------------------------------------------------------------------
@@ -570,10 +578,11 @@ __global__ void __launch_bounds__(GeoY<T, L>::NT, GeoY<T, L>::MINB) k_y2_rk4(con
 // kpsi_new --F^-1_y--> Ta.  RESID: per-CTA FP64 partial sums of
 // |new-old|^2, |old|^2, |new|^2 into part[blockIdx][3].
 // ------------------------------------------------------------------------
-template <typename T, int L, class G, bool RESID>
+template <typename T, int L, class G, bool RESID, bool DERIV = false>
 __device__ __forceinline__ void y2_argle_body(const cplx<T>* __restrict__ Td, cplx<T>* __restrict__ kpsi,
                                                          cplx<T>* __restrict__ Ta, const cplx<T>* __restrict__ tw,
-                                                         double* __restrict__ part, StepConsts c, const int tile, cplx<T>* __restrict__ s) {
+                                                         double* __restrict__ part, StepConsts c, const int tile, cplx<T>* __restrict__ s,
+                                                         cplx<T>* __restrict__ Tg = nullptr) {
   typedef cplx<T> C;
   static_assert(G::NT <= 512, "reduction buffer");
   __shared__ double red[3][512];
@@ -610,6 +619,7 @@ __device__ __forceinline__ void y2_argle_body(const cplx<T>* __restrict__ Td, cp
     nw.y = nw.y / t2;
     kpsi[gi] = nw;
     s[r * G::LP + pidx(ky)] = nw;
+    if (DERIV) s[(G::R + r) * G::LP + pidx(ky)] = mkc<T>(-T(k2) * nw.y, T(k2) * nw.x);  // i ky kpsi
     if (RESID) {
       const double dx = (double)nw.x - (double)old.x, dy = (double)nw.y - (double)old.y;
       dsum += dx * dx + dy * dy;
@@ -632,18 +642,116 @@ __device__ __forceinline__ void y2_argle_body(const cplx<T>* __restrict__ Td, cp
     part[tile * 3 + 2] = d;
   }
   fft_rows<T, L, G::R, G::NT, +1>(s, tw);
+  if (DERIV) fft_rows<T, L, G::R, G::NT, +1>(s + G::R * G::LP, tw);
   for (int e = threadIdx.x; e < G::R * L; e += G::NT) {
     const int r = e % G::R, y = e / G::R;
     Ta[(size_t)y * nx + x0 + r] = s[r * G::LP + pidx(y)];
+    if (DERIV) Tg[(size_t)y * nx + x0 + r] = s[(G::R + r) * G::LP + pidx(y)];
   }
 }
 
-template <typename T, int L, bool RESID>
+template <typename T, int L, bool RESID, bool DERIV = false>
 __global__ void __launch_bounds__(GeoY<T, L>::NT, GeoY<T, L>::MINB) k_y2_argle(const cplx<T>* __restrict__ Td, cplx<T>* __restrict__ kpsi,
                                                          cplx<T>* __restrict__ Ta, const cplx<T>* __restrict__ tw,
-                                                         double* __restrict__ part, StepConsts c) {
+                                                         double* __restrict__ part, StepConsts c,
+                                                         cplx<T>* __restrict__ Tg = nullptr) {
   extern __shared__ __align__(16) unsigned char smraw[];
-  y2_argle_body<T, L, GeoY<T, L>, RESID>(Td, kpsi, Ta, tw, part, c, blockIdx.x, reinterpret_cast<cplx<T>*>(smraw));
+  y2_argle_body<T, L, GeoY<T, L>, RESID, DERIV>(Td, kpsi, Ta, tw, part, c, blockIdx.x,
+                                                reinterpret_cast<cplx<T>*>(smraw), Tg);
+}
+
+// ------------------------------------------------------------------------
+// X2 for ARGLE with the flow terms of src/gpe.f90:78-146: rows y of
+// Tc -> P_G rho (two real rows per F^-1_x); rows of i*kx*Ta and of Tg
+// (= F^-1_y[i ky kpsi]) -> F^-1_x -> grad psi; N = -g P_G rho psi plus
+//   FLOW 1 (-DGPE_ADVECTION): -i(u.grad psi) - (1/4)(1/alpha)|u|^2 psi,
+//          u = (sin x cos y, -cos x sin y) at x = i1 dx, y = i2 dy;
+//   FLOW 2 (-DGPE_COUNTERFLOW): -i(v.grad psi), v = (vnx, vny);
+// then F_x -> Td[kx][y] (all kx).  Shared memory: 3 R rows.
+// ------------------------------------------------------------------------
+template <typename T, int L, int FLOW>
+__global__ void __launch_bounds__(GeoX<T, L>::NT, 1) k_x2_flow(const cplx<T>* __restrict__ Tc, const cplx<T>* __restrict__ psi,
+                                                             const cplx<T>* __restrict__ Ta, const cplx<T>* __restrict__ Tg,
+                                                             cplx<T>* __restrict__ Td, const cplx<T>* __restrict__ tw,
+                                                             StepConsts c, double vnx, double vny) {
+  typedef GeoX<T, L> G;
+  typedef cplx<T> C;
+  extern __shared__ __align__(16) unsigned char smraw[];
+  C* s = reinterpret_cast<C*>(smraw);
+  C* sg = s + G::R * G::LP;  // rows [0,R): d/dx psi, [R,2R): d/dy psi
+  const int y0 = blockIdx.x * G::R;
+  const int K = c.K, ny = c.ny, pk = c.pk;
+  constexpr int NPAIR = G::R / 2;
+  stage_rows<T, L, NPAIR, G::NT, G::LP>(s, [&](int p, int k) {
+    C v = mkc<T>(T(0), T(0));
+    const size_t ra = (size_t)(y0 + 2 * p) * pk, rb = ra + pk;
+    if (k <= K) {
+      const C a = Tc[ra + k], b = Tc[rb + k];
+      v = mkc<T>(a.x - b.y, a.y + b.x);
+    } else if (k >= L - K) {
+      const C a = Tc[ra + (L - k)], b = Tc[rb + (L - k)];
+      v = mkc<T>(a.x + b.y, b.x - a.y);
+    }
+    return v;
+  });
+  stage_rows<T, L, 2 * G::R, G::NT, G::LP>(sg, [&](int r, int k) {
+    if (r < G::R) {
+      const C v = Ta[(size_t)(y0 + r) * L + k];
+      const T kx = T(kwn(k, L));
+      return mkc<T>(-kx * v.y, kx * v.x);
+    }
+    return Tg[(size_t)(y0 + r - G::R) * L + k];
+  });
+  __syncthreads();
+  fft_rows<T, L, NPAIR, G::NT, +1, G::NT>(s, tw);
+  fft_rows<T, L, 2 * G::R, G::NT, +1>(sg, tw);
+  constexpr int PER = G::R * L / G::NT;
+  C nv[PER];
+  const T gs = T(-c.g);
+  const T scale = T(c.scale);
+  const double two_pi = 6.283185307179586476925286766559;
+  const double dx = two_pi / L, dy = two_pi / ny;
+#pragma unroll
+  for (int q = 0; q < PER; ++q) {
+    const int e = threadIdx.x + q * G::NT;
+    const int r = e / L, x = e % L;
+    const C z = s[(r >> 1) * G::LP + pidx(x)];
+    const T pg = ((r & 1) == 0 ? z.x : z.y) * scale;
+    const C ps = psi[(size_t)(y0 + r) * L + x];
+    const T gp = gs * pg;
+    C n = mkc<T>(gp * ps.x, gp * ps.y);
+    const C a1 = cscale(sg[r * G::LP + pidx(x)], scale), a2 = cscale(sg[(G::R + r) * G::LP + pidx(x)], scale);
+    T ux, uy;
+    if (FLOW == 1) {
+      double sx, cx, sy, cy;
+      sincos(x * dx, &sx, &cx);
+      sincos((y0 + r) * dy, &sy, &cy);
+      ux = T(sx * cy);
+      uy = T(-cx * sy);
+    } else {
+      ux = T(vnx);
+      uy = T(vny);
+    }
+    const C v = mkc<T>(ux * a1.x + uy * a2.x, ux * a1.y + uy * a2.y);
+    n = mkc<T>(n.x + v.y, n.y - v.x);  // -i v
+    if (FLOW == 1) {
+      const T w = T(0.25 * (1.0 / c.alpha)) * (ux * ux + uy * uy);
+      n = mkc<T>(n.x - w * ps.x, n.y - w * ps.y);
+    }
+    nv[q] = n;
+  }
+  __syncthreads();
+#pragma unroll
+  for (int q = 0; q < PER; ++q) {
+    const int e = threadIdx.x + q * G::NT;
+    s[(e / L) * G::LP + pidx(e % L)] = nv[q];
+  }
+  __syncthreads();
+  fft_rows<T, L, G::R, G::NT, -1>(s, tw);
+  for (int e = threadIdx.x; e < G::R * L; e += G::NT) {
+    const int r = e % G::R, k = e / G::R;
+    Td[(size_t)k * ny + y0 + r] = s[r * G::LP + pidx(k)];
+  }
 }
 
 // Seeded vortex state (vk_common.cu).

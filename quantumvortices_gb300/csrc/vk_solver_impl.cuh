@@ -213,11 +213,20 @@ class Solver : public SolverBase {
     return VK_OK;
   }
   int set_variant(const vk_variant* v) override {
-    if (v->flags & ~VK_VAR_FRCDISP) {
-      set_error("vk_set_variant: only VK_VAR_FRCDISP is built");
+    if (v->flags & ~(VK_VAR_FRCDISP | VK_VAR_ADVECTION | VK_VAR_COUNTERFLOW)) {
+      set_error("vk_set_variant: only VK_VAR_FRCDISP, VK_VAR_ADVECTION and VK_VAR_COUNTERFLOW are built");
       return VK_E_INVALID;
     }
-    const double vals[] = {v->vishypo_gp, v->vishype_gp, v->famp_gp, v->kf1_gp, v->kf2_gp};
+    const int flow = (v->flags & VK_VAR_ADVECTION) ? 1 : ((v->flags & VK_VAR_COUNTERFLOW) ? 2 : 0);
+    if ((v->flags & VK_VAR_ADVECTION) && (v->flags & VK_VAR_COUNTERFLOW)) {
+      set_error("vk_set_variant: advection and counterflow are exclusive");
+      return VK_E_INVALID;
+    }
+    if (flow && (np_ > 0 || (sizeof(T) == 8 && nx_ > 2048))) {
+      set_error("vk_set_variant: the ARGLE flow terms need no particles and nx <= 2048 in FP64");
+      return VK_E_INVALID;
+    }
+    const double vals[] = {v->vishypo_gp, v->vishype_gp, v->famp_gp, v->kf1_gp, v->kf2_gp, v->vnx, v->vny};
     for (double x : vals)
       if (!std::isfinite(x)) {
         set_error("vk_set_variant: non-finite parameter");
@@ -230,6 +239,10 @@ class Solver : public SolverBase {
     c_.kf1sq = v->kf1_gp * v->kf1_gp;
     c_.kf2sq = v->kf2_gp * v->kf2_gp;
     c_.seed = v->seed;
+    flow_ = flow;
+    vnx_ = v->vnx;
+    vny_ = v->vny;
+    if (flow_ && !Tg_) VK_CUDA_TRY(cudaMalloc(&Tg_, n2_ * sizeof(C)));
     // the captured step graphs bake the constants in: capture again
     if (g_rk4_) cudaGraphExecDestroy(g_rk4_);
     if (g_argle_) cudaGraphExecDestroy(g_argle_);
@@ -402,6 +415,9 @@ class Solver : public SolverBase {
     if (np_ > 0) {
       y1_pot(false, nullptr);
       x2_pot(-1);
+    } else if (flow_) {
+      y1();
+      x2_flow();
     } else {
       y1();
       x2(-1, false);
@@ -424,6 +440,7 @@ class Solver : public SolverBase {
     if (nsteps <= 0) return VK_OK;
     if (np_ > 0 && !have_particles_) { set_error("vk_argle: particles not set"); return VK_E_STATE; }
     if (ta_ != TA_FULL) yinv_to_ta();
+    if (flow_) yinv_deriv_to_tg();
     const int nblk = nx_ / geo_rows_y(ny_);
     if (np_ > 0) part_tables();
     for (int s = 0; s < nsteps; ++s) {
@@ -634,6 +651,28 @@ class Solver : public SolverBase {
                    (const C*)twx_, T(c_.scale), K_);
     });
   }
+  void yinv_deriv_to_tg() {
+    with_len(ny_, [&](auto lc) {
+      constexpr int L = decltype(lc)::value;
+      typedef GeoY<T, L> G;
+      launch_raw("k_yinv", k_yinv<T, L, true>, nx_ / G::R, G::NT, sizeof(C) * G::R * G::LP, (const C*)kpsi_, Tg_, (const C*)twy_, nx_);
+    });
+  }
+  void x2_flow() {
+    with_len(nx_, [&](auto lc) {
+      constexpr int L = decltype(lc)::value;
+      if constexpr (sizeof(T) == 4 || L <= 2048) {
+        typedef GeoX<T, L> G;
+        const size_t sm = sizeof(C) * 3 * G::R * G::LP;
+        if (flow_ == 1)
+          launch_raw("k_x2_flow", k_x2_flow<T, L, 1>, ny_ / G::R, G::NT, sm, (const C*)Tc_, (const C*)psi_, (const C*)Ta_,
+                     (const C*)Tg_, Td_, (const C*)twx_, c_, vnx_, vny_);
+        else
+          launch_raw("k_x2_flow", k_x2_flow<T, L, 2>, ny_ / G::R, G::NT, sm, (const C*)Tc_, (const C*)psi_, (const C*)Ta_,
+                     (const C*)Tg_, Td_, (const C*)twx_, c_, vnx_, vny_);
+      }
+    });
+  }
   void yinv_to_ta() {
     with_len(ny_, [&](auto lc) {
       constexpr int L = decltype(lc)::value;
@@ -687,12 +726,17 @@ class Solver : public SolverBase {
       typedef GeoY<T, L> G;
       const int grid = (2 * K_ + 1 + G::R - 1) / G::R;
       const size_t sm = sizeof(C) * G::R * G::LP;
-      switch (stage) {
-        case 1: launch_raw("k_y2_rk4", k_y2_rk4<T, L, 1>, grid, G::NT, sm, (const C*)Td_, kpsi_, str1_, str2_, Ta_, (const C*)twy_, c_); break;
-        case 2: launch_raw("k_y2_rk4", k_y2_rk4<T, L, 2>, grid, G::NT, sm, (const C*)Td_, kpsi_, str1_, str2_, Ta_, (const C*)twy_, c_); break;
-        case 3: launch_raw("k_y2_rk4", k_y2_rk4<T, L, 3>, grid, G::NT, sm, (const C*)Td_, kpsi_, str1_, str2_, Ta_, (const C*)twy_, c_); break;
-        default: launch_raw("k_y2_rk4", k_y2_rk4<T, L, 4>, grid, G::NT, sm, (const C*)Td_, kpsi_, str1_, str2_, Ta_, (const C*)twy_, c_); break;
-      }
+      auto go = [&](auto frc_c) {
+        constexpr bool F = decltype(frc_c)::value;
+        switch (stage) {
+          case 1: launch_raw("k_y2_rk4", k_y2_rk4<T, L, 1, F>, grid, G::NT, sm, (const C*)Td_, kpsi_, str1_, str2_, Ta_, (const C*)twy_, c_); break;
+          case 2: launch_raw("k_y2_rk4", k_y2_rk4<T, L, 2, F>, grid, G::NT, sm, (const C*)Td_, kpsi_, str1_, str2_, Ta_, (const C*)twy_, c_); break;
+          case 3: launch_raw("k_y2_rk4", k_y2_rk4<T, L, 3, F>, grid, G::NT, sm, (const C*)Td_, kpsi_, str1_, str2_, Ta_, (const C*)twy_, c_); break;
+          default: launch_raw("k_y2_rk4", k_y2_rk4<T, L, 4, F>, grid, G::NT, sm, (const C*)Td_, kpsi_, str1_, str2_, Ta_, (const C*)twy_, c_); break;
+        }
+      };
+      if (c_.frc) go(std::true_type());
+      else go(std::false_type());
     });
   }
   void y2_argle(bool resid) {
@@ -700,8 +744,11 @@ class Solver : public SolverBase {
       constexpr int L = decltype(lc)::value;
       typedef GeoY<T, L> G;
       const size_t sm = sizeof(C) * G::R * G::LP;
-      if (resid) launch_raw("k_y2_argle", k_y2_argle<T, L, true>, nx_ / G::R, G::NT, sm, (const C*)Td_, kpsi_, Ta_, (const C*)twy_, part_, c_);
-      else launch_raw("k_y2_argle", k_y2_argle<T, L, false>, nx_ / G::R, G::NT, sm, (const C*)Td_, kpsi_, Ta_, (const C*)twy_, part_, c_);
+      if (flow_) {
+        if (resid) launch_raw("k_y2_argle", k_y2_argle<T, L, true, true>, nx_ / G::R, G::NT, 2 * sm, (const C*)Td_, kpsi_, Ta_, (const C*)twy_, part_, c_, Tg_);
+        else launch_raw("k_y2_argle", k_y2_argle<T, L, false, true>, nx_ / G::R, G::NT, 2 * sm, (const C*)Td_, kpsi_, Ta_, (const C*)twy_, part_, c_, Tg_);
+      } else if (resid) launch_raw("k_y2_argle", k_y2_argle<T, L, true>, nx_ / G::R, G::NT, sm, (const C*)Td_, kpsi_, Ta_, (const C*)twy_, part_, c_, (C*)nullptr);
+      else launch_raw("k_y2_argle", k_y2_argle<T, L, false>, nx_ / G::R, G::NT, sm, (const C*)Td_, kpsi_, Ta_, (const C*)twy_, part_, c_, (C*)nullptr);
     });
   }
 
@@ -778,6 +825,8 @@ class Solver : public SolverBase {
     if (sums_) cudaFree(sums_);
     if (rngc_) cudaFree(rngc_);
     rngc_ = nullptr;
+    if (Tg_) cudaFree(Tg_);
+    Tg_ = nullptr;
     if (st_) cudaStreamDestroy(st_);
     psi_ = kpsi_ = str1_ = str2_ = Ta_ = Td_ = Tb_ = Tc_ = twx_ = twy_ = nullptr;
     st_ = nullptr;
@@ -809,6 +858,9 @@ class Solver : public SolverBase {
   bool graphs_ok_ = true;
   cudaGraphExec_t g_rk4_ = nullptr, g_argle_ = nullptr;
   unsigned long long* rngc_ = nullptr;  // forcing-phase counter (RHS evaluations)
+  int flow_ = 0;                          // ARGLE flow terms: 1 advection, 2 counterflow
+  double vnx_ = 0.0, vny_ = 0.0;
+  C* Tg_ = nullptr;                       // F^-1_y[i ky kpsi] for the flow terms
   int64_t g_rk4_n_ = 0, g_argle_n_ = 0;
   cudaError_t launch_err_ = cudaSuccess;
   const char* launch_err_tag_ = nullptr;

@@ -63,6 +63,8 @@ class VkNamelist(C.Structure):
 
 
 VK_VAR_FRCDISP = 1
+VK_VAR_ADVECTION = 2
+VK_VAR_COUNTERFLOW = 4
 
 
 class VkVariant(C.Structure):
@@ -71,6 +73,7 @@ class VkVariant(C.Structure):
         ("flags", C.c_int32), ("pad", C.c_int32),
         ("vishypo_gp", C.c_double), ("vishype_gp", C.c_double),
         ("famp_gp", C.c_double), ("kf1_gp", C.c_double), ("kf2_gp", C.c_double),
+        ("vnx", C.c_double), ("vny", C.c_double),
         ("seed", C.c_uint64), ("reserved", C.c_int32 * 8),
     ]
 
@@ -359,12 +362,17 @@ class GPESolver:
         return int(n.value)
 
     def set_variant(self, frcdisp: bool = False, vishypo: float = 0.0, vishype: float = 0.0, famp: float = 0.0,
-                    kf1: float = 0.0, kf2: float = 0.0, seed: int = 1) -> None:
+                    kf1: float = 0.0, kf2: float = 0.0, seed: int = 1, flow: str | None = None,
+                    vnx: float = 0.0, vny: float = 0.0) -> None:
         """-DGPE_FRCDISP: hypo/hyperviscosity and random-phase shell forcing in
-        every RK4 right-hand side (src/gpe.f90:623-658); kf in units of kdx."""
+        every RK4 right-hand side (src/gpe.f90:623-658); kf in units of kdx.
+        flow = "advection" / "counterflow": the ARGLE flow terms
+        (src/gpe.f90:78-146), counterflow velocity (vnx, vny)."""
         v = VkVariant()
-        v.flags = VK_VAR_FRCDISP if frcdisp else 0
+        v.flags = (VK_VAR_FRCDISP if frcdisp else 0) | {None: 0, "advection": VK_VAR_ADVECTION,
+                                                        "counterflow": VK_VAR_COUNTERFLOW}[flow]
         v.vishypo_gp, v.vishype_gp, v.famp_gp, v.kf1_gp, v.kf2_gp = vishypo, vishype, famp, kf1, kf2
+        v.vnx, v.vny = vnx, vny
         v.seed = seed
         _check(self.lib.vk_set_variant(self._h, C.byref(v)), "vk_set_variant")
 

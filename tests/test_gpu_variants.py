@@ -64,6 +64,49 @@ def test_frcdisp_fp32_and_reset():
 def test_unbuilt_variant_flags_are_rejected():
     with vk.GPESolver(vk.params_for(32)) as s:
         v = vk.VkVariant()
-        v.flags = 2
+        v.flags = 8                     # not a built branch
+        with pytest.raises(vk.VkError, match="VK_E_INVALID"):
+            vk._check(s.lib.vk_set_variant(s._h, vk.C.byref(v)), "vk_set_variant")
+
+
+@pytest.mark.parametrize("n", [64, 256])
+@pytest.mark.parametrize("flow,vel", [("counterflow", (0.3, -0.2)), ("advection", (0.0, 0.0))])
+def test_argle_flow_matches_oracle(n, flow, vel):
+    p = vk.params_for(n, dt=1e-3)
+    psi0, _ = vk.ic_vortices(n, n, 8, seed=6)
+    mode = {"advection": 1, "counterflow": 2}[flow]
+    with vk.GPESolver(p) as s:
+        s.set_psi(psi0)
+        s.set_variant(flow=flow, vnx=vel[0], vny=vel[1])
+        r1 = s.argle(20)
+        r2 = s.argle(30)
+        got = s.get_kpsi()
+    o = Oracle.from_vk_params(p)
+    o.set_psi(psi0)
+    o.set_argle_flow(mode, *vel)
+    o.argle(20)
+    ro = o.argle(30)
+    assert rel(got, o.get_kpsi()) < 1e-12
+    assert abs(r2 - ro) <= 1e-9 * abs(ro) and np.isfinite(r1)
+
+
+def test_argle_flow_fp32():
+    n = 128
+    psi0, _ = vk.ic_vortices(n, n, 8, seed=6)
+    o = Oracle.from_vk_params(vk.params_for(n, dt=1e-3))
+    o.set_psi(psi0)
+    o.set_argle_flow(1)
+    o.argle(50)
+    with vk.GPESolver(vk.params_for(n, dt=1e-3, precision=vk.VK_PREC_FP32)) as s:
+        s.set_psi(psi0)
+        s.set_variant(flow="advection")
+        s.argle(50)
+        assert rel(s.get_kpsi(), o.get_kpsi()) < 1e-5
+
+
+def test_flow_rejections():
+    with vk.GPESolver(vk.params_for(32)) as s:
+        v = vk.VkVariant()
+        v.flags = vk.VK_VAR_ADVECTION | vk.VK_VAR_COUNTERFLOW
         with pytest.raises(vk.VkError, match="VK_E_INVALID"):
             vk._check(s.lib.vk_set_variant(s._h, vk.C.byref(v)), "vk_set_variant")

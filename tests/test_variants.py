@@ -73,3 +73,47 @@ def test_hyperviscosity_damps_high_modes_more():
     hi = (kk[:, None] ** 2 + kk[None, :] ** 2) >= 64
     assert np.linalg.norm(k1[hi]) < np.linalg.norm(k2[hi])
     assert np.isfinite(k0).all()
+
+
+def test_counterflow_on_a_plane_wave_is_a_chemical_potential_shift():
+    """g = 0, psi = exp(i k.x): grad psi = i k psi, so the counterflow term
+    -i v.grad psi = (v.k) psi and one ARGLE step multiplies the mode by
+    (1 + dt (v.k + Omega)) / (1 + alpha k^2 dt)  (src/gpe.f90:135-145, 199-203)."""
+    n, dt = 32, 1e-3
+    p = vk.params_for(n, dt=dt)
+    p.gstrength = 0.0
+    o = Oracle.from_vk_params(p)
+    x = np.arange(n) * 2 * math.pi / n
+    kx, ky = 2, -3
+    psi = np.exp(1j * (kx * x[None, :] + ky * x[:, None]))
+    o.set_psi(psi, otoc=False)
+    vnx, vny = 0.3, -0.7
+    o.set_argle_flow(2, vnx, vny)
+    steps = 5
+    o.argle(steps)
+    f = (1 + dt * (vnx * kx + vny * ky + p.omega_chem)) / (1 + p.alpha * (kx * kx + ky * ky) * dt)
+    want = n * n * f ** steps
+    got = o.get_kpsi()[kx % n, ky % n]
+    assert abs(got - want) <= 1e-12 * abs(want)
+
+
+def test_advection_velocity_field_is_taylor_green():
+    """The advection term with psi = 1 (grad psi = 0) is -(1/4)(1/alpha)|u|^2,
+    |u|^2 = sin^2 x cos^2 y + cos^2 x sin^2 y: one step from psi = 1 with
+    g = 0 changes kpsi by dt * F[-(1/4)(1/alpha)|u|^2] / (1 + alpha k^2 dt)."""
+    n, dt = 32, 1e-3
+    p = vk.params_for(n, dt=dt)
+    p.gstrength = 0.0
+    o = Oracle.from_vk_params(p)
+    o.set_psi(np.ones((n, n), dtype=complex), otoc=False)
+    o.set_argle_flow(1)
+    k0 = o.get_kpsi()
+    o.argle(1)
+    x = np.arange(n) * 2 * math.pi / n
+    X, Y = np.meshgrid(x, x)
+    u2 = (np.sin(X) * np.cos(Y)) ** 2 + (np.cos(X) * np.sin(Y)) ** 2
+    nhat = np.fft.fft2(-0.25 / p.alpha * u2).T
+    k = np.array([i if i < n // 2 else i - n for i in range(n)])
+    denom = 1 + p.alpha * (k[:, None] ** 2 + k[None, :] ** 2) * dt
+    want = (k0 + dt * (nhat + p.omega_chem * k0)) / denom
+    assert np.abs(o.get_kpsi() - want).max() <= 1e-12 * np.abs(want).max()
