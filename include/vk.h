@@ -72,6 +72,10 @@ typedef struct vk_params {
                                 (src/gpe.f90:78-81, 93-96, 115-131)         */
 #define VK_VAR_COUNTERFLOW 4 /* -DGPE_COUNTERFLOW: ARGLE constant counterflow
                                 (src/gpe.f90:78-81, 93-96, 135-145)         */
+#define VK_VAR_SGLE 8        /* -DGPE_SGLE: ARGLE noise and chemical-potential
+                                ODE (src/gpe.f90:149-178, 199-219, 226-274)  */
+#define VK_VAR_SELFTRUNC 16  /* -DGPE_SELFTRUNC with SGLE: kpsi = 0 for
+                                k^2 > ktrunc^2 (src/gpe.f90:213-217)        */
 typedef struct vk_variant {
   int32_t flags;                      /* VK_VAR_* bits                      */
   int32_t pad;
@@ -79,6 +83,8 @@ typedef struct vk_variant {
   double famp_gp, kf1_gp, kf2_gp;     /* &gpforceparam, kf after *kdx
                                          (src/driver.f90:67, :384-387)       */
   double vnx, vny;                    /* &gpcounterflow (src/driver.f90:61)  */
+  double oneybeta, nuN, chempot0;     /* &gpfiniteT (src/driver.f90:59)      */
+  double ktrunc;                      /* &selftruncation (src/driver.f90:64) */
   uint64_t seed;                      /* counter-based stream of the forcing
                                          phases (stands in for RANDOM_NUMBER) */
   int32_t reserved[8];
@@ -228,9 +234,19 @@ int vk_fft2d_forward_noalloc(const double* psi_dev, double* kpsi_dev, int32_t nx
  *   advection   -i u.grad psi - (1/4)(1/alpha)|u|^2 psi,
  *               u = (sin x cos y, -cos x sin y);
  *   counterflow -i (vnx, vny).grad psi.
- * The flow terms need nx <= 2048 (FP64) and no particles.  Unbuilt flags
- * return VK_E_INVALID. */
+ * The flow terms need nx <= 2048 (FP64) and no particles.
+ * With VK_VAR_SGLE the chemical potential starts at chempot0 and before
+ * every ARGLE update becomes omega - dt nuN/(Lx Ly) (norm - Lx Ly)
+ * (finiteT_adhoc_chempot, src/gpe.f90:226-264), and the update adds
+ * sqrt(dt) F[noise] (2/3 mask), noise = (v1 + i v2) sqrt(oneybeta/(2 alpha))
+ * /sqrt(dvol) with standard normals v1, v2 per point from the same
+ * counter-based stream (the reference: the polar method on RANDOM_NUMBER,
+ * so parity with it is statistical).  VK_VAR_SELFTRUNC then zeroes
+ * k^2 > ktrunc^2.  Unbuilt flags return VK_E_INVALID. */
 int vk_set_variant(void* ctx, const vk_variant* v);
+/* Current chemical potential omega_chem (changes under VK_VAR_SGLE;
+ * write_chempot_for_restart, src/gpe.f90:266-300, writes it). */
+int vk_get_chempot(void* ctx, double* omega);
 
 /* ---- spatio-temporal spectra (the -DGPSTS path) ----
  * Replaces: sts_gpe (src/diagnostics.f90:636-695), called every ststeps

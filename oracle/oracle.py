@@ -56,6 +56,9 @@ def lib() -> C.CDLL:
             ("vko_set_frcdisp", None, [vp, C.c_int32, C.c_double, C.c_double, C.c_double, C.c_double,
                                        C.c_double, C.c_uint64]),
             ("vko_set_argle_flow", None, [vp, C.c_int32, C.c_double, C.c_double]),
+            ("vko_set_sgle", None, [vp, C.c_int32, C.c_double, C.c_double, C.c_double, C.c_int32, C.c_double,
+                                    C.c_uint64]),
+            ("vko_chempot", C.c_double, [vp]),
         ]:
             f = getattr(L, name)
             f.restype = res
@@ -162,6 +165,14 @@ class Oracle:
     def set_argle_flow(self, mode, vnx=0.0, vny=0.0):
         """ARGLE flow terms (gpe.f90:78-146): 1 advection, 2 counterflow."""
         lib().vko_set_argle_flow(self._h, int(mode), vnx, vny)
+
+    def set_sgle(self, on=True, oneybeta=0.0, nuN=0.0, chempot0=1.0, selftrunc=False, ktrunc=0.0, seed=1):
+        """-DGPE_SGLE noise and chemical potential ODE (gpe.f90:149-274)."""
+        lib().vko_set_sgle(self._h, int(on), oneybeta, nuN, chempot0, int(selftrunc), ktrunc, seed)
+
+    @property
+    def chempot(self):
+        return float(lib().vko_chempot(self._h))
 
     def count_vortices(self):
         a, b = C.c_int32(), C.c_int32()

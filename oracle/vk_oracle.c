@@ -62,6 +62,9 @@ struct vko_state {
   /* ARGLE flow terms: 1 = -DGPE_ADVECTION (Taylor-Green), 2 = -DGPE_COUNTERFLOW */
   int flow;
   double vnx, vny;
+  /* -DGPE_SGLE (gpe.f90:149-178, 199-219, 226-274) and -DGPE_SELFTRUNC */
+  int sgle, selftrunc;
+  double noisesigma, nuN, ktrunc;
 };
 
 /* Counter-based uniform [0,1) for the forcing phases: the GPU kernels use
@@ -76,6 +79,16 @@ static inline uint64_t mix64(uint64_t z) {
 }
 static inline double frc_uniform(uint64_t seed, uint64_t ctr, uint64_t mode) {
   return (double)(mix64(mix64(seed ^ (ctr * 0xD1B54A32D192ED03ull)) + mode) >> 11) * (1.0 / 9007199254740992.0);
+}
+
+/* Standard normal pair for the SGLE noise at point idx (Box-Muller on two
+ * counter-based uniforms; the reference uses the polar method on
+ * RANDOM_NUMBER, so parity with it is statistical). */
+static inline void sgle_normals(uint64_t seed, uint64_t ctr, uint64_t idx, double* v1, double* v2) {
+  const double u1 = 1.0 - frc_uniform(seed, ctr, 2 * idx), u2 = frc_uniform(seed, ctr, 2 * idx + 1);
+  const double r = sqrt(-2.0 * log(u1));
+  *v1 = r * cos(2.0 * PI * u2);
+  *v2 = r * sin(2.0 * PI * u2);
 }
 
 /* ---------------------------------------------------------------- grid -- */
@@ -585,8 +598,27 @@ void vko_gpe_rk4(vko_state* s, int32_t nsteps) {
  * optional renormalisation (neither exists in the reference). */
 static double argle_step(vko_state* s) {
   const int nx = s->nx, ny = s->ny;
-  const double alpha = s->p.alpha, g = s->p.gstrength, om = s->p.omega_chem, dt = s->p.dt;
+  const double alpha = s->p.alpha, g = s->p.gstrength, dt = s->p.dt;
   fft_inv(s, s->kpsi, s->psi); /* :42 */
+  if (s->sgle) {
+    /* noise (:149-165) and the ad hoc chemical potential (:189, :226-264);
+     * the norm uses psi of this step, so computing it first changes nothing */
+    const double f = (1.0 / sqrt(s->dvol)) * s->noisesigma;
+    double norm = 0.0;
+    for (size_t i = 0; i < s->n2; ++i) {
+      double v1, v2;
+      sgle_normals(s->seed, s->ctr, i, &v1, &v2);
+      s->cmpxtmp[i].re = v1 * f;
+      s->cmpxtmp[i].im = v2 * f;
+      const double a = cabs_f(s->psi[i]);
+      norm = norm + a * a;
+    }
+    norm = norm * s->dvol;
+    s->p.omega_chem = s->p.omega_chem - dt * (s->nuN / (s->lx * s->ly)) * (norm - s->nparticle);
+    fft_fwd(s, s->cmpxtmp, s->cmpxtmp); /* :192 */
+    ++s->ctr;
+  }
+  const double om = s->p.omega_chem;
   if (s->np > 0) translate_particle_potential(s, 0); /* :50-53 */
   if (s->flow) { /* :78-81, 93-96: gradients of psi in physical space */
     for (int kx = 0; kx < nx; ++kx)
@@ -642,8 +674,14 @@ static double argle_step(vko_state* s) {
       cx t1 = cadd(s->nlin[i], crmul(om, old));
       double t2 = 1.0 + alpha * kr2 * dt;
       cx nw = cadd(old, crmul(dt, t1));
+      if (s->sgle) { /* :199-212 */
+        cx noise = crmul(sqrt(dt), s->cmpxtmp[i]);
+        if (masked(s, s->kwn1[kx], s->kwn2[ky])) noise.re = noise.im = 0.0;
+        nw = cadd(nw, noise);
+      }
       nw.re /= t2;
       nw.im /= t2;
+      if (s->sgle && s->selftrunc && kr2 > s->ktrunc * s->ktrunc) nw.re = nw.im = 0.0; /* :213-217 */
       s->kpsi[i] = nw;
       cx dd = csub(nw, old);
       dsum += dd.re * dd.re + dd.im * dd.im;
@@ -659,6 +697,19 @@ static double argle_step(vko_state* s) {
   }
   return sqrt(dsum) / (dt * sqrt(osum));
 }
+
+void vko_set_sgle(vko_state* s, int32_t on, double oneybeta, double nuN, double chempot0, int32_t selftrunc,
+                  double ktrunc, uint64_t seed) {
+  s->sgle = on;
+  s->noisesigma = sqrt((1.0 / (2.0 * s->p.alpha)) * oneybeta); /* driver.f90:376 */
+  s->nuN = nuN;
+  s->selftrunc = selftrunc;
+  s->ktrunc = ktrunc;
+  s->seed = seed;
+  s->ctr = 0;
+  if (on) s->p.omega_chem = chempot0; /* driver.f90:372 */
+}
+double vko_chempot(const vko_state* s) { return s->p.omega_chem; }
 
 void vko_set_argle_flow(vko_state* s, int32_t mode, double vnx, double vny) {
   s->flow = mode;

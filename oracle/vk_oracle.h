@@ -84,6 +84,12 @@ void vko_set_frcdisp(vko_state* s, int32_t on, double vishypo, double vishype, d
 /* ARGLE flow terms (gpe.f90:78-146): mode 1 = -DGPE_ADVECTION (Taylor-Green
  * u = (sin x cos y, -cos x sin y)), 2 = -DGPE_COUNTERFLOW (u = (vnx, vny)). */
 void vko_set_argle_flow(vko_state* s, int32_t mode, double vnx, double vny);
+/* -DGPE_SGLE (gpe.f90:149-178, 199-219, 226-274): noise of amplitude
+ * noisesigma/sqrt(dvol), noisesigma = sqrt(oneybeta/(2 alpha)), and the
+ * chemical potential ODE from chempot0; -DGPE_SELFTRUNC zeroes k^2 > ktrunc^2. */
+void vko_set_sgle(vko_state* s, int32_t on, double oneybeta, double nuN, double chempot0, int32_t selftrunc,
+                  double ktrunc, uint64_t seed);
+double vko_chempot(const vko_state* s);
 
 /* Signed plaquette winding count on the physical grid (new component). */
 void vko_count_vortices(const vko_state* s, int32_t* n_plus, int32_t* n_minus);

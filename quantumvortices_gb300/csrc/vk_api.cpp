@@ -248,3 +248,12 @@ extern "C" int vk_set_variant(void* ctx, const vk_variant* v) {
   }
   return c->s->set_variant(v);
 }
+
+extern "C" int vk_get_chempot(void* ctx, double* omega) {
+  VK_CTX_OR_FAIL(ctx);
+  if (!omega) {
+    set_error("vk_get_chempot: null output");
+    return VK_E_INVALID;
+  }
+  return c->s->get_chempot(omega);
+}

@@ -4,6 +4,15 @@
 
 namespace vk {
 
+__global__ void k_chempot(const double* __restrict__ part, int nblk, double* __restrict__ omega, double dt,
+                          double nun_area, double dvol, double nparticle) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  double norm = 0.0;
+  for (int i = 0; i < nblk; ++i) norm += part[i];
+  norm = norm * dvol;
+  *omega = *omega - dt * nun_area * (norm - nparticle);
+}
+
 // Fixed-order sum of per-CTA partials part[i*3 + j] -> out[j], j = 0..2.
 // One block; each thread strides the partial list, then a fixed-shape tree.
 __global__ void k_reduce_partials3(const double* __restrict__ part, int nblk, double* __restrict__ out) {

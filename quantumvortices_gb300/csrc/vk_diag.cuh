@@ -463,7 +463,7 @@ struct Diagnostics {
     }
     const double two_pi = 6.283185307179586476925286766559;
     const double dvol = (two_pi / nx) * (two_pi / ny), area = two_pi * two_pi;
-    const double al = S_.p_.alpha, g = S_.p_.gstrength, om = S_.p_.omega_chem;
+    const double al = S_.p_.alpha, g = S_.p_.gstrength, om = S_.c_.omega;  // omega_chem (evolves under SGLE)
     double sums[DS_N];
     for (int j = 0; j < DS_N; ++j) sums[j] = neumaier_sum(part.data() + j, nblk_x, 8);
     const double momx = 2.0 * al * sums[DS_MOMX] * dvol / area;

@@ -126,6 +126,11 @@ struct StepConsts {
   double vishypo, vishype, famp, kf1sq, kf2sq;
   unsigned long long seed;
   const unsigned long long* rng_ctr;
+  // -DGPE_SGLE: the chemical potential evolves on the device; noise
+  // amplitude noisesigma/sqrt(dvol); -DGPE_SELFTRUNC cut k^2 > ktrunc^2.
+  const double* omega_dev;
+  double sgle_amp, sqrt_dt, ktrunc2;
+  int selftrunc;
 };
 
 // Counter-based uniform [0,1) of the forcing phases (SplitMix64 finaliser of
@@ -140,6 +145,17 @@ __host__ __device__ __forceinline__ double vk_frc_uniform(unsigned long long see
                                                           unsigned long long mode) {
   return (double)(vk_mix64(vk_mix64(seed ^ (ctr * 0xD1B54A32D192ED03ull)) + mode) >> 11) *
          (1.0 / 9007199254740992.0);
+}
+// Standard normal pair of the SGLE noise at point idx: Box-Muller on two
+// counter-based uniforms (the oracle defines the same).
+__device__ __forceinline__ void vk_sgle_normals(unsigned long long seed, unsigned long long ctr,
+                                                unsigned long long idx, double* v1, double* v2) {
+  const double u1 = 1.0 - vk_frc_uniform(seed, ctr, 2 * idx), u2 = vk_frc_uniform(seed, ctr, 2 * idx + 1);
+  const double r = sqrt(-2.0 * log(u1));
+  double sn, cs;
+  sincos(2.0 * 3.14159265358979323846 * u2, &sn, &cs);
+  *v1 = r * cs;
+  *v2 = r * sn;
 }
 
 // Device view of one field's buffers and constants (ensemble work items
@@ -578,20 +594,27 @@ __global__ void __launch_bounds__(GeoY<T, L>::NT, GeoY<T, L>::MINB) k_y2_rk4(con
 // kpsi_new --F^-1_y--> Ta.  RESID: per-CTA FP64 partial sums of
 // |new-old|^2, |old|^2, |new|^2 into part[blockIdx][3].
 // ------------------------------------------------------------------------
-template <typename T, int L, class G, bool RESID, bool DERIV = false>
+template <typename T, int L, class G, bool RESID, bool DERIV = false, bool SGLE = false>
 __device__ __forceinline__ void y2_argle_body(const cplx<T>* __restrict__ Td, cplx<T>* __restrict__ kpsi,
                                                          cplx<T>* __restrict__ Ta, const cplx<T>* __restrict__ tw,
                                                          double* __restrict__ part, StepConsts c, const int tile, cplx<T>* __restrict__ s,
-                                                         cplx<T>* __restrict__ Tg = nullptr) {
+                                                         cplx<T>* __restrict__ Tg = nullptr,
+                                                         const cplx<T>* __restrict__ Tn = nullptr) {
   typedef cplx<T> C;
   static_assert(G::NT <= 512, "reduction buffer");
   __shared__ double red[3][512];
   const int x0 = tile * G::R;
   const int nx = c.nx;
   stage_rows<T, L, G::R, G::NT, G::LP>(s, [&](int r, int y) { return Td[(size_t)(x0 + r) * L + y]; });
+  // SGLE: the x-spectrum of the noise, rows kx, in the second R rows (the
+  // derivative rows of DERIV reuse them: each slot is read, then written, by
+  // the same thread)
+  cplx<T>* sn = s + G::R * G::LP;
+  if (SGLE) stage_rows<T, L, G::R, G::NT, G::LP>(sn, [&](int r, int y) { return Tn[(size_t)(x0 + r) * L + y]; });
   __syncthreads();
   fft_rows<T, L, G::R, G::NT, -1>(s, tw);
-  const T al = T(c.alpha), om = T(c.omega), dt = T(c.dt);
+  if (SGLE) fft_rows<T, L, G::R, G::NT, -1>(sn, tw);
+  const T al = T(c.alpha), om = T(SGLE ? *c.omega_dev : c.omega), dt = T(c.dt);
   double dsum = 0.0, osum = 0.0, nsum = 0.0;
   constexpr int PER = G::R * L / G::NT;
   constexpr int B = sizeof(T) == 4 ? (PER < 8 ? PER : 8) : 1;
@@ -615,8 +638,14 @@ __device__ __forceinline__ void y2_argle_body(const cplx<T>* __restrict__ Td, cp
     const C t1 = mkc<T>(nh.x + omb * old.x, nh.y + omb * old.y);
     const T t2 = T(1) + al * T(k1 * k1 + k2 * k2) * dt;
     C nw = mkc<T>(old.x + dt * t1.x, old.y + dt * t1.y);
+    if (SGLE && k1 * k1 + k2 * k2 <= c.k2max) {  // noise_term = F[noise] sqrt(dt), masked (:199-209)
+      const C z = sn[r * G::LP + pidx(ky)];
+      const T sd = T(c.sqrt_dt);
+      nw = mkc<T>(nw.x + sd * z.x, nw.y + sd * z.y);
+    }
     nw.x = nw.x / t2;
     nw.y = nw.y / t2;
+    if (SGLE && c.selftrunc && (double)(k1 * k1 + k2 * k2) > c.ktrunc2) nw = mkc<T>(T(0), T(0));  // :213-217
     kpsi[gi] = nw;
     s[r * G::LP + pidx(ky)] = nw;
     if (DERIV) s[(G::R + r) * G::LP + pidx(ky)] = mkc<T>(-T(k2) * nw.y, T(k2) * nw.x);  // i ky kpsi
@@ -650,15 +679,65 @@ __device__ __forceinline__ void y2_argle_body(const cplx<T>* __restrict__ Td, cp
   }
 }
 
-template <typename T, int L, bool RESID, bool DERIV = false>
+template <typename T, int L, bool RESID, bool DERIV = false, bool SGLE = false>
 __global__ void __launch_bounds__(GeoY<T, L>::NT, GeoY<T, L>::MINB) k_y2_argle(const cplx<T>* __restrict__ Td, cplx<T>* __restrict__ kpsi,
                                                          cplx<T>* __restrict__ Ta, const cplx<T>* __restrict__ tw,
                                                          double* __restrict__ part, StepConsts c,
-                                                         cplx<T>* __restrict__ Tg = nullptr) {
+                                                         cplx<T>* __restrict__ Tg = nullptr,
+                                                         const cplx<T>* __restrict__ Tn = nullptr) {
   extern __shared__ __align__(16) unsigned char smraw[];
-  y2_argle_body<T, L, GeoY<T, L>, RESID, DERIV>(Td, kpsi, Ta, tw, part, c, blockIdx.x,
-                                                reinterpret_cast<cplx<T>*>(smraw), Tg);
+  y2_argle_body<T, L, GeoY<T, L>, RESID, DERIV, SGLE>(Td, kpsi, Ta, tw, part, c, blockIdx.x,
+                                                      reinterpret_cast<cplx<T>*>(smraw), Tg, Tn);
 }
+
+// SGLE noise (src/gpe.f90:149-165): rows y, noise(x, y) = (v1 + i v2)
+// noisesigma/sqrt(dvol) from the counter-based normals of point y*nx + x,
+// F_x -> Tn[kx][y] (all kx).
+template <typename T, int L>
+__global__ void __launch_bounds__(GeoX<T, L>::NT, GeoX<T, L>::MINB) k_noise_x(cplx<T>* __restrict__ Tn,
+                                                             const cplx<T>* __restrict__ tw, StepConsts c) {
+  typedef GeoX<T, L> G;
+  typedef cplx<T> C;
+  extern __shared__ __align__(16) unsigned char smraw[];
+  C* s = reinterpret_cast<C*>(smraw);
+  const int y0 = blockIdx.x * G::R;
+  const unsigned long long ctr = *c.rng_ctr;
+  for (int e = threadIdx.x; e < G::R * L; e += G::NT) {
+    const int r = e / L, x = e % L;
+    double v1, v2;
+    vk_sgle_normals(c.seed, ctr, (unsigned long long)(y0 + r) * L + x, &v1, &v2);
+    s[r * G::LP + pidx(x)] = mkc<T>(T(v1 * c.sgle_amp), T(v2 * c.sgle_amp));
+  }
+  __syncthreads();
+  fft_rows<T, L, G::R, G::NT, -1>(s, tw);
+  for (int e = threadIdx.x; e < G::R * L; e += G::NT) {
+    const int r = e % G::R, k = e / G::R;
+    Tn[(size_t)k * c.ny + y0 + r] = s[r * G::LP + pidx(k)];
+  }
+}
+
+// Per-block sums of |psi|^2 (Fortran ABS squared), fixed order.
+template <typename T>
+__global__ void k_sum_abs2(const cplx<T>* __restrict__ psi, size_t n, double* __restrict__ part) {
+  __shared__ double sh[256];
+  double a = 0.0;
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+    const double h = hypot((double)psi[i].x, (double)psi[i].y);
+    a += h * h;
+  }
+  sh[threadIdx.x] = a;
+  __syncthreads();
+  for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+    if ((int)threadIdx.x < o) sh[threadIdx.x] += sh[threadIdx.x + o];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) part[blockIdx.x] = sh[0];
+}
+
+// finiteT_adhoc_chempot (src/gpe.f90:226-264): omega -= dt nuN/(Lx Ly)
+// (norm - Nparticle), norm = dvol sum |psi|^2.  One thread.
+__global__ void k_chempot(const double* __restrict__ part, int nblk, double* __restrict__ omega, double dt,
+                          double nun_area, double dvol, double nparticle);
 
 // ------------------------------------------------------------------------
 // X2 for ARGLE with the flow terms of src/gpe.f90:78-146: rows y of

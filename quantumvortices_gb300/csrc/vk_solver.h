@@ -35,6 +35,7 @@ class SolverBase {
   virtual int snapshot_kpsi_f64(void* dst) = 0;
   // Compile-time branches of the reference selected at run time.
   virtual int set_variant(const vk_variant* v) = 0;
+  virtual int get_chempot(double* omega) = 0;
   virtual bool kpsi_is_masked() const = 0;
   virtual void mark_rk4_done() = 0;
 };

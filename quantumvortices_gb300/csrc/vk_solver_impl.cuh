@@ -213,8 +213,12 @@ class Solver : public SolverBase {
     return VK_OK;
   }
   int set_variant(const vk_variant* v) override {
-    if (v->flags & ~(VK_VAR_FRCDISP | VK_VAR_ADVECTION | VK_VAR_COUNTERFLOW)) {
-      set_error("vk_set_variant: only VK_VAR_FRCDISP, VK_VAR_ADVECTION and VK_VAR_COUNTERFLOW are built");
+    if (v->flags & ~(VK_VAR_FRCDISP | VK_VAR_ADVECTION | VK_VAR_COUNTERFLOW | VK_VAR_SGLE | VK_VAR_SELFTRUNC)) {
+      set_error("vk_set_variant: unknown flag");
+      return VK_E_INVALID;
+    }
+    if ((v->flags & VK_VAR_SELFTRUNC) && !(v->flags & VK_VAR_SGLE)) {
+      set_error("vk_set_variant: VK_VAR_SELFTRUNC acts inside the SGLE branch only");
       return VK_E_INVALID;
     }
     const int flow = (v->flags & VK_VAR_ADVECTION) ? 1 : ((v->flags & VK_VAR_COUNTERFLOW) ? 2 : 0);
@@ -226,7 +230,8 @@ class Solver : public SolverBase {
       set_error("vk_set_variant: the ARGLE flow terms need no particles and nx <= 2048 in FP64");
       return VK_E_INVALID;
     }
-    const double vals[] = {v->vishypo_gp, v->vishype_gp, v->famp_gp, v->kf1_gp, v->kf2_gp, v->vnx, v->vny};
+    const double vals[] = {v->vishypo_gp, v->vishype_gp, v->famp_gp, v->kf1_gp, v->kf2_gp, v->vnx, v->vny,
+                           v->oneybeta, v->nuN, v->chempot0, v->ktrunc};
     for (double x : vals)
       if (!std::isfinite(x)) {
         set_error("vk_set_variant: non-finite parameter");
@@ -243,12 +248,35 @@ class Solver : public SolverBase {
     vnx_ = v->vnx;
     vny_ = v->vny;
     if (flow_ && !Tg_) VK_CUDA_TRY(cudaMalloc(&Tg_, n2_ * sizeof(C)));
+    // SGLE (src/driver.f90:368-376): omega_chem = chempot0, noisesigma =
+    // sqrt(oneybeta/(2 alpha)), applied with 1/sqrt(dvol) (src/gpe.f90:163)
+    sgle_ = (v->flags & VK_VAR_SGLE) ? 1 : 0;
+    const double two_pi = 6.283185307179586476925286766559;
+    const double dvol = (two_pi / nx_) * (two_pi / ny_);
+    c_.sgle_amp = (1.0 / std::sqrt(dvol)) * std::sqrt((1.0 / (2.0 * c_.alpha)) * v->oneybeta);
+    c_.sqrt_dt = std::sqrt(c_.dt);
+    c_.selftrunc = (v->flags & VK_VAR_SELFTRUNC) ? 1 : 0;
+    c_.ktrunc2 = v->ktrunc * v->ktrunc;
+    nun_area_ = v->nuN / (two_pi * two_pi);
+    if (sgle_) {
+      if (!Tn_) VK_CUDA_TRY(cudaMalloc(&Tn_, n2_ * sizeof(C)));
+      if (!omega_dev_) VK_CUDA_TRY(cudaMalloc(&omega_dev_, sizeof(double) * (1 + kNormBlocks)));
+      c_.omega = v->chempot0;
+      VK_CUDA_TRY(cudaMemcpy(omega_dev_, &c_.omega, sizeof(double), cudaMemcpyHostToDevice));
+    } else {
+      c_.omega = p_.omega_chem;
+    }
+    c_.omega_dev = omega_dev_;
     // the captured step graphs bake the constants in: capture again
     if (g_rk4_) cudaGraphExecDestroy(g_rk4_);
     if (g_argle_) cudaGraphExecDestroy(g_argle_);
     g_rk4_ = g_argle_ = nullptr;
     VK_CUDA_TRY(cudaMemsetAsync(rngc_, 0, sizeof(unsigned long long), st_));
     return sync_check();
+  }
+  int get_chempot(double* omega) override {
+    *omega = c_.omega;
+    return VK_OK;
   }
   int snapshot_kpsi_f64(void* dst) override {
     launch_simple("k_to_f64", k_to_f64<T>, (const C*)kpsi_, (double2*)dst, n2_);
@@ -412,6 +440,17 @@ class Solver : public SolverBase {
   // One ARGLE step (src/gpe.f90:5-224) with the new residual sums when resid.
   void argle_step(bool resid, int nblk) {
     x1(1, false);
+    if (sgle_) {  // finiteT_adhoc_chempot on the psi of this step (src/gpe.f90:189), then the noise
+      launch_raw("k_sum_abs2", k_sum_abs2<T>, kNormBlocks, 256, 0, (const C*)psi_, n2_, omega_dev_ + 1);
+      const double two_pi = 6.283185307179586476925286766559;
+      launch_raw("k_chempot", k_chempot, 1, 32, 0, (const double*)(omega_dev_ + 1), kNormBlocks, omega_dev_,
+                 c_.dt, nun_area_, (two_pi / nx_) * (two_pi / ny_), two_pi * two_pi);
+      with_len(nx_, [&](auto lc) {
+        constexpr int L = decltype(lc)::value;
+        typedef GeoX<T, L> G;
+        launch_raw("k_noise_x", k_noise_x<T, L>, ny_ / G::R, G::NT, sizeof(C) * G::R * G::LP, Tn_, (const C*)twx_, c_);
+      });
+    }
     if (np_ > 0) {
       y1_pot(false, nullptr);
       x2_pot(-1);
@@ -423,6 +462,7 @@ class Solver : public SolverBase {
       x2(-1, false);
     }
     y2_argle(resid);
+    if (sgle_) launch_raw("k_rng_bump", k_rng_bump<T>, 1, 1, 0, rngc_);
     if (resid) launch_raw("k_reduce_partials3", k_reduce_partials3, 1, 256, 0, (const double*)part_, nblk, sums_);
     if (p_.argle_renorm) {
       // norm = dvol * (1/(nx ny)) * sum |kpsi|^2; target Nparticle = Lx*Ly
@@ -457,6 +497,14 @@ class Solver : public SolverBase {
     kpsi_masked_ = false;
     int rc = check_launch();
     if (rc) return rc;
+    if (sgle_) {
+      // the host copy feeds the diagnostics (echem) and any later RK4 steps,
+      // whose captured graph holds the old value
+      VK_CUDA_TRY(cudaMemcpyAsync(&c_.omega, omega_dev_, sizeof(double), cudaMemcpyDeviceToHost, st_));
+      VK_CUDA_TRY(cudaStreamSynchronize(st_));
+      if (g_rk4_) cudaGraphExecDestroy(g_rk4_);
+      g_rk4_ = nullptr;
+    }
     if (residual) {
       double h[3];
       VK_CUDA_TRY(cudaMemcpyAsync(h, sums_, sizeof(h), cudaMemcpyDeviceToHost, st_));
@@ -744,11 +792,21 @@ class Solver : public SolverBase {
       constexpr int L = decltype(lc)::value;
       typedef GeoY<T, L> G;
       const size_t sm = sizeof(C) * G::R * G::LP;
-      if (flow_) {
-        if (resid) launch_raw("k_y2_argle", k_y2_argle<T, L, true, true>, nx_ / G::R, G::NT, 2 * sm, (const C*)Td_, kpsi_, Ta_, (const C*)twy_, part_, c_, Tg_);
-        else launch_raw("k_y2_argle", k_y2_argle<T, L, false, true>, nx_ / G::R, G::NT, 2 * sm, (const C*)Td_, kpsi_, Ta_, (const C*)twy_, part_, c_, Tg_);
-      } else if (resid) launch_raw("k_y2_argle", k_y2_argle<T, L, true>, nx_ / G::R, G::NT, sm, (const C*)Td_, kpsi_, Ta_, (const C*)twy_, part_, c_, (C*)nullptr);
-      else launch_raw("k_y2_argle", k_y2_argle<T, L, false>, nx_ / G::R, G::NT, sm, (const C*)Td_, kpsi_, Ta_, (const C*)twy_, part_, c_, (C*)nullptr);
+      if (sgle_) {
+        auto go = [&](auto rc_, auto dc_) {
+          constexpr bool RS = decltype(rc_)::value, DV = decltype(dc_)::value;
+          launch_raw("k_y2_argle", k_y2_argle<T, L, RS, DV, true>, nx_ / G::R, G::NT, 2 * sm, (const C*)Td_, kpsi_, Ta_,
+                     (const C*)twy_, part_, c_, Tg_, (const C*)Tn_);
+        };
+        if (resid && flow_) go(std::true_type(), std::true_type());
+        else if (resid) go(std::true_type(), std::false_type());
+        else if (flow_) go(std::false_type(), std::true_type());
+        else go(std::false_type(), std::false_type());
+      } else if (flow_) {
+        if (resid) launch_raw("k_y2_argle", k_y2_argle<T, L, true, true>, nx_ / G::R, G::NT, 2 * sm, (const C*)Td_, kpsi_, Ta_, (const C*)twy_, part_, c_, Tg_, (const C*)nullptr);
+        else launch_raw("k_y2_argle", k_y2_argle<T, L, false, true>, nx_ / G::R, G::NT, 2 * sm, (const C*)Td_, kpsi_, Ta_, (const C*)twy_, part_, c_, Tg_, (const C*)nullptr);
+      } else if (resid) launch_raw("k_y2_argle", k_y2_argle<T, L, true>, nx_ / G::R, G::NT, sm, (const C*)Td_, kpsi_, Ta_, (const C*)twy_, part_, c_, (C*)nullptr, (const C*)nullptr);
+      else launch_raw("k_y2_argle", k_y2_argle<T, L, false>, nx_ / G::R, G::NT, sm, (const C*)Td_, kpsi_, Ta_, (const C*)twy_, part_, c_, (C*)nullptr, (const C*)nullptr);
     });
   }
 
@@ -827,6 +885,10 @@ class Solver : public SolverBase {
     rngc_ = nullptr;
     if (Tg_) cudaFree(Tg_);
     Tg_ = nullptr;
+    if (Tn_) cudaFree(Tn_);
+    Tn_ = nullptr;
+    if (omega_dev_) cudaFree(omega_dev_);
+    omega_dev_ = nullptr;
     if (st_) cudaStreamDestroy(st_);
     psi_ = kpsi_ = str1_ = str2_ = Ta_ = Td_ = Tb_ = Tc_ = twx_ = twy_ = nullptr;
     st_ = nullptr;
@@ -859,6 +921,11 @@ class Solver : public SolverBase {
   cudaGraphExec_t g_rk4_ = nullptr, g_argle_ = nullptr;
   unsigned long long* rngc_ = nullptr;  // forcing-phase counter (RHS evaluations)
   int flow_ = 0;                          // ARGLE flow terms: 1 advection, 2 counterflow
+  int sgle_ = 0;                          // -DGPE_SGLE noise + chemical potential ODE
+  double nun_area_ = 0.0;                 // nuN / (Lx Ly)
+  static constexpr int kNormBlocks = 152 * 4;
+  double* omega_dev_ = nullptr;           // [0] omega_chem, [1..] norm partial sums
+  C* Tn_ = nullptr;                       // x-spectrum of the SGLE noise
   double vnx_ = 0.0, vny_ = 0.0;
   C* Tg_ = nullptr;                       // F^-1_y[i ky kpsi] for the flow terms
   int64_t g_rk4_n_ = 0, g_argle_n_ = 0;

@@ -65,6 +65,8 @@ class VkNamelist(C.Structure):
 VK_VAR_FRCDISP = 1
 VK_VAR_ADVECTION = 2
 VK_VAR_COUNTERFLOW = 4
+VK_VAR_SGLE = 8
+VK_VAR_SELFTRUNC = 16
 
 
 class VkVariant(C.Structure):
@@ -74,6 +76,7 @@ class VkVariant(C.Structure):
         ("vishypo_gp", C.c_double), ("vishype_gp", C.c_double),
         ("famp_gp", C.c_double), ("kf1_gp", C.c_double), ("kf2_gp", C.c_double),
         ("vnx", C.c_double), ("vny", C.c_double),
+        ("oneybeta", C.c_double), ("nuN", C.c_double), ("chempot0", C.c_double), ("ktrunc", C.c_double),
         ("seed", C.c_uint64), ("reserved", C.c_int32 * 8),
     ]
 
@@ -129,6 +132,7 @@ def load_library(path: str | None = None) -> C.CDLL:
         "vk_ens_get_stream": (C.c_int, [vp, C.POINTER(vp)]),
         "vk_ens_kernel_launches": (C.c_int, [vp, C.POINTER(C.c_int64)]),
         "vk_set_variant": (C.c_int, [vp, C.POINTER(VkVariant)]),
+        "vk_get_chempot": (C.c_int, [vp, dp]),
         "vk_sts_begin": (C.c_int, [vp, C.c_int32]),
         "vk_sts_record": (C.c_int, [vp]),
         "vk_sts_count": (C.c_int, [vp, C.POINTER(C.c_int32)]),
@@ -363,18 +367,30 @@ class GPESolver:
 
     def set_variant(self, frcdisp: bool = False, vishypo: float = 0.0, vishype: float = 0.0, famp: float = 0.0,
                     kf1: float = 0.0, kf2: float = 0.0, seed: int = 1, flow: str | None = None,
-                    vnx: float = 0.0, vny: float = 0.0) -> None:
+                    vnx: float = 0.0, vny: float = 0.0, sgle: bool = False, oneybeta: float = 0.0,
+                    nuN: float = 0.0, chempot0: float = 0.0, selftrunc: bool = False, ktrunc: float = 0.0) -> None:
         """-DGPE_FRCDISP: hypo/hyperviscosity and random-phase shell forcing in
         every RK4 right-hand side (src/gpe.f90:623-658); kf in units of kdx.
         flow = "advection" / "counterflow": the ARGLE flow terms
-        (src/gpe.f90:78-146), counterflow velocity (vnx, vny)."""
+        (src/gpe.f90:78-146), counterflow velocity (vnx, vny).  sgle: the
+        finite-temperature ARGLE (noise + chemical potential ODE from chempot0,
+        src/gpe.f90:149-274), selftrunc: zero k^2 > ktrunc^2."""
         v = VkVariant()
         v.flags = (VK_VAR_FRCDISP if frcdisp else 0) | {None: 0, "advection": VK_VAR_ADVECTION,
                                                         "counterflow": VK_VAR_COUNTERFLOW}[flow]
+        v.flags |= (VK_VAR_SGLE if sgle else 0) | (VK_VAR_SELFTRUNC if selftrunc else 0)
+        v.oneybeta, v.nuN, v.chempot0, v.ktrunc = oneybeta, nuN, chempot0, ktrunc
         v.vishypo_gp, v.vishype_gp, v.famp_gp, v.kf1_gp, v.kf2_gp = vishypo, vishype, famp, kf1, kf2
         v.vnx, v.vny = vnx, vny
         v.seed = seed
         _check(self.lib.vk_set_variant(self._h, C.byref(v)), "vk_set_variant")
+
+    @property
+    def chempot(self) -> float:
+        """Current omega_chem (evolves under the SGLE variant)."""
+        x = C.c_double()
+        _check(self.lib.vk_get_chempot(self._h, C.byref(x)), "vk_get_chempot")
+        return float(x.value)
 
     # spatio-temporal spectra (sts_gpe + the Run/CompSTS post-processor)
     def sts_begin(self, nt: int) -> None:

@@ -110,3 +110,46 @@ def test_flow_rejections():
         v.flags = vk.VK_VAR_ADVECTION | vk.VK_VAR_COUNTERFLOW
         with pytest.raises(vk.VkError, match="VK_E_INVALID"):
             vk._check(s.lib.vk_set_variant(s._h, vk.C.byref(v)), "vk_set_variant")
+
+
+SGLE = dict(oneybeta=0.05, nuN=2.0, seed=13)
+
+
+def _sgle_pair(n, prec=vk.VK_PREC_FP64, flow=None, selftrunc=False):
+    p = vk.params_for(n, dt=1e-3, precision=prec)
+    kw = dict(SGLE, chempot0=p.gstrength * 0.9)
+    psi0, _ = vk.ic_vortices(n, n, 8, seed=8)
+    o = Oracle.from_vk_params(vk.params_for(n, dt=1e-3))
+    o.set_psi(psi0)
+    o.set_sgle(True, selftrunc=selftrunc, ktrunc=n / 4, **kw)
+    if flow:
+        o.set_argle_flow(2, 0.2, 0.1)
+    s = vk.GPESolver(p)
+    s.set_psi(psi0)
+    s.set_variant(sgle=True, selftrunc=selftrunc, ktrunc=n / 4,
+                  flow="counterflow" if flow else None, vnx=0.2, vny=0.1, **kw)
+    return s, o
+
+
+@pytest.mark.parametrize("n", [64, 128])
+@pytest.mark.parametrize("flow,trunc", [(None, False), (None, True), ("counterflow", False)])
+def test_sgle_matches_oracle(n, flow, trunc):
+    s, o = _sgle_pair(n, flow=flow, selftrunc=trunc)
+    s.argle(10)
+    s.argle(20)                           # split calls: noise counter and omega carry over
+    o.argle(30)
+    assert rel(s.get_kpsi(), o.get_kpsi()) < 1e-12
+    assert abs(s.chempot - o.chempot) <= 1e-12 * abs(o.chempot)
+    d = s.diagnostics_gpe()
+    sc, _ = o.diagnostics()
+    assert abs(d.echem - sc[3]) <= 1e-11 * abs(sc[3])
+    s.close()
+
+
+def test_sgle_fp32():
+    s, o = _sgle_pair(128, prec=vk.VK_PREC_FP32)
+    s.argle(30)
+    o.argle(30)
+    assert rel(s.get_kpsi(), o.get_kpsi()) < 1e-5
+    assert abs(s.chempot - o.chempot) <= 1e-6 * abs(o.chempot)
+    s.close()

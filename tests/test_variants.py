@@ -117,3 +117,49 @@ def test_advection_velocity_field_is_taylor_green():
     denom = 1 + p.alpha * (k[:, None] ** 2 + k[None, :] ** 2) * dt
     want = (k0 + dt * (nhat + p.omega_chem * k0)) / denom
     assert np.abs(o.get_kpsi() - want).max() <= 1e-12 * np.abs(want).max()
+
+
+def test_sgle_chemical_potential_ode_on_a_uniform_state():
+    """No noise (oneybeta = 0), psi = a: norm = a^2 Lx Ly, so one step sets
+    omega = chempot0 - dt nuN (a^2 - 1) (src/gpe.f90:264) and the k = 0 mode
+    follows a' = a + dt (-g a^3 + omega a) (src/gpe.f90:211)."""
+    n, dt, a, nun, mu0 = 32, 1e-3, 1.3, 5.0, 0.8
+    p = vk.params_for(n, dt=dt)
+    o = Oracle.from_vk_params(p)
+    o.set_psi(np.full((n, n), a, dtype=complex), otoc=False)
+    o.set_sgle(True, oneybeta=0.0, nuN=nun, chempot0=mu0)
+    o.argle(1)
+    om = mu0 - dt * nun * (a * a - 1.0)
+    assert abs(o.chempot - om) <= 1e-13 * abs(om)
+    want = a + dt * (-p.gstrength * a ** 3 + om * a)
+    assert abs(o.get_kpsi()[0, 0] / (n * n) - want) <= 1e-13 * abs(want)
+
+
+def test_sgle_noise_statistics_and_truncation():
+    """psi = 0, g = 0, nuN = 0: one step leaves kpsi = sqrt(dt) F[noise]
+    (2/3 mask) / (1 + alpha k^2 dt); E|F[noise]|^2 = 2 amp^2 nx ny with
+    amp = sqrt(oneybeta/(2 alpha))/sqrt(dvol).  With self-truncation every
+    k^2 > ktrunc^2 is zero."""
+    n, dt, beta = 64, 1e-3, 0.5
+    p = vk.params_for(n, dt=dt)
+    p.gstrength = 0.0
+    o = Oracle.from_vk_params(p)
+    o.set_psi(np.zeros((n, n), dtype=complex), otoc=False)
+    o.set_sgle(True, oneybeta=beta, nuN=0.0, chempot0=0.0, seed=5)
+    o.argle(1)
+    k = np.array([i if i < n // 2 else i - n for i in range(n)])
+    ksq = k[:, None] ** 2 + k[None, :] ** 2
+    kept = ksq < (n / 3.0) ** 2
+    den = 1 + p.alpha * ksq * dt
+    fz = o.get_kpsi() * den / math.sqrt(dt)
+    assert np.all(fz[~kept] == 0)
+    dvol = (2 * math.pi / n) ** 2
+    amp2 = beta / (2 * p.alpha) / dvol
+    ratio = np.mean(np.abs(fz[kept]) ** 2) / (2 * amp2 * n * n)
+    assert abs(ratio - 1.0) < 0.05, ratio
+    o2 = Oracle.from_vk_params(p)
+    o2.set_psi(np.zeros((n, n), dtype=complex), otoc=False)
+    o2.set_sgle(True, oneybeta=beta, chempot0=0.0, selftrunc=True, ktrunc=6.0, seed=5)
+    o2.argle(1)
+    kp = o2.get_kpsi()
+    assert np.all(kp[ksq > 36] == 0) and np.all(kp[ksq <= 36] != 0)
