@@ -102,6 +102,13 @@ typedef struct vk_namelist {
   int32_t maxiter, fsteps, ssteps, gsteps;  /* &tparam */
   int32_t nrst, sprst;                      /* &ckprst */
   int32_t strst, ststeps;                   /* &ckprst strst, &tparam ststeps (-DGPSTS) */
+  /* branches selected by vk_set_variant (src/driver.f90:59-68) */
+  double famp_gp, kf1_gp, kf2_gp;           /* &gpforceparam   */
+  double vishypo_gp, vishype_gp;            /* &gphypvis       */
+  double vnx, vny;                          /* &gpcounterflow  */
+  double oneybeta, nun, chempot0;           /* &gpfiniteT      */
+  double ktrunc;                            /* &selftruncation */
+  int32_t nsplit_orignal, nsplit_current;   /* &fileparam (split restart files) */
 } vk_namelist;
 
 /* Replaces: the namelist reads + MPI_BCAST block (src/driver.f90:147-334).
@@ -244,6 +251,9 @@ int vk_fft2d_forward_noalloc(const double* psi_dev, double* kpsi_dev, int32_t nx
  * so parity with it is statistical).  VK_VAR_SELFTRUNC then zeroes
  * k^2 > ktrunc^2.  Unbuilt flags return VK_E_INVALID. */
 int vk_set_variant(void* ctx, const vk_variant* v);
+/* vk_variant from the raw namelist values for the VK_VAR_* flags: kf1, kf2
+ * times kdx (src/driver.f90:384-387), the rest as read. */
+int vk_variant_derive(const vk_namelist* nl, int32_t flags, uint64_t seed, vk_variant* out);
 /* Current chemical potential omega_chem (changes under VK_VAR_SGLE;
  * write_chempot_for_restart, src/gpe.f90:266-300, writes it). */
 int vk_get_chempot(void* ctx, double* omega);
@@ -284,6 +294,13 @@ int vk_write_wf(const char* path, int32_t iopoint, double time, double dt,
 /* Reads the same layout (restart_from_argle_data, src/initial_config.f90:727-741). */
 int vk_read_wf(const char* path, int32_t nx, int32_t ny, int32_t* iopoint,
                double* time, double* dt, double* psi_phys);
+
+/* Regrouping of a field written as nsplit files (src/io_fields.f90:121-146,
+ * -DIOEVERYPROC, nsplit_orignal > nsplit_current = 1): reads
+ * <prefix>p1.dat .. <prefix>p<nsplit>.dat, each a header and ny/nsplit rows,
+ * into psi_phys[ny*nx] in file order.  prefix e.g. "restart/wf/wf0". */
+int vk_read_wf_split(const char* prefix, int32_t nsplit, int32_t nx, int32_t ny, int32_t* iopoint,
+                     double* time, double* dt, double* psi_phys);
 
 /* New (no reference counterpart): seeded N-vortex initial state.
  * Positions from SplitMix64(seed), uniform on [0,2pi)^2 with periodic

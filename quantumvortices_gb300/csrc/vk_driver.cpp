@@ -21,7 +21,14 @@
 // Text files use Fortran's E15.6 edit descriptor.  Output points between
 // which no file is written are stepped with one vk_gpe_rk4 call.
 //
+// --frcdisp / --advection / --counterflow / --sgle / --selftrunc select the
+// reference's compile-time branches (-DGPE_FRCDISP etc.) with their namelist
+// parameters; with --argle --sgle, data/cpot_sgle.dat_nrst0 every fsteps.
+// With &fileparam nsplit_orignal > 1 the restart field is regrouped from
+// restart/wf/wf<nrst>p1..p<nsplit>.dat.
+//
 // Usage: vikshobha_gb300 [--argle] [--fp32] [--no-otoc] [--steps N] [--sts NT]
+//                        [--frcdisp] [--advection] [--counterflow] [--sgle] [--selftrunc]
 #include <chrono>
 #include <cmath>
 #include <cstdio>
@@ -131,14 +138,23 @@ int main(int argc, char** argv) {
   bool argle = false, fp32 = false, otoc = true;
   long steps_override = -1;
   int sts_nt = 0;  // -DGPSTS path: records per spatio-temporal spectrum (0 = off)
+  int vflags = 0;  // -DGPE_FRCDISP / ADVECTION / COUNTERFLOW / SGLE / SELFTRUNC
   for (int i = 1; i < argc; ++i) {
     if (!std::strcmp(argv[i], "--argle")) argle = true;
     else if (!std::strcmp(argv[i], "--fp32")) fp32 = true;
     else if (!std::strcmp(argv[i], "--no-otoc")) otoc = false;
     else if (!std::strcmp(argv[i], "--steps") && i + 1 < argc) steps_override = std::atol(argv[++i]);
     else if (!std::strcmp(argv[i], "--sts") && i + 1 < argc) sts_nt = std::atoi(argv[++i]);
+    else if (!std::strcmp(argv[i], "--frcdisp")) vflags |= VK_VAR_FRCDISP;
+    else if (!std::strcmp(argv[i], "--advection")) vflags |= VK_VAR_ADVECTION;
+    else if (!std::strcmp(argv[i], "--counterflow")) vflags |= VK_VAR_COUNTERFLOW;
+    else if (!std::strcmp(argv[i], "--sgle")) vflags |= VK_VAR_SGLE;
+    else if (!std::strcmp(argv[i], "--selftrunc")) vflags |= VK_VAR_SELFTRUNC;
     else {
-      std::fprintf(stderr, "usage: %s [--argle] [--fp32] [--no-otoc] [--steps N] [--sts NT]\n", argv[0]);
+      std::fprintf(stderr,
+                   "usage: %s [--argle] [--fp32] [--no-otoc] [--steps N] [--sts NT] [--frcdisp] [--advection] "
+                   "[--counterflow] [--sgle] [--selftrunc]\n",
+                   argv[0]);
       return 2;
     }
   }
@@ -163,8 +179,19 @@ int main(int argc, char** argv) {
   const std::string fr = "restart/wf/wf" + std::to_string(nl.nrst) + "p1.dat";
   int32_t icpoint;
   double tfile, dtfile;
-  check(vk_read_wf(fr.c_str(), nx, ny, &icpoint, &tfile, &dtfile, psi.data()), "reading the restart field");
+  if (nl.nsplit_orignal > 1) {  // regroup the ranks' files (src/io_fields.f90:121-146)
+    const std::string pre = "restart/wf/wf" + std::to_string(nl.nrst);
+    check(vk_read_wf_split(pre.c_str(), nl.nsplit_orignal, nx, ny, &icpoint, &tfile, &dtfile, psi.data()),
+          "reading the split restart field");
+  } else {
+    check(vk_read_wf(fr.c_str(), nx, ny, &icpoint, &tfile, &dtfile, psi.data()), "reading the restart field");
+  }
   check(vk_set_psi(ctx, psi.data()), "vk_set_psi");
+  if (vflags) {  // the compile-time branches of the reference, from the namelists
+    vk_variant var;
+    check(vk_variant_derive(&nl, vflags, 1, &var), "vk_variant_derive");
+    check(vk_set_variant(ctx, &var), "vk_set_variant");
+  }
   const std::string nrs = std::to_string(0);  // restart_from_argle_data sets nrst = 0
   if (np > 0) {
     std::vector<double> pos, vel, f0;
@@ -308,6 +335,11 @@ int main(int argc, char** argv) {
     if (itime % fsteps == 0) {
       ++fldpoint;
       io_fields(fldpoint, time);
+      if (argle && (vflags & VK_VAR_SGLE)) {  // write_chempot_for_restart (src/solve.f90:112-114)
+        double om = 0.0;
+        check(vk_get_chempot(ctx, &om), "vk_get_chempot");
+        append_line("data/cpot_sgle.dat_nrst" + nrs, {time, om});
+      }
     }
     if (itime % gsteps == 0) {
       if (itime % ssteps == 0) ++spcpoint;

@@ -186,6 +186,39 @@ extern "C" int vk_read_namelists(const char* parameter_txt, const char* paramete
   get(nl, "gpparticle", "ppotd", [&](double x) { out->ppotd = x; });
   get(nl, "gpparticle", "ppotv0", [&](double x) { out->ppotv0 = x; });
   get(nl, "gpparticle", "ppotthick", [&](double x) { out->ppotthick = x; });
+  get(nl, "gpforceparam", "famp_gp", [&](double x) { out->famp_gp = x; });
+  get(nl, "gpforceparam", "kf1_gp", [&](double x) { out->kf1_gp = x; });
+  get(nl, "gpforceparam", "kf2_gp", [&](double x) { out->kf2_gp = x; });
+  get(nl, "gphypvis", "vishypo_gp", [&](double x) { out->vishypo_gp = x; });
+  get(nl, "gphypvis", "vishype_gp", [&](double x) { out->vishype_gp = x; });
+  get(nl, "gpcounterflow", "vnx", [&](double x) { out->vnx = x; });
+  get(nl, "gpcounterflow", "vny", [&](double x) { out->vny = x; });
+  get(nl, "gpfinitet", "oneybeta", [&](double x) { out->oneybeta = x; });
+  get(nl, "gpfinitet", "nun", [&](double x) { out->nun = x; });
+  get(nl, "gpfinitet", "chempot0", [&](double x) { out->chempot0 = x; });
+  get(nl, "selftruncation", "ktrunc", [&](double x) { out->ktrunc = x; });
+  get(nl, "fileparam", "nsplit_orignal", [&](double x) { out->nsplit_orignal = (int32_t)x; });
+  get(nl, "fileparam", "nsplit_current", [&](double x) { out->nsplit_current = (int32_t)x; });
+  return VK_OK;
+}
+
+extern "C" int vk_variant_derive(const vk_namelist* nl, int32_t flags, uint64_t seed, vk_variant* out) {
+  if (!nl || !out) { set_error("vk_variant_derive: null argument"); return VK_E_INVALID; }
+  std::memset(out, 0, sizeof(*out));
+  const double kdx = 1.0;  // 2 pi / lengthx with lengthx = 2 pi (src/mod_grid.f90)
+  out->flags = flags;
+  out->famp_gp = nl->famp_gp;
+  out->kf1_gp = nl->kf1_gp * kdx;
+  out->kf2_gp = nl->kf2_gp * kdx;
+  out->vishypo_gp = nl->vishypo_gp;
+  out->vishype_gp = nl->vishype_gp;
+  out->vnx = nl->vnx;
+  out->vny = nl->vny;
+  out->oneybeta = nl->oneybeta;
+  out->nuN = nl->nun;
+  out->chempot0 = nl->chempot0;
+  out->ktrunc = nl->ktrunc;
+  out->seed = seed;
   return VK_OK;
 }
 
@@ -287,6 +320,25 @@ extern "C" int vk_read_wf(const char* path, int32_t nx, int32_t ny, int32_t* iop
   if (iopoint) *iopoint = io;
   if (time) *time = t;
   if (dt) *dt = d;
+  return VK_OK;
+}
+
+// Regrouping of a field written by nsplit ranks (src/io_fields.f90:121-146,
+// -DIOEVERYPROC with nsplit_orignal > nsplit_current = 1): files
+// <prefix>p1.dat .. <prefix>p<nsplit>.dat, each a header record and ny/nsplit
+// rows of nx complex128, concatenated along y in file order.
+extern "C" int vk_read_wf_split(const char* prefix, int32_t nsplit, int32_t nx, int32_t ny, int32_t* iopoint,
+                                double* time, double* dt, double* psi) {
+  if (!prefix || !psi || nsplit <= 0 || nx <= 0 || ny <= 0 || ny % nsplit != 0) {
+    set_error("vk_read_wf_split: bad argument (ny must be a multiple of nsplit)");
+    return VK_E_INVALID;
+  }
+  const int32_t rows = ny / nsplit;
+  for (int32_t j = 1; j <= nsplit; ++j) {
+    const std::string path = std::string(prefix) + "p" + std::to_string(j) + ".dat";
+    const int rc = vk_read_wf(path.c_str(), nx, rows, iopoint, time, dt, psi + (size_t)2 * nx * rows * (j - 1));
+    if (rc != VK_OK) return rc;
+  }
   return VK_OK;
 }
 

@@ -59,6 +59,10 @@ class VkNamelist(C.Structure):
         ("gp_mass_part", C.c_double), ("ppotd", C.c_double), ("ppotv0", C.c_double), ("ppotthick", C.c_double),
         ("maxiter", C.c_int32), ("fsteps", C.c_int32), ("ssteps", C.c_int32), ("gsteps", C.c_int32),
         ("nrst", C.c_int32), ("sprst", C.c_int32), ("strst", C.c_int32), ("ststeps", C.c_int32),
+        ("famp_gp", C.c_double), ("kf1_gp", C.c_double), ("kf2_gp", C.c_double),
+        ("vishypo_gp", C.c_double), ("vishype_gp", C.c_double), ("vnx", C.c_double), ("vny", C.c_double),
+        ("oneybeta", C.c_double), ("nun", C.c_double), ("chempot0", C.c_double), ("ktrunc", C.c_double),
+        ("nsplit_orignal", C.c_int32), ("nsplit_current", C.c_int32),
     ]
 
 
@@ -121,6 +125,8 @@ def load_library(path: str | None = None) -> C.CDLL:
         "vk_nshell": (C.c_int32, [C.c_int32]),
         "vk_write_wf": (C.c_int, [C.c_char_p, C.c_int32, C.c_double, C.c_double, C.c_int32, C.c_int32, dp]),
         "vk_read_wf": (C.c_int, [C.c_char_p, C.c_int32, C.c_int32, C.POINTER(C.c_int32), dp, dp, dp]),
+        "vk_read_wf_split": (C.c_int, [C.c_char_p, C.c_int32, C.c_int32, C.c_int32, C.POINTER(C.c_int32), dp, dp,
+                                       dp]),
         "vk_ic_vortices": (C.c_int, [C.c_int32, C.c_int32, C.c_int32, C.c_uint64, C.c_double, C.c_double, dp, dp]),
         "vk_set_psi_vortices": (C.c_int, [vp, C.c_int32, C.c_uint64, C.c_double, C.c_double, dp]),
         "vk_ens_init": (C.c_int, [C.POINTER(VkParams), C.c_int32, C.POINTER(vp)]),
@@ -133,6 +139,7 @@ def load_library(path: str | None = None) -> C.CDLL:
         "vk_ens_kernel_launches": (C.c_int, [vp, C.POINTER(C.c_int64)]),
         "vk_set_variant": (C.c_int, [vp, C.POINTER(VkVariant)]),
         "vk_get_chempot": (C.c_int, [vp, dp]),
+        "vk_variant_derive": (C.c_int, [C.POINTER(VkNamelist), C.c_int32, C.c_uint64, C.POINTER(VkVariant)]),
         "vk_sts_begin": (C.c_int, [vp, C.c_int32]),
         "vk_sts_record": (C.c_int, [vp]),
         "vk_sts_count": (C.c_int, [vp, C.POINTER(C.c_int32)]),
@@ -177,6 +184,14 @@ def derive_params(nl: VkNamelist, precision: int = VK_PREC_FP64, otoc: bool = Tr
     return p
 
 
+def derive_variant(nl: VkNamelist, flags: int, seed: int = 1) -> VkVariant:
+    """vk_variant from the namelists (&gpforceparam, &gphypvis, &gpcounterflow,
+    &gpfiniteT, &selftruncation) for the VK_VAR_* flags."""
+    v = VkVariant()
+    _check(load_library().vk_variant_derive(C.byref(nl), flags, seed, C.byref(v)), "vk_variant_derive")
+    return v
+
+
 def params_for(nx: int, ny: int | None = None, dt: float = 1e-3, precision: int = VK_PREC_FP64,
                otoc: bool = True, xi_in: float = math.sqrt(2.0), n_particles: int = 0, ppotd: float = 2.0,
                ppotv0: float = 10.0, gp_mass_part: float = 0.0, argle_renorm: bool = False) -> VkParams:
@@ -215,6 +230,16 @@ def read_wf(path: str, nx: int, ny: int):
     _check(load_library().vk_read_wf(path.encode(), nx, ny, C.byref(io), C.byref(t), C.byref(d),
                                       _dptr(a.view(np.float64))), "vk_read_wf")
     return a, int(io.value), float(t.value), float(d.value)
+
+
+def read_wf_split(prefix: str, nsplit: int, nx: int, ny: int):
+    """A field written as nsplit files <prefix>p<j>.dat (src/io_fields.f90:121-146);
+    returns (psi[ny, nx], iopoint, time, dt)."""
+    psi = np.empty((ny, nx), dtype=np.complex128)
+    io, t, d = C.c_int32(), C.c_double(), C.c_double()
+    _check(load_library().vk_read_wf_split(prefix.encode(), nsplit, nx, ny, C.byref(io), C.byref(t), C.byref(d),
+                                           _dptr(psi.view(np.float64))), "vk_read_wf_split")
+    return psi, int(io.value), float(t.value), float(d.value)
 
 
 def ic_vortices(nx: int, ny: int, n_vort: int, seed: int, xi0: float | None = None, min_sep: float = 0.0):
@@ -383,6 +408,10 @@ class GPESolver:
         v.vishypo_gp, v.vishype_gp, v.famp_gp, v.kf1_gp, v.kf2_gp = vishypo, vishype, famp, kf1, kf2
         v.vnx, v.vny = vnx, vny
         v.seed = seed
+        _check(self.lib.vk_set_variant(self._h, C.byref(v)), "vk_set_variant")
+
+    def apply_variant(self, v: VkVariant) -> None:
+        """vk_set_variant with a ready vk_variant (see derive_variant)."""
         _check(self.lib.vk_set_variant(self._h, C.byref(v)), "vk_set_variant")
 
     @property

@@ -119,3 +119,49 @@ def test_driver_sts_path(tmp_path):
     assert g1.shape == r1.shape and g2.shape == r2.shape
     assert np.abs(g1 - r1).max() <= 1e-12 * np.abs(r1).max()
     assert np.abs(g2 - r2).max() <= 1e-12 * np.abs(r2).max()
+
+
+def test_driver_sgle_argle_and_counterflow(tmp_path):
+    """--argle --sgle --counterflow: the branches come from &gpfiniteT and
+    &gpcounterflow; data/cpot_sgle.dat_nrst0 gets (time, omega_chem) every
+    fsteps, equal to the Python API's run of the same variant."""
+    n, dt = 64, 1e-3
+    psi0 = _write_inputs(tmp_path, n, dt, maxiter=30, fsteps=10, gsteps=10, ssteps=10)
+    with open(tmp_path / "parameter_gpe.txt", "a") as f:
+        f.write("&gpfiniteT\noneybeta = 0.05d0\nnuN = 2.0d0\nchempot0 = 7.5d0\n/\n"
+                "&gpcounterflow\nvnx = 0.2d0\nvny = 0.1d0\n/\n")
+    r = subprocess.run([_build.DRIVER, "--argle", "--sgle", "--counterflow"], cwd=tmp_path, capture_output=True,
+                       text=True, timeout=300)
+    assert r.returncode == 0, r.stderr
+    rows = [[float(v) for v in ln.split()] for ln in (tmp_path / "data/cpot_sgle.dat_nrst0").read_text().splitlines()]
+    assert len(rows) == 3
+    nl = vk.read_namelists(str(tmp_path / "parameter.txt"), str(tmp_path / "parameter_gpe.txt"))
+    p = vk.derive_params(nl)
+    with vk.GPESolver(p) as s:
+        s.set_psi(psi0)
+        s.apply_variant(vk.derive_variant(nl, vk.VK_VAR_SGLE | vk.VK_VAR_COUNTERFLOW, seed=1))
+        for t, om in rows:
+            s.argle(10)
+            assert abs(om - s.chempot) <= 1e-5 * abs(s.chempot)
+        field, *_ = vk.read_wf(str(tmp_path / "data/wf/wf3p1.dat"), n, n)
+        assert np.array_equal(field, s.get_psi())
+
+
+def test_driver_regroups_split_restart(tmp_path):
+    """&fileparam nsplit_orignal = 4: the restart field is read from
+    restart/wf/wf0p1..p4.dat; the run equals one from the joined field."""
+    n, dt = 64, 1e-3
+    psi0 = _write_inputs(tmp_path, n, dt, maxiter=10, fsteps=10, gsteps=10, ssteps=10)
+    (tmp_path / "restart/wf/wf0p1.dat").unlink()
+    for j in range(4):
+        vk.write_wf(str(tmp_path / f"restart/wf/wf0p{j + 1}.dat"), psi0[j * n // 4:(j + 1) * n // 4])
+    txt = (tmp_path / "parameter.txt").read_text().replace("&resolution", "&fileparam\nnsplit_orignal = 4\n"
+                                                           "nsplit_current = 1\n/\n&resolution")
+    (tmp_path / "parameter.txt").write_text(txt)
+    r = subprocess.run([_build.DRIVER], cwd=tmp_path, capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0, r.stderr
+    with vk.GPESolver(vk.params_for(n, dt=dt)) as s:
+        s.set_psi(psi0)
+        s.gpe_rk4(10)
+        field, *_ = vk.read_wf(str(tmp_path / "data/wf/wf1p1.dat"), n, n)
+        assert np.array_equal(field, s.get_psi())

@@ -64,7 +64,7 @@ def test_frcdisp_fp32_and_reset():
 def test_unbuilt_variant_flags_are_rejected():
     with vk.GPESolver(vk.params_for(32)) as s:
         v = vk.VkVariant()
-        v.flags = 8                     # not a built branch
+        v.flags = 64                    # not a branch
         with pytest.raises(vk.VkError, match="VK_E_INVALID"):
             vk._check(s.lib.vk_set_variant(s._h, vk.C.byref(v)), "vk_set_variant")
 

@@ -47,15 +47,23 @@ def test_params_mapping():
 def test_namelist_parsing(tmp_path):
     a = tmp_path / "parameter.txt"
     a.write_text("! Parameters\n&ckprst\nnrst = 0   ! restart\nsprst = 0\nstrst = 2\n/\n&resolution\nNx=256\n"
-                 "Ny=128\nNz=64\n/\n&tparam\ndt_fix=1.0d-3  ! step\nmaxiter=400000\nfsteps=1000\nssteps=1000\n"
+                 "Ny=128\nNz=64\n/\n&fileparam\nnsplit_orignal = 4\nnsplit_current = 1\n/\n&tparam\ndt_fix=1.0d-3  ! step\nmaxiter=400000\nfsteps=1000\nssteps=1000\n"
                  "gsteps=100\nststeps=20     ! kpsi 1d-line output frequency\n/\n")
     b = tmp_path / "parameter_gpe.txt"
     b.write_text("&gpparam\nxi=1.0d0 !\ncsound=1.0d0 !\nrho_avg=1.0d0 !\ndisp_factor=0.0d0 !\n/\n"
                  "&gpparticle\ngp_N_obj = 16 !\ngp_mass_part = 100.0d0 !\nppotd = 2.0d0\nppotV0 = 10.0d0 !\n/\n"
-                 "&gpotoc\nk_otoc_gp = 1.8d0 !\neps_otoc_gp = 1.0d0-4 !\n/\n")
+                 "&gpotoc\nk_otoc_gp = 1.8d0 !\neps_otoc_gp = 1.0d0-4 !\n/\n"
+                 "&gpforceparam\nfamp_gp = 0.5d0\nkf1_gp = 2.0d0\nkf2_gp = 4.0d0\n/\n"
+                 "&gphypvis\nnhypvis1_gp = 8\nvishype_gp = 1.0d-20\n/\n&gpcounterflow\nvnx = 0.25d0\nvny = -0.5d0\n/\n"
+                 "&gpfiniteT\noneybeta = 0.1d0\nnuN = 3.0d0\nchempot0 = 0.9d0\n/\n&selftruncation\nktrunc = 40.0d0\n/\n")
     nl = vk.read_namelists(str(a), str(b))
     assert (nl.nx, nl.ny, nl.maxiter, nl.fsteps, nl.gsteps) == (256, 128, 400000, 1000, 100)
     assert (nl.strst, nl.ststeps) == (2, 20)
+    assert (nl.famp_gp, nl.kf1_gp, nl.kf2_gp, nl.vishype_gp) == (0.5, 2.0, 4.0, 1e-20)
+    assert (nl.vnx, nl.vny, nl.oneybeta, nl.nun, nl.chempot0, nl.ktrunc) == (0.25, -0.5, 0.1, 3.0, 0.9, 40.0)
+    assert (nl.nsplit_orignal, nl.nsplit_current) == (4, 1)
+    v = vk.derive_variant(nl, vk.VK_VAR_FRCDISP | vk.VK_VAR_SGLE, seed=7)
+    assert (v.flags, v.kf1_gp, v.kf2_gp, v.nuN, v.chempot0, v.seed) == (9, 2.0, 4.0, 3.0, 0.9, 7)
     assert nl.dt_fix == 1e-3 and nl.gp_n_obj == 16 and nl.ppotv0 == 10.0
     p = vk.derive_params(nl)
     dx = 2 * math.pi / 256
@@ -138,3 +146,20 @@ def test_ic_vortices_periodic_and_seeded():
     d = (d + np.pi) % (2 * np.pi) - np.pi
     dist = np.sqrt((d ** 2).sum(-1)) + np.eye(16) * 10
     assert dist.min() >= 0.5
+
+
+def test_split_restart_files_regroup(tmp_path):
+    """A field written by 4 ranks (y slabs, src/io_fields.f90 -DIOEVERYPROC)
+    reads back as one field; ny not a multiple of nsplit is rejected."""
+    nx, ny, ns = 16, 32, 4
+    rng = np.random.default_rng(3)
+    psi = rng.standard_normal((ny, nx)) + 1j * rng.standard_normal((ny, nx))
+    for j in range(ns):
+        vk.write_wf(str(tmp_path / f"wf7p{j + 1}.dat"), psi[j * ny // ns:(j + 1) * ny // ns], iopoint=7,
+                    time=0.5, dt=1e-3)
+    got, io, t, d = vk.read_wf_split(str(tmp_path / "wf7"), ns, nx, ny)
+    assert np.array_equal(got, psi) and io == 7 and t == 0.5 and d == 1e-3
+    with pytest.raises(vk.VkError):
+        vk.read_wf_split(str(tmp_path / "wf7"), 3, nx, ny)
+    with pytest.raises(vk.VkError):
+        vk.read_wf_split(str(tmp_path / "missing"), ns, nx, ny)
