@@ -279,11 +279,12 @@ __device__ __forceinline__ void fft_rows_warp(cplx<T>* s, const cplx<T>* __restr
 // number of points per thread (NR*L/NTA), capped at 16.  The caller must
 // __syncthreads() after filling s; on return s holds the natural-order
 // transform and the block is synchronised.  DIR = -1 forward, +1 inverse.
-// FP32 1024-point rows with at least a warp per row (and every thread of
-// the block active) take the warp-per-row transform instead.
+// FP32 1024-point rows with exactly one warp per row take the warp-per-row
+// transform instead (the x passes; measured on GB300, the y passes and the
+// paired half-height transforms are faster in the Stockham stages).
 template <typename T, int L, int NR, int NTA, int DIR, int NTB = NTA>
 __device__ __forceinline__ void fft_rows(cplx<T>* s, const cplx<T>* __restrict__ tw) {
-  if constexpr (sizeof(T) == 4 && L == 1024 && NTA == NTB && NTA >= 32 * NR) {
+  if constexpr (sizeof(T) == 4 && L == 1024 && NTA == NTB && NTA == 32 * NR) {
     fft_rows_warp<T, L, NR, DIR>(s, tw);
   } else {
     constexpr int E = NR * L / NTA;

@@ -45,9 +45,10 @@ inline void ensure_smem_attr(const void* fn, size_t dyn_bytes) {
 // Launch geometry.  x passes (rows y, GeoX) hold R >= 2 rows per CTA so two
 // real rows can share one complex FFT; y passes (rows kx, GeoY) hold R rows.
 // NT = R*L/16 threads: full-height transforms run radix-16 stages, the
-// half-height paired transforms radix-8 stages on the same threads.  FP32
-// at L = 1024 uses one warp per row (NT = 32 R) and the warp-per-row
-// transform of vk_fft.cuh (sizes chosen by a sweep on GB300).
+// half-height paired transforms radix-8 stages on the same threads.  The
+// FP32 x passes at L = 1024 use one warp per row (NT = 32 R) and the
+// warp-per-row transform of vk_fft.cuh; the choice of geometry and of the
+// transform per pass follows whole-step timings on GB300.
 // MINB is the CTAs per SM the register budget is sized for.
 template <typename T, int L> struct GeoX;
 template <typename T, int L> struct GeoY;
@@ -68,7 +69,7 @@ VK_GEO(GeoX, float, 128, 8, 4) VK_GEO(GeoX, float, 256, 4, 4) VK_GEO(GeoX, float
 VK_GEOE(GeoX, float, 1024, 4, 2, 32) VK_GEO(GeoX, float, 2048, 2, 2) VK_GEO(GeoX, float, 4096, 2, 1)
 VK_GEO(GeoY, float, 16, 16, 4) VK_GEO(GeoY, float, 32, 8, 8) VK_GEO(GeoY, float, 64, 4, 8)
 VK_GEO(GeoY, float, 128, 2, 8) VK_GEO(GeoY, float, 256, 1, 8) VK_GEO(GeoY, float, 512, 1, 8)
-VK_GEOE(GeoY, float, 1024, 2, 4, 32) VK_GEO(GeoY, float, 2048, 1, 4) VK_GEO(GeoY, float, 4096, 1, 2)
+VK_GEO(GeoY, float, 1024, 1, 8) VK_GEO(GeoY, float, 2048, 1, 4) VK_GEO(GeoY, float, 4096, 1, 2)
 #undef VK_GEO
 #undef VK_GEOE
 
