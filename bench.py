@@ -33,6 +33,9 @@ METRIC = "RK4 grid-pt-steps/s at 1024^2"
 UNIT = "grid-pt-steps/s"
 PEAKS_FILE = os.path.join(ROOT, "MEASURED_PEAKS.json")
 FALLBACK_HBM_GBS = 6800.0
+# k_x1<double,1024> DRAM bytes per launch from one ncu capture of this workload
+# (profiles/k_x1_fp64_1024_traffic.md: 11.36 MB read, 0 written within the launch)
+X1_FP64_1024_DRAM_BYTES = 11361536 + 0
 
 
 def parse():
@@ -47,6 +50,7 @@ def parse():
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--no-ensemble", action="store_true")
     ap.add_argument("--no-4096", action="store_true")
+    ap.add_argument("--no-argle", action="store_true")
     return ap.parse_args()
 
 
@@ -222,6 +226,30 @@ def ensemble_bench(torch, K, W, S):
             "errors_vs_fp64_after_100_steps": errs, "autotune": report}
 
 
+def argle_bench(torch, n, psi0):
+    """ARGLE relaxation at n^2 (configs[1]: 2000 steps at dt = 1e-3 from the
+    64-vortex state), FP64 and FP32: throughput and the residual
+    ||kpsi_new - kpsi_old|| / (dt ||kpsi_old||) after the 2000 steps."""
+    from quantumvortices_gb300 import vk
+    out = {"unit": UNIT, "steps": 2000}
+    for nm, prec in (("fp64", vk.VK_PREC_FP64), ("fp32", vk.VK_PREC_FP32)):
+        s = vk.GPESolver(vk.params_for(n, dt=1e-3, precision=prec))
+        s.set_psi(psi0)
+        s.argle(5)
+        s.set_psi(psi0)
+        ext = torch.cuda.ExternalStream(s.stream)
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(ext)
+        r = s.argle(2000)
+        e1.record(ext)
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1)
+        out[nm] = {"value": n * n * 2000 / (ms * 1e-3), "ms_per_step": ms / 2000, "residual": r}
+        s.close()
+    return out
+
+
 def grid4096_bench(torch, steps=5):
     """One 4096^2 field with 1024 seeded vortices: FP64 and FP32 throughput
     and the FP32-vs-FP64 psi error after 100 RK4 steps."""
@@ -363,6 +391,7 @@ def run_ours(args, rank, world, local_rank):
 
     ens = None if args.no_ensemble else ensemble_bench(torch, K, W, S)
     g4096 = None if args.no_4096 else grid4096_bench(torch)
+    argle = None if args.no_argle else argle_bench(torch, n, psi0)
     if rank != 0:
         return
     dgemm_tf = fp64_peak_tflops(torch)
@@ -388,7 +417,10 @@ def run_ours(args, rank, world, local_rank):
         "clocks": clocks, "gpu_launches": launches,
         "roofline": {"bound": "hbm", "kernel": tag, "achieved": achieved, "peak": peak,
                      "peak_source": peak_kind, "unit": "GB/s",
-                     "frac": achieved / peak if achieved else None, "traffic": None,
+                     "frac": achieved / peak if achieved else None,
+                     "traffic": X1_FP64_1024_DRAM_BYTES if (tag == "k_x1" and n == 1024) else None,
+                     "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum per launch, "
+                                       "profiles/k_x1_fp64_1024_traffic.md",
                      "algorithmic_bytes_per_launch": nbytes, "launch_ms": per_launch_ms,
                      "step_canonical_gbs": canonical, "step_canonical_frac": canonical / peak,
                      "binding": "fp64 pipe (the fields of a 1024^2 step stay in L2)",
@@ -403,6 +435,7 @@ def run_ours(args, rank, world, local_rank):
         "fp32": fp32,
         "ensemble": ens,
         "grid_4096": g4096,
+        "argle": argle,
     }
     out["cpu_baseline"] = cpu_baseline(n, psi0, args.cpu_seconds)
     print(json.dumps(out))
