@@ -43,7 +43,7 @@ __device__ __forceinline__ int wrapi(int v, int n) { return v < 0 ? v + n : (v >
 // vectors, 8 channels of one pixel); thread 0 issues the chunk's four
 // K = 16 MMAs and commits them to the stage's mbarrier, which frees the stage
 // for the copies S - 1 chunks ahead.  Every wait is bounded.
-constexpr int kConvStages = 3;
+constexpr int kConvStages = 2;
 
 template <int BN>
 __global__ void __launch_bounds__(128) k_conv(const bf16* __restrict__ in, int H, int W, int Cin,
@@ -683,7 +683,7 @@ class Net {
     const int npix = in.h * in.w, M = 9 * in.c;
     const int mt = (M + 127) / 128;
     int ppc = 8192;
-    while ((npix + ppc - 1) / ppc * mt < 4 * 152 && ppc > 512) ppc /= 2;
+    while ((npix + ppc - 1) / ppc * mt < 8 * 152 && ppc > 256) ppc /= 2;
     dim3 grid(mt, (npix + ppc - 1) / ppc);
     const size_t smem = 2 * (128 * 64 * 2 + (size_t)coutp * 64 * 2);
     cudaMemsetAsync(out, 0, sizeof(float) * (size_t)M * coutp, st);
