@@ -281,6 +281,16 @@ int vk_sts_spectra(void* ctx, double* sts1d, double* sts2d);
 /* Frees the ring. */
 int vk_sts_end(void* ctx);
 
+/* Asynchronous field dump (the io_fields writes of src/io_fields.f90:1-66
+ * without stalling the stepping).  vk_dump_begin snapshots psi (as FP64)
+ * in step order and starts its copy to pinned host memory on a second
+ * stream, then returns; later vk_gpe_rk4 / vk_argle calls proceed meanwhile.
+ * vk_dump_wait blocks until that copy is done and copies psi_phys[ny*nx]
+ * out; it touches only the dump's event and buffer, so another host thread
+ * may call it while this context steps.  One dump in flight at a time. */
+int vk_dump_begin(void* ctx);
+int vk_dump_wait(void* ctx, double* psi_phys);
+
 /* Thread-local message for the last failing call on this thread. */
 const char* vk_last_error(void);
 

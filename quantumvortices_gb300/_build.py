@@ -69,7 +69,7 @@ def build(verbose: bool = False, jobs: int | None = None) -> str:
         _run([nvcc, *ARCH, "-shared", "-o", LIB, *objs, "-Xcompiler", "-fopenmp", "-lgomp"])
     drv_src = os.path.join(CSRC, "vk_driver.cpp")
     if not os.path.exists(DRIVER) or os.path.getmtime(DRIVER) < max(os.path.getmtime(drv_src), os.path.getmtime(LIB)):
-        _run([cxx, "-O2", "-std=c++17", "-o", DRIVER, drv_src, "-L" + PKG, "-lvk", "-Wl,-rpath,$ORIGIN"])
+        _run([cxx, "-O2", "-std=c++17", "-pthread", "-o", DRIVER, drv_src, "-L" + PKG, "-lvk", "-Wl,-rpath,$ORIGIN"])
     if verbose:
         print("built", LIB)
     return LIB

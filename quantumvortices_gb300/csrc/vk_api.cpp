@@ -257,3 +257,17 @@ extern "C" int vk_get_chempot(void* ctx, double* omega) {
   }
   return c->s->get_chempot(omega);
 }
+
+extern "C" int vk_dump_begin(void* ctx) {
+  VK_CTX_OR_FAIL(ctx);
+  return c->s->dump_begin();
+}
+
+extern "C" int vk_dump_wait(void* ctx, double* psi_phys) {
+  VK_CTX_OR_FAIL(ctx);
+  if (!psi_phys) {
+    set_error("vk_dump_wait: null output");
+    return VK_E_INVALID;
+  }
+  return c->s->dump_wait(psi_phys);
+}

@@ -36,6 +36,7 @@
 #include <cstring>
 #include <string>
 #include <sys/stat.h>
+#include <thread>
 #include <vector>
 #include "../../include/vk.h"
 
@@ -247,14 +248,25 @@ int main(int argc, char** argv) {
     }
   };
 
+  // io_fields: the field goes out asynchronously (vk_dump_begin); a writer
+  // thread waits for the copy and writes the file while the GPU steps on.
+  std::thread writer;
+  std::vector<double> wbuf(2 * (size_t)nx * ny);
+  auto join_writer = [&]() {
+    if (writer.joinable()) writer.join();
+  };
   auto io_fields = [&](int n, double t) {
     const std::string f = "data/wf/wf" + std::to_string(n) + "p1.dat";
     if (file_exists(f)) {  // the reference opens with STATUS='NEW'
       std::fprintf(stderr, "%s exists; refusing to overwrite\n", f.c_str());
       std::exit(1);
     }
-    check(vk_get_psi(ctx, psi.data()), "vk_get_psi");
-    check(vk_write_wf(f.c_str(), n, t, p.dt, nx, ny, psi.data()), "writing the field");
+    join_writer();  // one dump in flight at a time
+    check(vk_dump_begin(ctx), "vk_dump_begin");
+    writer = std::thread([&, f, n, t]() {
+      check(vk_dump_wait(ctx, wbuf.data()), "vk_dump_wait");
+      check(vk_write_wf(f.c_str(), n, t, p.dt, nx, ny, wbuf.data()), "writing the field");
+    });
     if (np > 0) {
       check(vk_particles_get(ctx, ppos.data(), pvel.data(), pfrc.data()), "vk_particles_get");
       const char* names[3] = {"gppos", "gpvel", "gpf0ext"};
@@ -347,6 +359,7 @@ int main(int argc, char** argv) {
       if (argle) append_line("data/argle_residual.dat_nrst" + nrs, {time, residual});
       if (!std::isfinite(sc[6]) || sc[6] > 1e6 * (2 * M_PI) * (2 * M_PI)) {
         std::fprintf(stderr, "norm blew up at step %ld (norm = %g)\n", itime, sc[6]);
+        join_writer();
         return 3;
       }
     }
@@ -355,6 +368,7 @@ int main(int argc, char** argv) {
       sts(time);
     }
   }
+  join_writer();
   check(vk_finalize(ctx), "vk_finalize");
   const double secs = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
   FILE* f = std::fopen("run_info.dat", "w");

@@ -36,6 +36,10 @@ class SolverBase {
   // Compile-time branches of the reference selected at run time.
   virtual int set_variant(const vk_variant* v) = 0;
   virtual int get_chempot(double* omega) = 0;
+  // Asynchronous psi dump: snapshot on the device, copy to pinned host memory
+  // on a second stream; dump_wait blocks for it and copies it out.
+  virtual int dump_begin() = 0;
+  virtual int dump_wait(double* psi) = 0;
   virtual bool kpsi_is_masked() const = 0;
   virtual void mark_rk4_done() = 0;
 };

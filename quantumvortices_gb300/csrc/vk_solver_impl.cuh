@@ -274,6 +274,36 @@ class Solver : public SolverBase {
     VK_CUDA_TRY(cudaMemsetAsync(rngc_, 0, sizeof(unsigned long long), st_));
     return sync_check();
   }
+  int dump_begin() override {
+    if (!have_psi_) { set_error("vk_dump_begin: no psi set"); return VK_E_STATE; }
+    if (dump_pending_) { set_error("vk_dump_begin: the previous dump was not waited for"); return VK_E_STATE; }
+    if (!dump_dev_) {
+      VK_CUDA_TRY(cudaMalloc(&dump_dev_, n2_ * sizeof(double2)));
+      VK_CUDA_TRY(cudaMallocHost(&dump_host_, n2_ * sizeof(double2)));
+      VK_CUDA_TRY(cudaStreamCreateWithFlags(&dump_st_, cudaStreamNonBlocking));
+      VK_CUDA_TRY(cudaEventCreateWithFlags(&dump_snap_, cudaEventDisableTiming));
+      VK_CUDA_TRY(cudaEventCreateWithFlags(&dump_done_, cudaEventDisableTiming));
+    }
+    // device snapshot in step order on the solver stream (FP64 for the file)
+    if (std::is_same<T, double>::value)
+      VK_CUDA_TRY(cudaMemcpyAsync(dump_dev_, psi_, n2_ * sizeof(double2), cudaMemcpyDeviceToDevice, st_));
+    else
+      launch_simple("k_to_f64", k_to_f64<T>, (const C*)psi_, dump_dev_, n2_);
+    VK_CUDA_TRY(cudaEventRecord(dump_snap_, st_));
+    // the copy to the host runs on its own stream while later steps proceed
+    VK_CUDA_TRY(cudaStreamWaitEvent(dump_st_, dump_snap_, 0));
+    VK_CUDA_TRY(cudaMemcpyAsync(dump_host_, dump_dev_, n2_ * sizeof(double2), cudaMemcpyDeviceToHost, dump_st_));
+    VK_CUDA_TRY(cudaEventRecord(dump_done_, dump_st_));
+    dump_pending_ = true;
+    return check_launch();
+  }
+  int dump_wait(double* psi) override {
+    if (!dump_pending_) { set_error("vk_dump_wait: no dump in flight"); return VK_E_STATE; }
+    VK_CUDA_TRY(cudaEventSynchronize(dump_done_));
+    std::memcpy(psi, dump_host_, n2_ * sizeof(double2));
+    dump_pending_ = false;
+    return VK_OK;
+  }
   int get_chempot(double* omega) override {
     *omega = c_.omega;
     return VK_OK;
@@ -887,6 +917,16 @@ class Solver : public SolverBase {
     Tg_ = nullptr;
     if (Tn_) cudaFree(Tn_);
     Tn_ = nullptr;
+    if (dump_st_) cudaStreamSynchronize(dump_st_);
+    if (dump_dev_) cudaFree(dump_dev_);
+    if (dump_host_) cudaFreeHost(dump_host_);
+    if (dump_st_) cudaStreamDestroy(dump_st_);
+    if (dump_snap_) cudaEventDestroy(dump_snap_);
+    if (dump_done_) cudaEventDestroy(dump_done_);
+    dump_dev_ = nullptr;
+    dump_host_ = nullptr;
+    dump_st_ = nullptr;
+    dump_snap_ = dump_done_ = nullptr;
     if (omega_dev_) cudaFree(omega_dev_);
     omega_dev_ = nullptr;
     if (st_) cudaStreamDestroy(st_);
@@ -926,6 +966,11 @@ class Solver : public SolverBase {
   static constexpr int kNormBlocks = 152 * 4;
   double* omega_dev_ = nullptr;           // [0] omega_chem, [1..] norm partial sums
   C* Tn_ = nullptr;                       // x-spectrum of the SGLE noise
+  double2* dump_dev_ = nullptr;           // asynchronous dump: device snapshot (FP64)
+  double2* dump_host_ = nullptr;          //   pinned host copy
+  cudaStream_t dump_st_ = nullptr;
+  cudaEvent_t dump_snap_ = nullptr, dump_done_ = nullptr;
+  bool dump_pending_ = false;
   double vnx_ = 0.0, vny_ = 0.0;
   C* Tg_ = nullptr;                       // F^-1_y[i ky kpsi] for the flow terms
   int64_t g_rk4_n_ = 0, g_argle_n_ = 0;

@@ -139,6 +139,8 @@ def load_library(path: str | None = None) -> C.CDLL:
         "vk_ens_kernel_launches": (C.c_int, [vp, C.POINTER(C.c_int64)]),
         "vk_set_variant": (C.c_int, [vp, C.POINTER(VkVariant)]),
         "vk_get_chempot": (C.c_int, [vp, dp]),
+        "vk_dump_begin": (C.c_int, [vp]),
+        "vk_dump_wait": (C.c_int, [vp, dp]),
         "vk_variant_derive": (C.c_int, [C.POINTER(VkNamelist), C.c_int32, C.c_uint64, C.POINTER(VkVariant)]),
         "vk_sts_begin": (C.c_int, [vp, C.c_int32]),
         "vk_sts_record": (C.c_int, [vp]),
@@ -409,6 +411,16 @@ class GPESolver:
         v.vnx, v.vny = vnx, vny
         v.seed = seed
         _check(self.lib.vk_set_variant(self._h, C.byref(v)), "vk_set_variant")
+
+    def dump_begin(self) -> None:
+        """Start an asynchronous copy of the current psi (vk_dump_begin)."""
+        _check(self.lib.vk_dump_begin(self._h), "vk_dump_begin")
+
+    def dump_wait(self) -> np.ndarray:
+        """psi[ny, nx] of the last dump_begin (blocks until its copy is done)."""
+        a = np.empty((self.ny, self.nx), dtype=np.complex128)
+        _check(self.lib.vk_dump_wait(self._h, _dptr(a.view(np.float64))), "vk_dump_wait")
+        return a
 
     def apply_variant(self, v: VkVariant) -> None:
         """vk_set_variant with a ready vk_variant (see derive_variant)."""

@@ -203,3 +203,26 @@ def test_4096_fp32_vs_fp64_with_1024_vortices():
             out[prec] = s.get_psi()
     assert np.isfinite(out[vk.VK_PREC_FP64]).all()
     assert rel(out[vk.VK_PREC_FP32], out[vk.VK_PREC_FP64]) < 1e-5
+
+
+@pytest.mark.parametrize("prec", [vk.VK_PREC_FP64, vk.VK_PREC_FP32])
+def test_async_dump_is_the_field_at_the_dump_point(prec):
+    """vk_dump_begin snapshots psi in step order; steps issued afterwards do
+    not change what vk_dump_wait returns (bitwise equal to get_psi there)."""
+    n = 128
+    psi0, _ = vk.ic_vortices(n, n, 8, seed=3)
+    with vk.GPESolver(vk.params_for(n, dt=1e-3, precision=prec)) as s, \
+            vk.GPESolver(vk.params_for(n, dt=1e-3, precision=prec)) as r:
+        s.set_psi(psi0)
+        r.set_psi(psi0)
+        s.gpe_rk4(7)
+        r.gpe_rk4(7)
+        s.dump_begin()
+        s.gpe_rk4(30)                  # runs while the copy is in flight
+        got = s.dump_wait()
+        assert np.array_equal(got, r.get_psi())
+        with pytest.raises(vk.VkError, match="VK_E_STATE"):
+            s.dump_wait()              # nothing in flight
+        s.dump_begin()
+        r.gpe_rk4(30)
+        assert np.array_equal(s.dump_wait(), r.get_psi())
