@@ -73,15 +73,6 @@ VK_GEO(GeoY, float, 1024, 1, 8) VK_GEO(GeoY, float, 2048, 1, 4) VK_GEO(GeoY, flo
 #undef VK_GEO
 #undef VK_GEOE
 
-// Programmatic dependent launch: wait until the previous kernel of the
-// stream has completed and its writes are visible, then allow the next
-// kernel's CTAs onto free SM slots (they wait in turn at their own entry).
-// Both instructions are no-ops for a launch without the attribute.
-__device__ __forceinline__ void vk_pdl_entry() {
-  asm volatile("griddepcontrol.wait;" ::: "memory");
-  asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
-}
-
 __device__ __forceinline__ int kwn(int i, int n) { return i < n / 2 ? i : i - n; }
 
 // Row index of logical row l when only |kx| <= K rows are processed.
@@ -275,7 +266,6 @@ template <typename T, int L, bool PRUNE>
 __global__ void __launch_bounds__(GeoX<T, L>::NT, GeoX<T, L>::MINB) k_xinv(const cplx<T>* __restrict__ src, cplx<T>* __restrict__ dst,
                                                      const cplx<T>* __restrict__ tw, T scale, int K) {
   extern __shared__ __align__(16) unsigned char smraw[];
-  vk_pdl_entry();
   xinv_body<T, L, GeoX<T, L>, PRUNE>(src, dst, tw, scale, K, blockIdx.x, reinterpret_cast<cplx<T>*>(smraw));
 }
 
@@ -363,7 +353,6 @@ __global__ void __launch_bounds__(GeoX<T, L>::NT, GeoX<T, L>::MINB) k_x1(const c
                                                    cplx<T>* __restrict__ Tb, const cplx<T>* __restrict__ tw,
                                                    StepConsts c) {
   extern __shared__ __align__(16) unsigned char smraw[];
-  vk_pdl_entry();
   x1_body<T, L, GeoX<T, L>, FROM_T, PRUNE>(Ta, psi, Tb, tw, c, blockIdx.x, reinterpret_cast<cplx<T>*>(smraw));
 }
 
@@ -400,7 +389,6 @@ template <typename T, int L>
 __global__ void __launch_bounds__(GeoY<T, L>::NT, GeoY<T, L>::MINB) k_y1(const cplx<T>* __restrict__ Tb, cplx<T>* __restrict__ Tc,
                                                    const cplx<T>* __restrict__ tw, StepConsts c) {
   extern __shared__ __align__(16) unsigned char smraw[];
-  vk_pdl_entry();
   y1_body<T, L, GeoY<T, L>>(Tb, Tc, tw, c, blockIdx.x, reinterpret_cast<cplx<T>*>(smraw));
 }
 
@@ -483,7 +471,6 @@ __global__ void __launch_bounds__(GeoX<T, L>::NT, GeoX<T, L>::MINB) k_x2(const c
                                                    const T* __restrict__ vpot, cplx<T>* __restrict__ Td,
                                                    const cplx<T>* __restrict__ tw, StepConsts c) {
   extern __shared__ __align__(16) unsigned char smraw[];
-  vk_pdl_entry();
   x2_body<T, L, GeoX<T, L>, SIGN, PRUNE_OUT, POT>(Tc, psi, vpot, Td, tw, c, blockIdx.x, reinterpret_cast<cplx<T>*>(smraw));
 }
 
@@ -599,7 +586,6 @@ __global__ void __launch_bounds__(GeoY<T, L>::NT, GeoY<T, L>::MINB) k_y2_rk4(con
                                                        cplx<T>* __restrict__ Ta, const cplx<T>* __restrict__ tw,
                                                        StepConsts c) {
   extern __shared__ __align__(16) unsigned char smraw[];
-  vk_pdl_entry();
   y2_rk4_body<T, L, GeoY<T, L>, STAGE, FRC>(Td, kpsi, str1, str2, Ta, tw, c, blockIdx.x, reinterpret_cast<cplx<T>*>(smraw));
 }
 
@@ -701,7 +687,6 @@ __global__ void __launch_bounds__(GeoY<T, L>::NT, GeoY<T, L>::MINB) k_y2_argle(c
                                                          cplx<T>* __restrict__ Tg = nullptr,
                                                          const cplx<T>* __restrict__ Tn = nullptr) {
   extern __shared__ __align__(16) unsigned char smraw[];
-  vk_pdl_entry();
   y2_argle_body<T, L, GeoY<T, L>, RESID, DERIV, SGLE>(Td, kpsi, Ta, tw, part, c, blockIdx.x,
                                                       reinterpret_cast<cplx<T>*>(smraw), Tg, Tn);
 }

@@ -3,7 +3,6 @@
 #pragma once
 #include <cuda_runtime.h>
 #include <cmath>
-#include <cstdlib>
 #include <cstring>
 #include <mutex>
 #include <string>
@@ -633,35 +632,6 @@ class Solver : public SolverBase {
     }
     if (timing_) record_event(tag);
   }
-  // Launch of a pass kernel that starts with vk_pdl_entry(): with
-  // programmatic stream serialization its CTAs may be scheduled while the
-  // previous kernel drains (they wait for it on entry).
-  template <typename... KA, typename... A>
-  void launch_pdl(const char* tag, void (*kern)(KA...), int grid, int block, size_t smem, A... args) {
-    if (!pdl_) {
-      launch_raw(tag, kern, grid, block, smem, args...);
-      return;
-    }
-    ensure_smem_attr((const void*)kern, smem);
-    if (timing_ && ev_used_ == 0) record_event(nullptr);
-    cudaLaunchConfig_t cfg = {};
-    cfg.gridDim = dim3((unsigned)grid);
-    cfg.blockDim = dim3((unsigned)block);
-    cfg.dynamicSmemBytes = smem;
-    cfg.stream = st_;
-    cudaLaunchAttribute at[1];
-    at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
-    at[0].val.programmaticStreamSerializationAllowed = 1;
-    cfg.attrs = at;
-    cfg.numAttrs = 1;
-    const cudaError_t le = cudaLaunchKernelEx(&cfg, kern, ((KA)args)...);
-    ++launches_;
-    if (le != cudaSuccess && launch_err_ == cudaSuccess) {
-      launch_err_ = le;
-      launch_err_tag_ = tag;
-    }
-    if (timing_) record_event(tag);
-  }
   template <typename... KA, typename... A>
   void launch_simple(const char* tag, void (*kern)(KA...), A... args) {
     const int grid = (int)std::min<size_t>((n2_ + 255) / 256, 152 * 16);
@@ -752,10 +722,10 @@ class Solver : public SolverBase {
       constexpr int L = decltype(lc)::value;
       typedef GeoX<T, L> G;
       if (prune)
-        launch_pdl("k_xinv", k_xinv<T, L, true>, ny_ / G::R, G::NT, sizeof(C) * G::R * G::LP, (const C*)Ta_, phys,
+        launch_raw("k_xinv", k_xinv<T, L, true>, ny_ / G::R, G::NT, sizeof(C) * G::R * G::LP, (const C*)Ta_, phys,
                    (const C*)twx_, T(c_.scale), K_);
       else
-        launch_pdl("k_xinv", k_xinv<T, L, false>, ny_ / G::R, G::NT, sizeof(C) * G::R * G::LP, (const C*)Ta_, phys,
+        launch_raw("k_xinv", k_xinv<T, L, false>, ny_ / G::R, G::NT, sizeof(C) * G::R * G::LP, (const C*)Ta_, phys,
                    (const C*)twx_, T(c_.scale), K_);
     });
   }
@@ -793,10 +763,10 @@ class Solver : public SolverBase {
       constexpr int L = decltype(lc)::value;
       typedef GeoX<T, L> G;
       if (prune)
-        launch_pdl("k_xinv", k_xinv<T, L, true>, ny_ / G::R, G::NT, sizeof(C) * G::R * G::LP, (const C*)Ta_, psi_,
+        launch_raw("k_xinv", k_xinv<T, L, true>, ny_ / G::R, G::NT, sizeof(C) * G::R * G::LP, (const C*)Ta_, psi_,
                    (const C*)twx_, T(c_.scale), K_);
       else
-        launch_pdl("k_xinv", k_xinv<T, L, false>, ny_ / G::R, G::NT, sizeof(C) * G::R * G::LP, (const C*)Ta_, psi_,
+        launch_raw("k_xinv", k_xinv<T, L, false>, ny_ / G::R, G::NT, sizeof(C) * G::R * G::LP, (const C*)Ta_, psi_,
                    (const C*)twx_, T(c_.scale), K_);
     });
   }
@@ -805,16 +775,16 @@ class Solver : public SolverBase {
       constexpr int L = decltype(lc)::value;
       typedef GeoX<T, L> G;
       const size_t sm = sizeof(C) * G::R * G::LP;
-      if (!from_t) launch_pdl("k_x1", k_x1<T, L, false, false>, ny_ / G::R, G::NT, sm, (const C*)Ta_, psi_, Tb_, (const C*)twx_, c_);
-      else if (prune) launch_pdl("k_x1", k_x1<T, L, true, true>, ny_ / G::R, G::NT, sm, (const C*)Ta_, psi_, Tb_, (const C*)twx_, c_);
-      else launch_pdl("k_x1", k_x1<T, L, true, false>, ny_ / G::R, G::NT, sm, (const C*)Ta_, psi_, Tb_, (const C*)twx_, c_);
+      if (!from_t) launch_raw("k_x1", k_x1<T, L, false, false>, ny_ / G::R, G::NT, sm, (const C*)Ta_, psi_, Tb_, (const C*)twx_, c_);
+      else if (prune) launch_raw("k_x1", k_x1<T, L, true, true>, ny_ / G::R, G::NT, sm, (const C*)Ta_, psi_, Tb_, (const C*)twx_, c_);
+      else launch_raw("k_x1", k_x1<T, L, true, false>, ny_ / G::R, G::NT, sm, (const C*)Ta_, psi_, Tb_, (const C*)twx_, c_);
     });
   }
   void y1() {
     with_len(ny_, [&](auto lc) {
       constexpr int L = decltype(lc)::value;
       typedef GeoY<T, L> G;
-      launch_pdl("k_y1", k_y1<T, L>, (K_ + 1 + G::R - 1) / G::R, G::NT, sizeof(C) * G::R * G::LP, (const C*)Tb_, Tc_,
+      launch_raw("k_y1", k_y1<T, L>, (K_ + 1 + G::R - 1) / G::R, G::NT, sizeof(C) * G::R * G::LP, (const C*)Tb_, Tc_,
                  (const C*)twy_, c_);
     });
   }
@@ -823,8 +793,8 @@ class Solver : public SolverBase {
       constexpr int L = decltype(lc)::value;
       typedef GeoX<T, L> G;
       const size_t sm = sizeof(C) * G::R * G::LP;
-      if (sign > 0) launch_pdl("k_x2", k_x2<T, L, +1, true, false>, ny_ / G::R, G::NT, sm, (const C*)Tc_, (const C*)psi_, (const T*)nullptr, Td_, (const C*)twx_, c_);
-      else launch_pdl("k_x2", k_x2<T, L, -1, false, false>, ny_ / G::R, G::NT, sm, (const C*)Tc_, (const C*)psi_, (const T*)nullptr, Td_, (const C*)twx_, c_);
+      if (sign > 0) launch_raw("k_x2", k_x2<T, L, +1, true, false>, ny_ / G::R, G::NT, sm, (const C*)Tc_, (const C*)psi_, (const T*)nullptr, Td_, (const C*)twx_, c_);
+      else launch_raw("k_x2", k_x2<T, L, -1, false, false>, ny_ / G::R, G::NT, sm, (const C*)Tc_, (const C*)psi_, (const T*)nullptr, Td_, (const C*)twx_, c_);
       (void)prune_out;
     });
   }
@@ -837,10 +807,10 @@ class Solver : public SolverBase {
       auto go = [&](auto frc_c) {
         constexpr bool F = decltype(frc_c)::value;
         switch (stage) {
-          case 1: launch_pdl("k_y2_rk4", k_y2_rk4<T, L, 1, F>, grid, G::NT, sm, (const C*)Td_, kpsi_, str1_, str2_, Ta_, (const C*)twy_, c_); break;
-          case 2: launch_pdl("k_y2_rk4", k_y2_rk4<T, L, 2, F>, grid, G::NT, sm, (const C*)Td_, kpsi_, str1_, str2_, Ta_, (const C*)twy_, c_); break;
-          case 3: launch_pdl("k_y2_rk4", k_y2_rk4<T, L, 3, F>, grid, G::NT, sm, (const C*)Td_, kpsi_, str1_, str2_, Ta_, (const C*)twy_, c_); break;
-          default: launch_pdl("k_y2_rk4", k_y2_rk4<T, L, 4, F>, grid, G::NT, sm, (const C*)Td_, kpsi_, str1_, str2_, Ta_, (const C*)twy_, c_); break;
+          case 1: launch_raw("k_y2_rk4", k_y2_rk4<T, L, 1, F>, grid, G::NT, sm, (const C*)Td_, kpsi_, str1_, str2_, Ta_, (const C*)twy_, c_); break;
+          case 2: launch_raw("k_y2_rk4", k_y2_rk4<T, L, 2, F>, grid, G::NT, sm, (const C*)Td_, kpsi_, str1_, str2_, Ta_, (const C*)twy_, c_); break;
+          case 3: launch_raw("k_y2_rk4", k_y2_rk4<T, L, 3, F>, grid, G::NT, sm, (const C*)Td_, kpsi_, str1_, str2_, Ta_, (const C*)twy_, c_); break;
+          default: launch_raw("k_y2_rk4", k_y2_rk4<T, L, 4, F>, grid, G::NT, sm, (const C*)Td_, kpsi_, str1_, str2_, Ta_, (const C*)twy_, c_); break;
         }
       };
       if (c_.frc) go(std::true_type());
@@ -855,7 +825,7 @@ class Solver : public SolverBase {
       if (sgle_) {
         auto go = [&](auto rc_, auto dc_) {
           constexpr bool RS = decltype(rc_)::value, DV = decltype(dc_)::value;
-          launch_pdl("k_y2_argle", k_y2_argle<T, L, RS, DV, true>, nx_ / G::R, G::NT, 2 * sm, (const C*)Td_, kpsi_, Ta_,
+          launch_raw("k_y2_argle", k_y2_argle<T, L, RS, DV, true>, nx_ / G::R, G::NT, 2 * sm, (const C*)Td_, kpsi_, Ta_,
                      (const C*)twy_, part_, c_, Tg_, (const C*)Tn_);
         };
         if (resid && flow_) go(std::true_type(), std::true_type());
@@ -863,10 +833,10 @@ class Solver : public SolverBase {
         else if (flow_) go(std::false_type(), std::true_type());
         else go(std::false_type(), std::false_type());
       } else if (flow_) {
-        if (resid) launch_pdl("k_y2_argle", k_y2_argle<T, L, true, true>, nx_ / G::R, G::NT, 2 * sm, (const C*)Td_, kpsi_, Ta_, (const C*)twy_, part_, c_, Tg_, (const C*)nullptr);
-        else launch_pdl("k_y2_argle", k_y2_argle<T, L, false, true>, nx_ / G::R, G::NT, 2 * sm, (const C*)Td_, kpsi_, Ta_, (const C*)twy_, part_, c_, Tg_, (const C*)nullptr);
-      } else if (resid) launch_pdl("k_y2_argle", k_y2_argle<T, L, true>, nx_ / G::R, G::NT, sm, (const C*)Td_, kpsi_, Ta_, (const C*)twy_, part_, c_, (C*)nullptr, (const C*)nullptr);
-      else launch_pdl("k_y2_argle", k_y2_argle<T, L, false>, nx_ / G::R, G::NT, sm, (const C*)Td_, kpsi_, Ta_, (const C*)twy_, part_, c_, (C*)nullptr, (const C*)nullptr);
+        if (resid) launch_raw("k_y2_argle", k_y2_argle<T, L, true, true>, nx_ / G::R, G::NT, 2 * sm, (const C*)Td_, kpsi_, Ta_, (const C*)twy_, part_, c_, Tg_, (const C*)nullptr);
+        else launch_raw("k_y2_argle", k_y2_argle<T, L, false, true>, nx_ / G::R, G::NT, 2 * sm, (const C*)Td_, kpsi_, Ta_, (const C*)twy_, part_, c_, Tg_, (const C*)nullptr);
+      } else if (resid) launch_raw("k_y2_argle", k_y2_argle<T, L, true>, nx_ / G::R, G::NT, sm, (const C*)Td_, kpsi_, Ta_, (const C*)twy_, part_, c_, (C*)nullptr, (const C*)nullptr);
+      else launch_raw("k_y2_argle", k_y2_argle<T, L, false>, nx_ / G::R, G::NT, sm, (const C*)Td_, kpsi_, Ta_, (const C*)twy_, part_, c_, (C*)nullptr, (const C*)nullptr);
     });
   }
 
@@ -990,12 +960,6 @@ class Solver : public SolverBase {
   bool graphs_ok_ = true;
   cudaGraphExec_t g_rk4_ = nullptr, g_argle_ = nullptr;
   unsigned long long* rngc_ = nullptr;  // forcing-phase counter (RHS evaluations)
-  // programmatic dependent launch of the pass kernels (VK_PDL=0 in the
-  // environment turns it off, for comparison)
-  bool pdl_ = [] {
-    const char* e = std::getenv("VK_PDL");
-    return !(e && e[0] == '0');
-  }();
   int flow_ = 0;                          // ARGLE flow terms: 1 advection, 2 counterflow
   int sgle_ = 0;                          // -DGPE_SGLE noise + chemical potential ODE
   double nun_area_ = 0.0;                 // nuN / (Lx Ly)
