@@ -79,3 +79,19 @@ def test_quantglobal_sums():
     assert abs(eintr - spec[4, :].sum()) <= 1e-10 * abs(eintr)
     assert abs(n0 - spec[5, 0]) <= 1e-10 * abs(n0)
     s.close()
+
+
+def test_diagnostics_4096_fp64_largest_grid():
+    """The largest grid (4096^2, nshell = 2897, histogram of K + 3 shells in
+    shared memory beside two 4096-point rows): GPU diagnostics of a
+    1024-vortex state against the oracle's."""
+    import os
+    n = 4096
+    p = vk.params_for(n, dt=5e-4)
+    with vk.GPESolver(p) as s:
+        s.set_psi_vortices(1024, seed=5, min_sep=4 * np.sqrt(2) * 2 * np.pi / n)
+        psi = s.get_psi()
+        o = Oracle.from_vk_params(p, threads=os.cpu_count())
+        o.set_psi(psi, otoc=False)
+        o.set_kpsi(s.get_kpsi())
+        _check(s, o, 1e-12, 1e-10)
