@@ -539,7 +539,8 @@ class Solver : public SolverBase {
       double h[3];
       VK_CUDA_TRY(cudaMemcpyAsync(h, sums_, sizeof(h), cudaMemcpyDeviceToHost, st_));
       VK_CUDA_TRY(cudaStreamSynchronize(st_));
-      *residual = std::sqrt(h[0]) / (p_.dt * std::sqrt(h[1]));
+      // a zero field stays zero: report 0 rather than 0/0
+      *residual = h[1] > 0.0 ? std::sqrt(h[0]) / (p_.dt * std::sqrt(h[1])) : (h[0] > 0.0 ? HUGE_VAL : 0.0);
     }
     return VK_OK;
   }

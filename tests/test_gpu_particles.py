@@ -122,3 +122,16 @@ def test_particles_1024_sixteen_particles_rk4_smoke():
     pos, vel, _ = s.particles_get()
     assert np.isfinite(pos).all() and np.isfinite(vel).all() and np.isfinite(s.get_psi()).all()
     s.close()
+
+
+def test_particles_fp32_bulk():
+    """FP32 bulk path with particles: psi within 1e-5 and positions within
+    1e-6 of the FP64 oracle after 20 steps."""
+    s, o, _ = _state(64, 4, prec=vk.VK_PREC_FP32)
+    s.gpe_rk4(20)
+    o.gpe_rk4(20)
+    assert rel(s.get_psi(), o.get_psi()) < 1e-5
+    pos, _, _ = s.particles_get()
+    opos, _, _ = o.particles_get()
+    assert np.abs(pos - opos).max() < 1e-6
+    s.close()

@@ -153,3 +153,41 @@ def test_sgle_fp32():
     assert rel(s.get_kpsi(), o.get_kpsi()) < 1e-5
     assert abs(s.chempot - o.chempot) <= 1e-6 * abs(o.chempot)
     s.close()
+
+
+def test_variants_nonsquare_grid():
+    """nx != ny (128 x 64): forced-dissipative RK4, counterflow ARGLE and SGLE
+    against the oracle."""
+    nx, ny = 128, 64
+    psi0, _ = vk.ic_vortices(nx, ny, 8, seed=2)
+    p = vk.params_for(nx, ny, dt=1e-3)
+    with vk.GPESolver(p) as s:
+        s.set_psi(psi0)
+        s.set_variant(frcdisp=True, vishypo=0.3, famp=0.2, kf1=2.0, kf2=5.0, seed=9)
+        s.gpe_rk4(20)
+        got = s.get_psi()
+    o = Oracle.from_vk_params(p)
+    o.set_psi(psi0)
+    o.set_frcdisp(True, vishypo=0.3, famp=0.2, kf1=2.0, kf2=5.0, seed=9)
+    o.gpe_rk4(20)
+    assert rel(got, o.get_psi()) < 1e-12
+    with vk.GPESolver(p) as s:
+        s.set_psi(psi0)
+        s.set_variant(flow="counterflow", vnx=0.3, vny=-0.1, sgle=True, oneybeta=0.05, nuN=1.0,
+                      chempot0=p.gstrength, seed=4)
+        s.argle(20)
+        got = s.get_kpsi()
+        mu = s.chempot
+    o = Oracle.from_vk_params(p)
+    o.set_psi(psi0)
+    o.set_argle_flow(2, 0.3, -0.1)
+    o.set_sgle(True, oneybeta=0.05, nuN=1.0, chempot0=p.gstrength, seed=4)
+    o.argle(20)
+    assert rel(got, o.get_kpsi()) < 1e-12
+    assert abs(mu - o.chempot) <= 1e-12 * abs(o.chempot)
+
+
+def test_argle_residual_of_a_zero_field_is_zero():
+    with vk.GPESolver(vk.params_for(32, dt=1e-3, otoc=False)) as s:
+        s.set_psi(np.zeros((32, 32), dtype=complex))
+        assert s.argle(3) == 0.0
