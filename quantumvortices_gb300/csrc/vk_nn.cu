@@ -18,6 +18,7 @@
 #include <cuda_runtime.h>
 #include <cmath>
 #include <cstdint>
+#include <cstdlib>
 #include <cstring>
 #include <string>
 #include <type_traits>
@@ -172,6 +173,143 @@ __global__ void __launch_bounds__(128) k_conv(const bf16* __restrict__ in, int H
         if (out_f)
           for (int j = 0; j < NC; ++j)
             if (n0 + c0 + j < nout) out_f[(size_t)p * nout + n0 + c0 + j] = v[j];
+      }
+    }
+  }
+  tc::fence_before();
+  __syncthreads();
+  if (warp == 0) tc::tmem_dealloc(taddr, NCOL);
+}
+
+// Row-block convolution for the narrow layers (Cin <= 64, W a multiple of
+// 128, H a multiple of RB).  A CTA computes RB output rows x 128 columns x BN
+// channels in RB tensor-memory accumulators.  Each of the RB + 2 input rows
+// it needs (periodic) is gathered once, as three column-shifted K-major tiles
+// (dx = -1, 0, +1; [128 pixels][Cin]); each tile feeds the accumulators of up
+// to three output rows (dy = -1, 0, +1) with the weights of tap (dy, dx),
+// which stay in shared memory for the whole CTA.  Per output pixel that is
+// 3 (RB + 2) / RB gathered row tiles instead of the 9 of k_conv.  Two input
+// stages: row s + 1 is gathered while the tensor core works on row s.
+template <int BN, int CIN, int RB>
+__global__ void __launch_bounds__(128) k_conv_rows(const bf16* __restrict__ in, int H, int W,
+                                                   const bf16* __restrict__ wgt, const float* __restrict__ bias,
+                                                   int cout, int relu, bf16* __restrict__ out_bf, int ldo,
+                                                   float* __restrict__ out_f, int nout, int* __restrict__ err) {
+  constexpr int TA = 128 * CIN * 2;  // one shifted input tile
+  constexpr int STAGE = 3 * TA;
+  constexpr int WT = BN * CIN * 2;   // one tap's weight tile
+  constexpr int VR = CIN / 8;        // 16-byte vectors per pixel
+  constexpr int NS = RB + 2;         // input rows
+  constexpr uint32_t SBO = (CIN / 8) * 128;
+  constexpr int ACC = RB * BN;
+  constexpr uint32_t NCOL = ACC <= 32 ? 32 : (ACC <= 64 ? 64 : (ACC <= 128 ? 128 : (ACC <= 256 ? 256 : 512)));
+  extern __shared__ __align__(1024) unsigned char sm[];
+  unsigned char* sW = sm;           // 9 * WT
+  unsigned char* sI = sm + 9 * WT;  // 2 * STAGE
+  __shared__ __align__(8) uint64_t bar[2];
+  __shared__ uint32_t tslot;
+  const int tid = threadIdx.x, warp = tid >> 5;
+  const int x0 = blockIdx.x * 128, y0 = blockIdx.y * RB, n0 = blockIdx.z * BN;
+  if (warp == 0) tc::tmem_alloc(&tslot, NCOL);
+  if (tid < 2) tc::mbar_init(&bar[tid]);
+  tc::fence_before();
+  __syncthreads();
+  tc::fence_after();
+  const uint32_t taddr = tslot;
+  const uint32_t idesc = tc::idesc_bf16(128, BN);
+  // weights of all nine taps: rows co = n0 + r, K = ci (row stride 9 * CIN)
+  for (int i = tid; i < 9 * BN * VR; i += 128) {
+    const int tap = i / (BN * VR), rem = i - tap * (BN * VR), r = rem / VR, kv = rem - r * VR;
+    tc::cp_async16<false>(sW + tap * WT + tc::tile_off(r, 8 * kv, CIN), wgt + ((size_t)(n0 + r) * 9 + tap) * CIN + 8 * kv,
+                          16u);
+  }
+  tc::cp_async_commit();
+  auto load_row = [&](int srow, int buf) {
+    const int j = wrapi(y0 - 1 + srow, H);
+    unsigned char* st = sI + buf * STAGE;
+    for (int i = tid; i < 3 * 128 * VR; i += 128) {
+      const int dx = i / (128 * VR), rem = i - dx * (128 * VR), m = rem / VR, kv = rem - m * VR;
+      const int x = wrapi(x0 + m + dx - 1, W);
+      tc::cp_async16<true>(st + dx * TA + tc::tile_off(m, 8 * kv, CIN), in + ((size_t)j * W + x) * CIN + 8 * kv, 16u);
+    }
+  };
+  load_row(0, 0);
+  tc::cp_async_commit();
+  bool ok = true;
+  int issued = 0;
+  for (int srow = 0; srow < NS; ++srow) {
+    if (srow + 1 < NS) {
+      if (srow >= 1) ok = tc::mbar_wait(&bar[(srow - 1) & 1], ((srow - 1) >> 1) & 1, err) && ok;  // frees buffer
+      if (ok) load_row(srow + 1, (srow + 1) & 1);
+    }
+    tc::cp_async_commit();
+    tc::cp_async_wait<1>();  // everything but the newest group: row srow (and the weights)
+    tc::fence_async_smem();
+    tc::fence_before();
+    if (!__syncthreads_and(ok)) { ok = false; break; }
+    tc::fence_after();
+    ++issued;
+    if (tid == 0) {
+      const uint32_t a0 = tc::smem_u32(sI + (srow & 1) * STAGE), w0 = tc::smem_u32(sW);
+#pragma unroll
+      for (int dy = -1; dy <= 1; ++dy) {
+        const int r = srow - 1 - dy;  // output row fed by input row srow through dy
+        if (r < 0 || r >= RB) continue;
+#pragma unroll
+        for (int dx = 0; dx < 3; ++dx) {
+          const int tap = (dy + 1) * 3 + dx;
+#pragma unroll
+          for (int kk = 0; kk < CIN / 16; ++kk) {
+            const uint64_t ad = tc::smem_desc(a0 + dx * TA + kk * 256, 128, SBO);
+            const uint64_t bd = tc::smem_desc(w0 + tap * WT + kk * 256, 128, SBO);
+            const bool first = (dy == -1 && dx == 0 && kk == 0);  // input row srow = r opens accumulator r
+            tc::mma(taddr + (uint32_t)(r * BN), ad, bd, idesc, first ? 0u : 1u);
+          }
+        }
+      }
+      tc::commit(&bar[srow & 1]);
+    }
+  }
+  tc::cp_async_wait<0>();
+  if (issued > 0) ok = tc::mbar_wait(&bar[(issued - 1) & 1], ((issued - 1) >> 1) & 1, err) && ok;
+  tc::fence_after();
+  if (__syncthreads_and(ok) && issued == NS) {
+    const int xcol = x0 + 32 * warp + (tid & 31);
+    constexpr int NC = BN < 32 ? 16 : 32;
+#pragma unroll 1
+    for (int r = 0; r < RB; ++r) {
+      const size_t p = (size_t)(y0 + r) * W + xcol;
+#pragma unroll 1
+      for (int c0 = 0; c0 < BN; c0 += NC) {
+        float v[32];
+        const uint32_t ta = taddr + ((uint32_t)(32 * warp) << 16) + (uint32_t)(r * BN + c0);
+        if (NC == 16) tc::tmem_ld16(ta, v);
+        else tc::tmem_ld32(ta, v);
+#pragma unroll
+        for (int j = 0; j < NC; ++j) {
+          const int c = n0 + c0 + j;
+          float a = v[j] + ((bias && c < cout) ? bias[c] : 0.f);
+          if (relu) a = fmaxf(a, 0.f);
+          v[j] = a;
+        }
+        if (out_bf) {
+#pragma unroll
+          for (int q = 0; q < NC / 8; ++q) {
+            uint4 w;
+            __nv_bfloat162 h0 = __floats2bfloat162_rn(v[8 * q + 0], v[8 * q + 1]);
+            __nv_bfloat162 h1 = __floats2bfloat162_rn(v[8 * q + 2], v[8 * q + 3]);
+            __nv_bfloat162 h2 = __floats2bfloat162_rn(v[8 * q + 4], v[8 * q + 5]);
+            __nv_bfloat162 h3 = __floats2bfloat162_rn(v[8 * q + 6], v[8 * q + 7]);
+            w.x = *reinterpret_cast<uint32_t*>(&h0);
+            w.y = *reinterpret_cast<uint32_t*>(&h1);
+            w.z = *reinterpret_cast<uint32_t*>(&h2);
+            w.w = *reinterpret_cast<uint32_t*>(&h3);
+            *reinterpret_cast<uint4*>(out_bf + p * ldo + n0 + c0 + 8 * q) = w;
+          }
+        }
+        if (out_f)
+          for (int j = 0; j < NC; ++j)
+            if (n0 + c0 + j < nout) out_f[p * nout + n0 + c0 + j] = v[j];
       }
     }
   }
@@ -521,6 +659,11 @@ class Net {
   float* out_f = nullptr;     // head output [p][2]
   int64_t steps = 0;
   cudaStream_t st = nullptr;
+  // row-block kernel for the narrow layers (VK_CONV_ROWS=0 turns it off)
+  bool rows_ok_ = [] {
+    const char* e = std::getenv("VK_CONV_ROWS");
+    return !(e && e[0] == '0');
+  }();
   std::vector<void*> allocs;
   // activations (forward) per level and gradient scratch
   Tensor x0;
@@ -655,6 +798,7 @@ class Net {
   // channels split into blocks of BN so that small levels still fill the GPU.
   void conv(const Tensor& in, const bf16* w, int cout_p, int cout, const float* bias, int relu, bf16* out_bf,
             float* out_f32, int nout) {
+    if (conv_rows(in, w, cout_p, cout, bias, relu, out_bf, out_f32, nout)) return;
     const int npix = in.h * in.w;
     const int tiles = (npix + 127) / 128;
     int bn = std::min(cout_p, 128);
@@ -666,6 +810,41 @@ class Net {
       case 64: launch_conv<64>(grid, in, w, bias, cout, relu, out_bf, cout_p, out_f32, nout); break;
       default: launch_conv<128>(grid, in, w, bias, cout, relu, out_bf, cout_p, out_f32, nout); break;
     }
+  }
+  // The row-block kernel for narrow layers when the shape allows it.
+  bool conv_rows(const Tensor& in, const bf16* w, int cout_p, int cout, const float* bias, int relu, bf16* ob,
+                 float* of, int nout) {
+    const int cin = in.c;
+    if (!rows_ok_ || (cin != 16 && cin != 32 && cin != 64) || in.w % 128 != 0 || cout_p > 64) return false;
+    int rb = 4;
+    int bn = cout_p;
+    auto ctas = [&]() { return (in.w / 128) * (in.h / rb) * (cout_p / bn); };
+    if (ctas() < 2 * 152 && bn > 32) bn /= 2;
+    if (ctas() < 2 * 152) rb = 2;
+    if (in.h % rb != 0) return false;
+    const dim3 grid(in.w / 128, in.h / rb, cout_p / bn);
+#define VK_ROWS(B, CI, R)                                                                     \
+  if (bn == B && cin == CI && rb == R) {                                                      \
+    launch_rows<B, CI, R>(grid, in, w, bias, cout, relu, ob, cout_p, of, nout);               \
+    return true;                                                                              \
+  }
+    VK_ROWS(16, 16, 4) VK_ROWS(16, 32, 4) VK_ROWS(16, 64, 4) VK_ROWS(32, 16, 4) VK_ROWS(32, 32, 4)
+    VK_ROWS(32, 64, 4) VK_ROWS(64, 16, 4) VK_ROWS(64, 32, 4) VK_ROWS(64, 64, 4)
+    VK_ROWS(16, 16, 2) VK_ROWS(16, 32, 2) VK_ROWS(16, 64, 2) VK_ROWS(32, 16, 2) VK_ROWS(32, 32, 2)
+    VK_ROWS(32, 64, 2) VK_ROWS(64, 16, 2) VK_ROWS(64, 32, 2) VK_ROWS(64, 64, 2)
+#undef VK_ROWS
+    return false;
+  }
+  template <int BN, int CIN, int RB>
+  void launch_rows(dim3 grid, const Tensor& in, const bf16* w, const float* bias, int cout, int relu, bf16* ob, int ldo,
+                   float* of, int nout) {
+    const size_t smem = (size_t)9 * BN * CIN * 2 + 2 * 3 * 128 * CIN * 2;
+    static bool attr = false;
+    if (!attr) {
+      cudaFuncSetAttribute(k_conv_rows<BN, CIN, RB>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+      attr = true;
+    }
+    k_conv_rows<BN, CIN, RB><<<grid, 128, smem, st>>>(in.d, in.h, in.w, w, bias, cout, relu, ob, ldo, of, nout, err);
   }
   template <int BN>
   void launch_conv(dim3 grid, const Tensor& in, const bf16* w, const float* bias, int cout, int relu, bf16* ob,

@@ -63,3 +63,46 @@ def test_training_reduces_loss():
         last = net.train_step(di, dt, 2e-3, want_loss=True)
     assert last < 0.3 * l0, (l0, last)
     net.close()
+
+
+@pytest.mark.parametrize("h,base,levels", [(128, 16, 2), (128, 32, 2)])
+def test_row_block_conv_matches_oracle(h, base, levels):
+    """Widths that are multiples of 128 take the row-block convolution for the
+    narrow layers: forward and gradient against the oracle as above."""
+    torch = pytest.importorskip("torch")
+    net = WarmStartNet(h, h, base, levels, seed=11)
+    inp, tgt, di, dt = _data(h, seed=3)
+    out = torch.empty((2, h, h), dtype=torch.float32, device="cuda")
+    net.forward(di, out)
+    prm = net.get_params().astype(np.float64)
+    ref, _ = nn_oracle.forward(prm, inp.astype(np.float64), base, levels)
+    assert rel(out.cpu().numpy(), ref) < 1e-2
+    loss, g = net.loss_grad(di, dt)
+    rloss, rg = nn_oracle.loss_grad(prm, inp.astype(np.float64), tgt.astype(np.float64), base, levels)
+    assert abs(loss - rloss) <= 1e-2 * rloss
+    assert rel(g, rg) < 2e-2
+    net.close()
+
+
+def test_row_block_conv_matches_generic_kernel_at_512():
+    """512^2, 4 levels (row blocks of 4 and 2 rows, 16/32/64 channels): the
+    row-block kernel against the generic implicit-GEMM kernel (same BF16
+    products, FP32 sums in another order): output and gradient within 1e-3."""
+    import os
+    torch = pytest.importorskip("torch")
+    h = 512
+    inp, tgt, di, dt = _data(h, seed=4)
+    res = []
+    for flag in ("0", "1"):
+        os.environ["VK_CONV_ROWS"] = flag
+        try:
+            net = WarmStartNet(h, h, 32, 4, seed=2)
+        finally:
+            os.environ.pop("VK_CONV_ROWS", None)
+        out = torch.empty((2, h, h), dtype=torch.float32, device="cuda")
+        net.forward(di, out)
+        loss, g = net.loss_grad(di, dt)
+        res.append((out.cpu().numpy(), loss, g))
+        net.close()
+    (o0, l0, g0), (o1, l1, g1) = res
+    assert rel(o1, o0) < 1e-3 and abs(l1 - l0) <= 1e-3 * l0 and rel(g1, g0) < 1e-3
