@@ -33,8 +33,8 @@ METRIC = "RK4 grid-pt-steps/s at 1024^2"
 UNIT = "grid-pt-steps/s"
 PEAKS_FILE = os.path.join(ROOT, "MEASURED_PEAKS.json")
 FALLBACK_HBM_GBS = 6800.0
-# k_x1<double,1024> DRAM bytes per launch from one ncu capture of this workload
-# (profiles/k_x1_fp64_1024_traffic.md: 11.36 MB read, 0 written within the launch)
+# k_x1<double,1024> DRAM bytes per launch from one ncu capture of this
+# workload (11.36 MB read, 0 written within the launch)
 X1_FP64_1024_DRAM_BYTES = 11361536 + 0
 
 
@@ -227,7 +227,7 @@ def ensemble_bench(torch, K, W, S):
 
 
 def argle_bench(torch, n, psi0):
-    """ARGLE relaxation at n^2 (configs[1]: 2000 steps at dt = 1e-3 from the
+    """ARGLE relaxation at n^2 (the relaxation of the 1024^2 workload: 2000 steps at dt = 1e-3 from the
     64-vortex state), FP64 and FP32: throughput and the residual
     ||kpsi_new - kpsi_old|| / (dt ||kpsi_old||) after the 2000 steps."""
     from quantumvortices_gb300 import vk
@@ -406,7 +406,7 @@ def run_ours(args, rank, world, local_rank):
     flops = kernel_flops(tag, n, Kk)
     f64_tf = flops / (per_launch_ms * 1e-3) / 1e12 if flops else None
     step_ms = ms_max / (K * S)
-    canonical = 1344.0 * n * n / (step_ms * 1e-3) / 1e9  # SURVEY 8(d) model: 84 field transfers
+    canonical = 1344.0 * n * n / (step_ms * 1e-3) / 1e9  # canonical model: 84 field transfers per RK4 step
     out = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": K, "warmup": W,
         "ms_per_step": ms_max / K, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
@@ -420,7 +420,7 @@ def run_ours(args, rank, world, local_rank):
                      "frac": achieved / peak if achieved else None,
                      "traffic": X1_FP64_1024_DRAM_BYTES if (tag == "k_x1" and n == 1024) else None,
                      "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum per launch, "
-                                       "profiles/k_x1_fp64_1024_traffic.md",
+                                       "one capture of this workload at 1024^2",
                      "algorithmic_bytes_per_launch": nbytes, "launch_ms": per_launch_ms,
                      "step_canonical_gbs": canonical, "step_canonical_frac": canonical / peak,
                      "binding": "fp64 pipe (the fields of a 1024^2 step stay in L2)",

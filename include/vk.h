@@ -174,7 +174,7 @@ int vk_kernel_launches(void* ctx, int64_t* count);
  * [2*n_vort] may be NULL. */
 int vk_set_psi_vortices(void* ctx, int32_t n_vort, uint64_t seed, double xi0, double min_sep, double* pos_out);
 
-/* Ensembles (new, no reference counterpart; BASELINE configs[3]): n
+/* Ensembles (new, no reference counterpart): n
  * independent fields of uneven sizes (nx, ny in {128, 256, 512, 1024}, one
  * precision, no particles) stepped together.  Each RK4 pass is one
  * persistent kernel over all members' row tiles; tile heights and grid sizes

@@ -12,7 +12,7 @@
  * file's own radix-2 FP64 transform (FFTW 3.3.8's plan-dependent rounding is
  * not reproducible); tests cross-check it against numpy.fft.
  *
- * One deliberate deviation, documented in the design doc: the uninitialised
+ * One deliberate deviation: the uninitialised
  * `ksqr` used as the dealias test in translate_particle_potential
  * (src/gpe_particle.f90:275, declared :206) is replaced by the intended
  * k1^2+k2^2 of the current mode.

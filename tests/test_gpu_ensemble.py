@@ -56,7 +56,7 @@ def test_ensemble_fp64_members_vs_oracle():
 
 
 def test_ensemble_fp32_config_shape_sample_vs_oracle():
-    """BASELINE configs[3] shape: 192 x 256^2 + 48 x 512^2 in one ensemble,
+    """The benchmark ensemble: 192 x 256^2 + 48 x 512^2 in one ensemble,
     FP32 bulk; a sample of members is checked against the FP64 oracle."""
     sizes = [256] * 192 + [512] * 48
     ps, psis = _members(sizes, vk.VK_PREC_FP32)

@@ -192,7 +192,7 @@ def test_device_vortex_ic_matches_host():
 
 
 def test_4096_fp32_vs_fp64_with_1024_vortices():
-    """configs[3] second part: one 4096^2 field with 1024 vortices, FP32 bulk
+    """One 4096^2 field with 1024 vortices, FP32 bulk
     against plain FP64 after 100 RK4 steps."""
     n = 4096
     out = {}
