@@ -392,7 +392,7 @@ struct Diagnostics {
     with_len(nx, [&](auto lc) {
       constexpr int L = decltype(lc)::value;
       typedef GeoX<T, L> G;
-      S_.launch_raw("k_x1", k_x1<T, L, false, false>, ny / G::R, G::NT, sizeof(C) * G::R * G::LP, (const C*)S_.Ta_,
+      S_.launch_raw("k_x1", k_x1<T, L, false, false>, S_.x_grid(G::R), G::NT, sizeof(C) * G::R * G::LP, (const C*)S_.Ta_,
                     S_.psi_, S_.Tb_, (const C*)S_.twx_, c);
     });
     if (S_.np_ > 0) {

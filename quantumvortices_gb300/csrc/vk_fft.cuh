@@ -180,8 +180,10 @@ __host__ __device__ constexpr int padded(int L) { return L + L / 16; }
 __device__ __forceinline__ int pidx(int i) { return i + (i >> 4); }
 
 // One Stockham stage over NR rows held in s (pitch LP); threads [0, NTA) of
-// the block (size NTB) do the work, all threads pass the barriers.
-template <typename T, int L, int NR, int NTA, int RAD, int NS, int DIR, int NTB>
+// the block (size NTB) do the work, all threads pass the barriers.  The
+// twiddle table holds W_{TWS*L}: TWS = 2 runs an L-point transform on the
+// table of a 2L-point one.
+template <typename T, int L, int NR, int NTA, int RAD, int NS, int DIR, int NTB, int TWS = 1>
 __device__ __forceinline__ void stockham_stage(cplx<T>* s, const cplx<T>* __restrict__ tw) {
   typedef cplx<T> C;
   constexpr int NB = L / RAD;
@@ -202,7 +204,7 @@ __device__ __forceinline__ void stockham_stage(cplx<T>* s, const cplx<T>* __rest
         const int jj = j % NS;
 #pragma unroll
         for (int m = 1; m < RAD; ++m) {
-          C w = __ldg(tw + jj * m * (L / (NS * RAD)));
+          C w = __ldg(tw + jj * m * (TWS * L / (NS * RAD)));
           if (DIR > 0) w.y = -w.y;
           v[p][m] = cmul(v[p][m], w);
         }
@@ -225,13 +227,13 @@ __device__ __forceinline__ void stockham_stage(cplx<T>* s, const cplx<T>* __rest
   __syncthreads();
 }
 
-template <typename T, int L, int NR, int NTA, int DIR, int NS, int NTB>
+template <typename T, int L, int NR, int NTA, int DIR, int NS, int NTB, int TWS>
 __device__ __forceinline__ void run_stages(cplx<T>*, const cplx<T>*, RadixList<>) {}
 
-template <typename T, int L, int NR, int NTA, int DIR, int NS, int NTB, int RAD, int... Rest>
+template <typename T, int L, int NR, int NTA, int DIR, int NS, int NTB, int TWS, int RAD, int... Rest>
 __device__ __forceinline__ void run_stages(cplx<T>* s, const cplx<T>* tw, RadixList<RAD, Rest...>) {
-  stockham_stage<T, L, NR, NTA, RAD, NS, DIR, NTB>(s, tw);
-  run_stages<T, L, NR, NTA, DIR, NS * RAD, NTB>(s, tw, RadixList<Rest...>());
+  stockham_stage<T, L, NR, NTA, RAD, NS, DIR, NTB, TWS>(s, tw);
+  run_stages<T, L, NR, NTA, DIR, NS * RAD, NTB, TWS>(s, tw, RadixList<Rest...>());
 }
 
 __host__ __device__ constexpr int plan_maxrad(int e) { return e >= 16 ? 16 : (e >= 8 ? 8 : 4); }
@@ -282,14 +284,16 @@ __device__ __forceinline__ void fft_rows_warp(cplx<T>* s, const cplx<T>* __restr
 // FP32 1024-point rows with exactly one warp per row take the warp-per-row
 // transform instead (the x passes; measured on GB300, the y passes and the
 // paired half-height transforms are faster in the Stockham stages).
-template <typename T, int L, int NR, int NTA, int DIR, int NTB = NTA>
+// TWS = 2: tw is the table of a 2L-point transform (the half-length
+// transforms of single real rows).
+template <typename T, int L, int NR, int NTA, int DIR, int NTB = NTA, int TWS = 1>
 __device__ __forceinline__ void fft_rows(cplx<T>* s, const cplx<T>* __restrict__ tw) {
-  if constexpr (sizeof(T) == 4 && L == 1024 && NTA == NTB && NTA == 32 * NR) {
+  if constexpr (sizeof(T) == 4 && L == 1024 && NTA == NTB && NTA == 32 * NR && TWS == 1) {
     fft_rows_warp<T, L, NR, DIR>(s, tw);
   } else {
     constexpr int E = NR * L / NTA;
     static_assert(E >= 4, "at least four points per thread");
-    run_stages<T, L, NR, NTA, DIR, 1, NTB>(s, tw, typename PlanFor<L, plan_maxrad(E)>::type());
+    run_stages<T, L, NR, NTA, DIR, 1, NTB, TWS>(s, tw, typename PlanFor<L, plan_maxrad(E)>::type());
   }
 }
 

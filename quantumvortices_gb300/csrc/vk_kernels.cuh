@@ -47,8 +47,9 @@ inline void ensure_smem_attr(const void* fn, size_t dyn_bytes) {
 // NT = R*L/16 threads: full-height transforms run radix-16 stages, the
 // half-height paired transforms radix-8 stages on the same threads.  The
 // FP32 x passes at L = 1024 use one warp per row (NT = 32 R) and the
-// warp-per-row transform of vk_fft.cuh; the choice of geometry and of the
-// transform per pass follows whole-step timings on GB300.
+// warp-per-row transform of vk_fft.cuh; the FP64 y passes at L = 1024 run
+// four warps per row (8 points per thread); the choice of geometry and of
+// the transform per pass follows timings on GB300.
 // MINB is the CTAs per SM the register budget is sized for.
 template <typename T, int L> struct GeoX;
 template <typename T, int L> struct GeoY;
@@ -63,7 +64,7 @@ VK_GEO(GeoX, double, 128, 8, 4) VK_GEO(GeoX, double, 256, 4, 4) VK_GEO(GeoX, dou
 VK_GEO(GeoX, double, 1024, 2, 4) VK_GEO(GeoX, double, 2048, 2, 2) VK_GEO(GeoX, double, 4096, 2, 1)
 VK_GEO(GeoY, double, 16, 16, 4) VK_GEO(GeoY, double, 32, 8, 8) VK_GEO(GeoY, double, 64, 4, 8)
 VK_GEO(GeoY, double, 128, 2, 8) VK_GEO(GeoY, double, 256, 1, 8) VK_GEO(GeoY, double, 512, 1, 8)
-VK_GEO(GeoY, double, 1024, 1, 8) VK_GEO(GeoY, double, 2048, 1, 4) VK_GEO(GeoY, double, 4096, 1, 2)
+VK_GEOE(GeoY, double, 1024, 1, 5, 8) VK_GEO(GeoY, double, 2048, 1, 4) VK_GEO(GeoY, double, 4096, 1, 2)
 VK_GEO(GeoX, float, 16, 16, 4) VK_GEO(GeoX, float, 32, 16, 4) VK_GEO(GeoX, float, 64, 16, 4)
 VK_GEO(GeoX, float, 128, 8, 4) VK_GEO(GeoX, float, 256, 4, 4) VK_GEO(GeoX, float, 512, 2, 8)
 VK_GEOE(GeoX, float, 1024, 4, 2, 32) VK_GEO(GeoX, float, 2048, 2, 2) VK_GEO(GeoX, float, 4096, 2, 1)
@@ -112,6 +113,9 @@ struct StepConsts {
   int K;             // max |k| kept by the 2/3 rule
   int k2max;         // largest kept k1^2+k2^2
   int pk;            // row pitch of Tc (>= K+1)
+  // x passes: the last xsingle CTAs of k_x1/k_x2 take one row each (the
+  // half-length real transforms) instead of R rows; 0 = row groups only.
+  int xsingle;
   double alpha, g, omega, dt;
   double prefac_re, prefac_im;   // (1 - i*disp_factor)/i
   double scale;      // 1/(nx*ny)
@@ -348,12 +352,74 @@ __device__ __forceinline__ void x1_body(const cplx<T>* __restrict__ Ta, cplx<T>*
   }
 }
 
+// X1 on one row y (the tail CTAs of k_x1).  The real row rho runs as the
+// L/2-point complex transform of z[n] = rho(2n) + i rho(2n+1) on the L-point
+// twiddle table, and is unpacked with
+//   E(k) = (Z(k) + conj Z(L/2-k))/2,  O(k) = -i (Z(k) - conj Z(L/2-k))/2,
+//   rho^(k) = E(k) + W_L^k O(k),  k in [0, K] (K < L/2).
+template <typename T, int L, class G, bool FROM_T, bool PRUNE, bool SPREAD = false>
+__device__ __forceinline__ void x1_single_body(const cplx<T>* __restrict__ Ta, cplx<T>* __restrict__ psi,
+                                               cplx<T>* __restrict__ Tb, const cplx<T>* __restrict__ tw,
+                                               StepConsts c, const int y, cplx<T>* __restrict__ s) {
+  typedef cplx<T> C;
+  constexpr int H = L / 2;
+  constexpr bool SP = SPREAD && H / G::NT >= 4;  // all threads in both transforms
+  constexpr int NA = SP || G::NT < L / 16 ? G::NT : L / 16;  // threads of the L-point transform
+  constexpr int NH = SP || G::NT < H / 8 ? G::NT : H / 8;    // threads of the L/2-point transform
+  const int ny = c.ny, K = c.K;
+  if (FROM_T) {
+    stage_rows<T, L, 1, G::NT, G::LP>(s, [&](int, int k) {
+      C v = mkc<T>(T(0), T(0));
+      if (!PRUNE || k <= K || k >= L - K) v = Ta[(size_t)y * L + k];
+      return v;
+    });
+    __syncthreads();
+    fft_rows<T, L, 1, NA, +1, G::NT>(s, tw);
+    const T scale = T(c.scale);
+    for (int x = threadIdx.x; x < L; x += G::NT) {
+      const C v = cscale(s[pidx(x)], scale);
+      s[pidx(x)] = v;
+      psi[(size_t)y * L + x] = v;
+    }
+  } else {
+    stage_rows<T, L, 1, G::NT, G::LP>(s, [&](int, int x) { return psi[(size_t)y * L + x]; });
+  }
+  __syncthreads();
+  constexpr int PER = H / G::NT;
+  static_assert(H % G::NT == 0, "half-row tile");
+  C z[PER];
+  const T bg = T(c.rho_bg);
+#pragma unroll
+  for (int q = 0; q < PER; ++q) {
+    const int n = threadIdx.x + q * G::NT;
+    const C a = s[pidx(2 * n)], b = s[pidx(2 * n + 1)];
+    z[q] = mkc<T>(a.x * a.x + a.y * a.y - bg, b.x * b.x + b.y * b.y - bg);
+  }
+  __syncthreads();
+#pragma unroll
+  for (int q = 0; q < PER; ++q) s[pidx(threadIdx.x + q * G::NT)] = z[q];
+  __syncthreads();
+  fft_rows<T, H, 1, NH, -1, G::NT, 2>(s, tw);
+  for (int k = threadIdx.x; k <= K; k += G::NT) {
+    const C zk = s[pidx(k)], zm = s[pidx((H - k) & (H - 1))];
+    const T er = T(0.5) * (zk.x + zm.x), ei = T(0.5) * (zk.y - zm.y);
+    const T o_r = T(0.5) * (zk.y + zm.y), o_i = T(0.5) * (zm.x - zk.x);
+    const C w = __ldg(tw + k);
+    Tb[(size_t)k * ny + y] = mkc<T>(er + (w.x * o_r - w.y * o_i), ei + (w.x * o_i + w.y * o_r));
+  }
+}
+
 template <typename T, int L, bool FROM_T, bool PRUNE>
 __global__ void __launch_bounds__(GeoX<T, L>::NT, GeoX<T, L>::MINB) k_x1(const cplx<T>* __restrict__ Ta, cplx<T>* __restrict__ psi,
                                                    cplx<T>* __restrict__ Tb, const cplx<T>* __restrict__ tw,
                                                    StepConsts c) {
   extern __shared__ __align__(16) unsigned char smraw[];
-  x1_body<T, L, GeoX<T, L>, FROM_T, PRUNE>(Ta, psi, Tb, tw, c, blockIdx.x, reinterpret_cast<cplx<T>*>(smraw));
+  const int npair = (int)gridDim.x - c.xsingle;
+  if (L < 128 || (int)blockIdx.x < npair)
+    x1_body<T, L, GeoX<T, L>, FROM_T, PRUNE>(Ta, psi, Tb, tw, c, blockIdx.x, reinterpret_cast<cplx<T>*>(smraw));
+  else if constexpr (L >= 128)
+    x1_single_body<T, L, GeoX<T, L>, FROM_T, PRUNE>(Ta, psi, Tb, tw, c, GeoX<T, L>::R * npair + ((int)blockIdx.x - npair),
+                                                    reinterpret_cast<cplx<T>*>(smraw));
 }
 
 // ------------------------------------------------------------------------
@@ -466,12 +532,81 @@ __device__ __forceinline__ void x2_body(const cplx<T>* __restrict__ Tc, const cp
   }
 }
 
+// X2 on one row y (the tail CTAs of k_x2).  The Hermitian row A(k) of Tc
+// (A(k) = conj A(L-k), zero for K < k < L-K) is inverted as one L/2-point
+// complex transform: with
+//   Z(k) = A(k) + conj A(L/2-k) + i (A(k) - conj A(L/2-k)) W_L^-k,
+// k in [0, L/2), F^-1 Z (n) = P_G rho(2n) + i P_G rho(2n+1).
+template <typename T, int L, class G, int SIGN, bool PRUNE_OUT, bool POT, bool SPREAD = false>
+__device__ __forceinline__ void x2_single_body(const cplx<T>* __restrict__ Tc, const cplx<T>* __restrict__ psi,
+                                               const T* __restrict__ vpot, cplx<T>* __restrict__ Td,
+                                               const cplx<T>* __restrict__ tw, StepConsts c, const int y,
+                                               cplx<T>* __restrict__ s) {
+  typedef cplx<T> C;
+  constexpr int H = L / 2;
+  constexpr bool SP = SPREAD && H / G::NT >= 4;
+  constexpr int NA = SP || G::NT < L / 16 ? G::NT : L / 16;
+  constexpr int NH = SP || G::NT < H / 8 ? G::NT : H / 8;
+  const int K = c.K, ny = c.ny;
+  const C* row = Tc + (size_t)y * c.pk;
+  stage_rows<T, H, 1, G::NT, padded(H)>(s, [&](int, int k) {
+    const int m = H - k;
+    const C a = k <= K ? row[k] : mkc<T>(T(0), T(0));
+    const C b = m <= K ? row[m] : mkc<T>(T(0), T(0));
+    const T er = a.x + b.x, ei = a.y - b.y;  // a + conj b
+    const T dr = a.x - b.x, di = a.y + b.y;  // a - conj b
+    const C w = __ldg(tw + k);               // W_L^k; W_L^-k = conj
+    const T o_r = dr * w.x + di * w.y, o_i = di * w.x - dr * w.y;
+    return mkc<T>(er - o_i, ei + o_r);
+  });
+  __syncthreads();
+  fft_rows<T, H, 1, NH, +1, G::NT, 2>(s, tw);
+  constexpr int PER = L / G::NT;
+  C nv[PER];
+  const T gs = T(SIGN * c.g);
+  const T scale = T(c.scale);
+#pragma unroll
+  for (int q = 0; q < PER; ++q) {
+    const int x = threadIdx.x + q * G::NT;
+    const C z = s[pidx(x >> 1)];
+    const T pg = ((x & 1) == 0 ? z.x : z.y) * scale;  // P_G[|psi|^2](x, y)
+    const C ps = psi[(size_t)y * L + x];
+    const T gp = gs * pg;
+    C n = mkc<T>(gp * ps.x, gp * ps.y);
+    if (POT) {
+      const T v = T(SIGN) * vpot[(size_t)y * L + x];
+      n.x += v * ps.x;
+      n.y += v * ps.y;
+    }
+    nv[q] = n;
+  }
+  __syncthreads();
+#pragma unroll
+  for (int q = 0; q < PER; ++q) s[pidx(threadIdx.x + q * G::NT)] = nv[q];
+  __syncthreads();
+  fft_rows<T, L, 1, NA, -1, G::NT>(s, tw);
+  if (PRUNE_OUT) {
+    for (int l = threadIdx.x; l < 2 * K + 1; l += G::NT) {
+      const int k = pruned_row(l, K, L);
+      Td[(size_t)k * ny + y] = s[pidx(k)];
+    }
+  } else {
+    for (int k = threadIdx.x; k < L; k += G::NT) Td[(size_t)k * ny + y] = s[pidx(k)];
+  }
+}
+
 template <typename T, int L, int SIGN, bool PRUNE_OUT, bool POT>
 __global__ void __launch_bounds__(GeoX<T, L>::NT, GeoX<T, L>::MINB) k_x2(const cplx<T>* __restrict__ Tc, const cplx<T>* __restrict__ psi,
                                                    const T* __restrict__ vpot, cplx<T>* __restrict__ Td,
                                                    const cplx<T>* __restrict__ tw, StepConsts c) {
   extern __shared__ __align__(16) unsigned char smraw[];
-  x2_body<T, L, GeoX<T, L>, SIGN, PRUNE_OUT, POT>(Tc, psi, vpot, Td, tw, c, blockIdx.x, reinterpret_cast<cplx<T>*>(smraw));
+  const int npair = (int)gridDim.x - c.xsingle;
+  if (L < 128 || (int)blockIdx.x < npair)
+    x2_body<T, L, GeoX<T, L>, SIGN, PRUNE_OUT, POT>(Tc, psi, vpot, Td, tw, c, blockIdx.x, reinterpret_cast<cplx<T>*>(smraw));
+  else if constexpr (L >= 128)
+    x2_single_body<T, L, GeoX<T, L>, SIGN, PRUNE_OUT, POT, true>(Tc, psi, vpot, Td, tw, c,
+                                                           GeoX<T, L>::R * npair + ((int)blockIdx.x - npair),
+                                                           reinterpret_cast<cplx<T>*>(smraw));
 }
 
 // ------------------------------------------------------------------------
@@ -680,8 +815,10 @@ __device__ __forceinline__ void y2_argle_body(const cplx<T>* __restrict__ Td, cp
   }
 }
 
+// The flow and noise variants hold two rows per CTA: at most four CTAs per
+// SM, so that they keep 128 registers a thread.
 template <typename T, int L, bool RESID, bool DERIV = false, bool SGLE = false>
-__global__ void __launch_bounds__(GeoY<T, L>::NT, GeoY<T, L>::MINB) k_y2_argle(const cplx<T>* __restrict__ Td, cplx<T>* __restrict__ kpsi,
+__global__ void __launch_bounds__(GeoY<T, L>::NT, (DERIV || SGLE) && GeoY<T, L>::MINB > 4 ? 4 : GeoY<T, L>::MINB) k_y2_argle(const cplx<T>* __restrict__ Td, cplx<T>* __restrict__ kpsi,
                                                          cplx<T>* __restrict__ Ta, const cplx<T>* __restrict__ tw,
                                                          double* __restrict__ part, StepConsts c,
                                                          cplx<T>* __restrict__ Tg = nullptr,

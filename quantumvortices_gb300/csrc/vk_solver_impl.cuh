@@ -3,6 +3,7 @@
 #pragma once
 #include <cuda_runtime.h>
 #include <cmath>
+#include <cstdlib>
 #include <cstring>
 #include <mutex>
 #include <string>
@@ -146,6 +147,14 @@ class Solver : public SolverBase {
     c_.prefac_im = -1.0;
     c_.scale = 1.0 / ((double)nx_ * (double)ny_);
     c_.rho_bg = std::is_same<T, double>::value ? 0.0 : (p_.gstrength != 0.0 ? p_.omega_chem / p_.gstrength : 0.0);
+    // FP64 x passes at nx = 1024 run one row per CTA.  The pass is bound by
+    // the FP64 pipe of the busiest SM: 512 row-pair CTAs leave 4 pairs on
+    // some SMs and 3 on others (135 us for k_x1 on GB300), while 1024
+    // single-row CTAs, 608 resident and the rest taking the SMs that free
+    // first, even the rows out (119 us).  VK_XSPLIT=0 keeps the row pairs.
+    c_.xsingle = 0;
+    const char* xs_env = std::getenv("VK_XSPLIT");
+    if (std::is_same<T, double>::value && nx_ == 1024 && !(xs_env && xs_env[0] == '0')) c_.xsingle = ny_;
     if (p_.n_particles > 0) {
       int prc = init_particles();
       if (prc) return prc;
@@ -683,6 +692,8 @@ class Solver : public SolverBase {
     ev_used_ = 0;
     return VK_OK;
   }
+  // CTAs of k_x1 / k_x2: row groups of R, then c_.xsingle single rows.
+  int x_grid(int R) const { return (ny_ - c_.xsingle) / R + c_.xsingle; }
   static int geo_rows_x(int L) {
     int r = 0;
     with_len(L, [&](auto lc) { r = GeoX<T, decltype(lc)::value>::R; });
@@ -776,9 +787,10 @@ class Solver : public SolverBase {
       constexpr int L = decltype(lc)::value;
       typedef GeoX<T, L> G;
       const size_t sm = sizeof(C) * G::R * G::LP;
-      if (!from_t) launch_raw("k_x1", k_x1<T, L, false, false>, ny_ / G::R, G::NT, sm, (const C*)Ta_, psi_, Tb_, (const C*)twx_, c_);
-      else if (prune) launch_raw("k_x1", k_x1<T, L, true, true>, ny_ / G::R, G::NT, sm, (const C*)Ta_, psi_, Tb_, (const C*)twx_, c_);
-      else launch_raw("k_x1", k_x1<T, L, true, false>, ny_ / G::R, G::NT, sm, (const C*)Ta_, psi_, Tb_, (const C*)twx_, c_);
+      const int grid = x_grid(G::R);
+      if (!from_t) launch_raw("k_x1", k_x1<T, L, false, false>, grid, G::NT, sm, (const C*)Ta_, psi_, Tb_, (const C*)twx_, c_);
+      else if (prune) launch_raw("k_x1", k_x1<T, L, true, true>, grid, G::NT, sm, (const C*)Ta_, psi_, Tb_, (const C*)twx_, c_);
+      else launch_raw("k_x1", k_x1<T, L, true, false>, grid, G::NT, sm, (const C*)Ta_, psi_, Tb_, (const C*)twx_, c_);
     });
   }
   void y1() {
@@ -794,8 +806,9 @@ class Solver : public SolverBase {
       constexpr int L = decltype(lc)::value;
       typedef GeoX<T, L> G;
       const size_t sm = sizeof(C) * G::R * G::LP;
-      if (sign > 0) launch_raw("k_x2", k_x2<T, L, +1, true, false>, ny_ / G::R, G::NT, sm, (const C*)Tc_, (const C*)psi_, (const T*)nullptr, Td_, (const C*)twx_, c_);
-      else launch_raw("k_x2", k_x2<T, L, -1, false, false>, ny_ / G::R, G::NT, sm, (const C*)Tc_, (const C*)psi_, (const T*)nullptr, Td_, (const C*)twx_, c_);
+      const int grid = x_grid(G::R);
+      if (sign > 0) launch_raw("k_x2", k_x2<T, L, +1, true, false>, grid, G::NT, sm, (const C*)Tc_, (const C*)psi_, (const T*)nullptr, Td_, (const C*)twx_, c_);
+      else launch_raw("k_x2", k_x2<T, L, -1, false, false>, grid, G::NT, sm, (const C*)Tc_, (const C*)psi_, (const T*)nullptr, Td_, (const C*)twx_, c_);
       (void)prune_out;
     });
   }

@@ -63,6 +63,35 @@ def test_rk4_parity_fp64_1024():
     s.close()
 
 
+def test_x_single_rows_equal_row_pairs_1024(monkeypatch):
+    """The FP64 x passes at nx = 1024 run one real row per CTA (half-length
+    complex transforms); VK_XSPLIT=0 selects the row-pair transforms.  Both
+    layouts agree to rounding through RK4, ARGLE and the diagnostics."""
+    p = vk.params_for(1024, dt=5e-4)
+    psi0, _ = vk.ic_vortices(1024, 1024, 32, seed=4)
+    out = []
+    for flag in ("1", "0"):
+        monkeypatch.setenv("VK_XSPLIT", flag)
+        with vk.GPESolver(p) as s:
+            s.set_psi(psi0)
+            r = s.argle(10)
+            s.gpe_rk4(20)
+            out.append((s.get_psi(), r, s.diagnostics_gpe().etot))
+    assert rel(out[0][0], out[1][0]) < 1e-13
+    assert abs(out[0][1] - out[1][1]) <= 1e-12 * abs(out[1][1])
+    assert abs(out[0][2] - out[1][2]) <= 1e-12 * abs(out[1][2])
+
+
+def test_x_single_rows_nonsquare_1024_by_256():
+    s, o, _ = _pair(1024, 256, nv=8, seed=6)
+    s.argle(5)
+    o.argle(5)
+    s.gpe_rk4(10)
+    o.gpe_rk4(10)
+    assert rel(s.get_psi(), o.get_psi()) < 1e-12
+    s.close()
+
+
 def test_rk4_without_otoc_uses_raw_psi_first_stage():
     s, o, _ = _pair(64, otoc=False, nv=4)
     s.gpe_rk4(10)
