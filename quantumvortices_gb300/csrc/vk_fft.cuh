@@ -11,8 +11,8 @@
 //
 // FP64 on GB300 issues about two DFMA per clock per SM, so the codelets are
 // written for the fewest floating-point instructions: radix-16/8/4 butterflies
-// with +-i rotations as register swaps, W8 rotations as add+mul, and table
-// twiddles as 2 MUL + 2 FMA.
+// with +-i rotations as register swaps, and every product by a constant
+// rotation or a table twiddle fused into the butterfly that consumes it.
 #pragma once
 #include <cuda_runtime.h>
 #include <stdint.h>
@@ -62,59 +62,121 @@ template <int DIR, typename C, typename T> __device__ __forceinline__ C rotc(C a
 }
 
 // ---- radix codelets: v[k] <- sum_m v[m] exp(DIR*2*pi*i*m*k/RAD) ----------
+//
+// Each codelet is a first butterfly layer over the pairs (m, m + RAD/2)
+// followed by a tail.  Butterflies whose second operand is multiplied by a
+// constant rotation or a table twiddle w are written as
+//   e' = e + w o   (four FMAs: the products fused into the sum),
+//   o' = e - w o = 2e - e'   (two FMAs),
+// six FP64 instructions instead of four for the product and four for the
+// sum and difference; the FP64 passes are bound by the FP64 pipe.
 
-template <int DIR, typename C> __device__ __forceinline__ void dft2(C& a, C& b) {
-  C t = a;
-  a = cadd(t, b);
-  b = csub(t, b);
+template <typename C> __device__ __forceinline__ void bfly(C& e, C& o) {
+  const C t = e;
+  e = cadd(t, o);
+  o = csub(t, o);
 }
 
-template <int DIR, typename C> __device__ __forceinline__ void dft4(C& a0, C& a1, C& a2, C& a3) {
-  C t0 = cadd(a0, a2), t1 = csub(a0, a2);
-  C t2 = cadd(a1, a3), t3 = rot90<DIR>(csub(a1, a3));
-  a0 = cadd(t0, t2);
-  a2 = csub(t0, t2);
-  a1 = cadd(t1, t3);
-  a3 = csub(t1, t3);
+// (e, o) <- (e + w o, e - w o) for w = (c, DIR*s).
+template <int DIR, typename C, typename T> __device__ __forceinline__ void bfly_rot(C& e, C& o, T c, T s) {
+  C p;
+  if (DIR < 0) {  // w o = (o.x c + o.y s, o.y c - o.x s)
+    p.x = fma(o.x, c, fma(o.y, s, e.x));
+    p.y = fma(o.y, c, fma(-o.x, s, e.y));
+  } else {        // w o = (o.x c - o.y s, o.y c + o.x s)
+    p.x = fma(o.x, c, fma(-o.y, s, e.x));
+    p.y = fma(o.y, c, fma(o.x, s, e.y));
+  }
+  o.x = fma(T(2), e.x, -p.x);
+  o.y = fma(T(2), e.y, -p.y);
+  e = p;
 }
 
-template <int DIR, typename C> __device__ __forceinline__ void dft8(C* v) {
-  // even / odd DFT4 then one radix-2 layer with W8 rotations.
+// (a, b) <- (a + w b, a - w b) for a table twiddle w (already conjugated for
+// the inverse).
+template <typename C> __device__ __forceinline__ void bfly_tw(C& a, C& b, C w) {
+  typedef decltype(a.x) T;
+  C p;
+  p.x = fma(b.x, w.x, fma(-b.y, w.y, a.x));
+  p.y = fma(b.y, w.x, fma(b.x, w.y, a.y));
+  b.x = fma(T(2), a.x, -p.x);
+  b.y = fma(T(2), a.y, -p.y);
+  a = p;
+}
+
+// Tails: on entry v[m] = s_m = x_m + x_{m+RAD/2} and v[m+RAD/2] = d_m =
+// x_m - x_{m+RAD/2} (m < RAD/2) for the RAD inputs x; on return v holds the
+// DFT of x in natural order.
+
+template <int DIR, typename C> __device__ __forceinline__ void dft4_tail(C& a0, C& a1, C& a2, C& a3) {
+  // in: a0 = s0, a1 = s1, a2 = d0, a3 = d1
+  C s0 = a0, s1 = a1, d0 = a2, d1 = rot90<DIR>(a3);
+  bfly(s0, s1);
+  bfly(d0, d1);
+  a0 = s0; a2 = s1; a1 = d0; a3 = d1;
+}
+
+template <int DIR, typename C> __device__ __forceinline__ void dft8_tail(C* v) {
+  typedef decltype(v[0].x) T;
+  const T r = T(0.70710678118654752440084436210484903928);
+  // even outputs: DFT4 of x0, x2, x4, x6 (pairs (x0,x4), (x2,x6));
+  // odd: DFT4 of x1, x3, x5, x7 (pairs (x1,x5), (x3,x7))
   C e0 = v[0], e1 = v[2], e2 = v[4], e3 = v[6];
   C o0 = v[1], o1 = v[3], o2 = v[5], o3 = v[7];
-  dft4<DIR>(e0, e1, e2, e3);
-  dft4<DIR>(o0, o1, o2, o3);
-  o1 = rot45<DIR>(o1);
+  dft4_tail<DIR>(e0, e1, e2, e3);
+  dft4_tail<DIR>(o0, o1, o2, o3);
+  bfly(e0, o0);
+  bfly_rot<DIR>(e1, o1, r, r);
   o2 = rot90<DIR>(o2);
-  o3 = rot135<DIR>(o3);
-  v[0] = cadd(e0, o0); v[4] = csub(e0, o0);
-  v[1] = cadd(e1, o1); v[5] = csub(e1, o1);
-  v[2] = cadd(e2, o2); v[6] = csub(e2, o2);
-  v[3] = cadd(e3, o3); v[7] = csub(e3, o3);
+  bfly(e2, o2);
+  bfly_rot<DIR>(e3, o3, -r, r);
+  v[0] = e0; v[1] = e1; v[2] = e2; v[3] = e3;
+  v[4] = o0; v[5] = o1; v[6] = o2; v[7] = o3;
 }
 
-template <int DIR, typename C> __device__ __forceinline__ void dft16(C* v) {
+template <int DIR, typename C> __device__ __forceinline__ void dft16_tail(C* v) {
   typedef decltype(v[0].x) T;
-  C e[8], o[8];
-#pragma unroll
-  for (int i = 0; i < 8; ++i) { e[i] = v[2 * i]; o[i] = v[2 * i + 1]; }
-  dft8<DIR>(e);
-  dft8<DIR>(o);
+  const T r = T(0.70710678118654752440084436210484903928);
   const T c1 = T(0.92387953251128675612818318939678828682);  // cos(pi/8)
   const T s1 = T(0.38268343236508977172845998403039886676);  // sin(pi/8)
-  o[1] = rotc<DIR>(o[1], c1, s1);
-  o[2] = rot45<DIR>(o[2]);
-  o[3] = rotc<DIR>(o[3], s1, c1);
+  // even outputs: DFT8 of x_{2i} (its pairs (x_{2i}, x_{2i+8}) are s_{2i}, d_{2i})
+  C e[8], o[8];
+#pragma unroll
+  for (int i = 0; i < 4; ++i) {
+    e[i] = v[2 * i]; e[i + 4] = v[8 + 2 * i];
+    o[i] = v[2 * i + 1]; o[i + 4] = v[9 + 2 * i];
+  }
+  dft8_tail<DIR>(e);
+  dft8_tail<DIR>(o);
+  bfly(e[0], o[0]);
+  bfly_rot<DIR>(e[1], o[1], c1, s1);
+  bfly_rot<DIR>(e[2], o[2], r, r);
+  bfly_rot<DIR>(e[3], o[3], s1, c1);
   o[4] = rot90<DIR>(o[4]);
-  o[5] = rot90<DIR>(rotc<DIR>(o[5], c1, s1));
-  o[6] = rot135<DIR>(o[6]);
-  o[7] = rot90<DIR>(rotc<DIR>(o[7], s1, c1));
+  bfly(e[4], o[4]);
+  bfly_rot<DIR>(e[5], o[5], -s1, c1);
+  bfly_rot<DIR>(e[6], o[6], -r, r);
+  bfly_rot<DIR>(e[7], o[7], -c1, s1);
 #pragma unroll
   for (int k = 0; k < 8; ++k) {
-    v[k] = cadd(e[k], o[k]);
-    v[k + 8] = csub(e[k], o[k]);
+    v[k] = e[k];
+    v[k + 8] = o[k];
   }
 }
+
+template <int RAD, int DIR, typename C> __device__ __forceinline__ void dft_tail(C* v) {
+  if (RAD == 4) dft4_tail<DIR>(v[0], v[1], v[2], v[3]);
+  else if (RAD == 8) dft8_tail<DIR>(v);
+  else if (RAD == 16) dft16_tail<DIR>(v);
+}
+
+template <int RAD, int DIR, typename C> __device__ __forceinline__ void dft(C* v) {
+#pragma unroll
+  for (int m = 0; m < RAD / 2; ++m) bfly(v[m], v[m + RAD / 2]);
+  dft_tail<RAD, DIR>(v);
+}
+
+template <int DIR, typename C> __device__ __forceinline__ void dft16(C* v) { dft<16, DIR>(v); }
 
 // 32-point DFT in registers: even/odd DFT16 and one radix-2 layer with the
 // W32^k rotations, k = 0..15 (cos and sin of k*pi/16).
@@ -150,12 +212,6 @@ template <int DIR, typename C> __device__ __forceinline__ void dft32(C* v) {
   }
 }
 
-template <int RAD, int DIR, typename C> __device__ __forceinline__ void dft(C* v) {
-  if (RAD == 2) dft2<DIR>(v[0], v[1]);
-  else if (RAD == 4) dft4<DIR>(v[0], v[1], v[2], v[3]);
-  else if (RAD == 8) dft8<DIR>(v);
-  else if (RAD == 16) dft16<DIR>(v);
-}
 
 // ---- plans ----------------------------------------------------------------
 // PlanFor<L, MAXRAD>: radices of an L-point transform, none above MAXRAD.
@@ -201,15 +257,23 @@ __device__ __forceinline__ void stockham_stage(cplx<T>* s, const cplx<T>* __rest
 #pragma unroll
       for (int m = 0; m < RAD; ++m) v[p][m] = sr[pidx(j + m * NB)];
       if (NS > 1) {
+        // twiddles fused into the first butterfly layer
         const int jj = j % NS;
 #pragma unroll
-        for (int m = 1; m < RAD; ++m) {
-          C w = __ldg(tw + jj * m * (TWS * L / (NS * RAD)));
-          if (DIR > 0) w.y = -w.y;
-          v[p][m] = cmul(v[p][m], w);
+        for (int m = 0; m < RAD / 2; ++m) {
+          if (m > 0) {
+            C w = __ldg(tw + jj * m * (TWS * L / (NS * RAD)));
+            if (DIR > 0) w.y = -w.y;
+            v[p][m] = cmul(v[p][m], w);
+          }
+          C wb = __ldg(tw + jj * (m + RAD / 2) * (TWS * L / (NS * RAD)));
+          if (DIR > 0) wb.y = -wb.y;
+          bfly_tw(v[p][m], v[p][m + RAD / 2], wb);
         }
+        dft_tail<RAD, DIR>(v[p]);
+      } else {
+        dft<RAD, DIR>(v[p]);
       }
-      dft<RAD, DIR>(v[p]);
     }
   }
   __syncthreads();

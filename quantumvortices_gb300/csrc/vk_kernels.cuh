@@ -609,6 +609,68 @@ __global__ void __launch_bounds__(GeoX<T, L>::NT, GeoX<T, L>::MINB) k_x2(const c
                                                            reinterpret_cast<cplx<T>*>(smraw));
 }
 
+// Stage coefficients with the reference's evaluation order
+// (dt*oney6, dt*oney6*two, dt*half, dt) and the RHS constants.
+template <typename T> struct Rk4Coef { T c1, c2, pr, pi, al, omb; };
+template <typename T, int STAGE>
+__device__ __forceinline__ Rk4Coef<T> rk4_coef(const StepConsts& c) {
+  const double oney6 = 1.0 / 6.0;
+  Rk4Coef<T> q;
+  q.c2 = T((STAGE == 1 || STAGE == 4) ? c.dt * oney6 : c.dt * oney6 * 2.0);
+  q.c1 = T(STAGE == 3 ? c.dt : c.dt * 0.5);
+  q.pr = T(c.prefac_re);
+  q.pi = T(c.prefac_im);
+  q.al = T(c.alpha);
+  q.omb = T(c.omega) - T(c.g * c.rho_bg);
+  return q;
+}
+
+// One Fourier mode of an RK4 stage: rhs = prefac*((alpha k^2 - Omega) kpsi
+// + N^) on the 2/3 disk (src/gpe.f90:609-669; FRC adds :623-658), the stage
+// update of src/gpe.f90:366-489 (str1 / str2 written at gi); returns the new
+// kpsi, 0 off the disk.
+template <typename T, int STAGE, bool FRC>
+__device__ __forceinline__ cplx<T> rk4_mode(const StepConsts& c, const Rk4Coef<T>& q, int ksq, size_t gi, cplx<T> nh,
+                                            cplx<T> ps, cplx<T> s1v, cplx<T> s2v, cplx<T>* __restrict__ str1,
+                                            cplx<T>* __restrict__ str2, unsigned long long rctr) {
+  typedef cplx<T> C;
+  C nw = mkc<T>(T(0), T(0));
+  if (ksq <= c.k2max) {
+    const T kin = q.al * T(ksq) - q.omb;
+    const C t = mkc<T>(kin * ps.x + nh.x, kin * ps.y + nh.y);
+    C rhs = mkc<T>(q.pr * t.x - q.pi * t.y, q.pr * t.y + q.pi * t.x);
+    if (FRC) {  // src/gpe.f90:623-658, in the reference's order
+      const double kr2 = (double)ksq;
+      const double x2 = kr2 * kr2, x4 = x2 * x2, x8 = x4 * x4;  // kradius2**8
+      if (ksq != 0) {
+        const T a = T(c.vishypo * (1.0 / x8));
+        rhs = mkc<T>(rhs.x - a * ps.x, rhs.y - a * ps.y);
+      }
+      const T b = T(c.vishype * x8);
+      rhs = mkc<T>(rhs.x - b * ps.x, rhs.y - b * ps.y);
+      if (kr2 >= c.kf1sq && kr2 <= c.kf2sq) {
+        double sn, cs;
+        sincos(2.0 * 3.14159265358979323846 * vk_frc_uniform(c.seed, rctr, gi), &sn, &cs);
+        rhs = mkc<T>(rhs.x + T(c.famp * cs), rhs.y + T(c.famp * sn));
+      }
+    }
+    if (STAGE == 1) {
+      str1[gi] = ps;
+      str2[gi] = mkc<T>(q.c2 * rhs.x, q.c2 * rhs.y);
+      nw = mkc<T>(ps.x + q.c1 * rhs.x, ps.y + q.c1 * rhs.y);
+    } else {
+      const C s2 = mkc<T>(s2v.x + q.c2 * rhs.x, s2v.y + q.c2 * rhs.y);
+      if (STAGE < 4) {
+        str2[gi] = s2;
+        nw = mkc<T>(s1v.x + q.c1 * rhs.x, s1v.y + q.c1 * rhs.y);
+      } else {
+        nw = mkc<T>(s1v.x + s2.x, s1v.y + s2.y);
+      }
+    }
+  }
+  return nw;
+}
+
 // ------------------------------------------------------------------------
 // Y2 (RK4 stage STAGE = 1..4): rows |kx| <= K of Td: F_y -> N^ ->
 // rhs = prefac*((alpha k^2 - Omega) kpsi + N^), masked (src/gpe.f90:609-669)
@@ -632,13 +694,7 @@ __device__ __forceinline__ void y2_rk4_body(const cplx<T>* __restrict__ Td, cplx
   });
   __syncthreads();
   fft_rows<T, L, G::R, G::NT, -1>(s, tw);
-  // Stage coefficients with the reference's evaluation order:
-  // dt*oney6, dt*oney6*two, dt*half, dt.
-  const double oney6 = 1.0 / 6.0;
-  const T c2 = T((STAGE == 1 || STAGE == 4) ? c.dt * oney6 : c.dt * oney6 * 2.0);
-  const T c1 = T(STAGE == 3 ? c.dt : c.dt * 0.5);
-  const T pr = T(c.prefac_re), pi_ = T(c.prefac_im);
-  const T al = T(c.alpha), om = T(c.omega);
+  const Rk4Coef<T> q = rk4_coef<T, STAGE>(c);
   const unsigned long long rctr = FRC ? *c.rng_ctr : 0ull;
   // batches of B elements per thread: all loads of a batch before any use
   constexpr int PER = G::R * L / G::NT;
@@ -666,43 +722,9 @@ __device__ __forceinline__ void y2_rk4_body(const cplx<T>* __restrict__ Td, cplx
       if (l0 + r >= nrow) continue;
       const int kxi = pruned_row(l0 + r, K, nx);
       const int k1 = kwn(kxi, nx), k2 = kwn(ky, L);
-      const int ksq = k1 * k1 + k2 * k2;
       const size_t gi = (size_t)kxi * L + ky;
-      C nw = mkc<T>(T(0), T(0));
-      if (ksq <= c.k2max) {
-        const C nh = s[r * G::LP + pidx(ky)];
-        const T kin = al * T(ksq) - (om - T(c.g * c.rho_bg));
-        const C t = mkc<T>(kin * ps[j].x + nh.x, kin * ps[j].y + nh.y);
-        C rhs = mkc<T>(pr * t.x - pi_ * t.y, pr * t.y + pi_ * t.x);
-        if (FRC) {  // src/gpe.f90:623-658, in the reference's order
-          const double kr2 = (double)ksq;
-          const double x2 = kr2 * kr2, x4 = x2 * x2, x8 = x4 * x4;  // kradius2**8
-          if (ksq != 0) {
-            const T a = T(c.vishypo * (1.0 / x8));
-            rhs = mkc<T>(rhs.x - a * ps[j].x, rhs.y - a * ps[j].y);
-          }
-          const T b = T(c.vishype * x8);
-          rhs = mkc<T>(rhs.x - b * ps[j].x, rhs.y - b * ps[j].y);
-          if (kr2 >= c.kf1sq && kr2 <= c.kf2sq) {
-            double sn, cs;
-            sincos(2.0 * 3.14159265358979323846 * vk_frc_uniform(c.seed, rctr, gi), &sn, &cs);
-            rhs = mkc<T>(rhs.x + T(c.famp * cs), rhs.y + T(c.famp * sn));
-          }
-        }
-        if (STAGE == 1) {
-          str1[gi] = ps[j];
-          str2[gi] = mkc<T>(c2 * rhs.x, c2 * rhs.y);
-          nw = mkc<T>(ps[j].x + c1 * rhs.x, ps[j].y + c1 * rhs.y);
-        } else {
-          const C s2 = mkc<T>(s2v[j].x + c2 * rhs.x, s2v[j].y + c2 * rhs.y);
-          if (STAGE < 4) {
-            str2[gi] = s2;
-            nw = mkc<T>(s1v[j].x + c1 * rhs.x, s1v[j].y + c1 * rhs.y);
-          } else {
-            nw = mkc<T>(s1v[j].x + s2.x, s1v[j].y + s2.y);
-          }
-        }
-      }
+      const C nw = rk4_mode<T, STAGE, FRC>(c, q, k1 * k1 + k2 * k2, gi, s[r * G::LP + pidx(ky)], ps[j], s1v[j], s2v[j],
+                                           str1, str2, rctr);
       kpsi[gi] = nw;
       s[r * G::LP + pidx(ky)] = nw;
     }

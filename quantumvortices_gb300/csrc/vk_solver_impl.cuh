@@ -151,7 +151,9 @@ class Solver : public SolverBase {
     // the FP64 pipe of the busiest SM: 512 row-pair CTAs leave 4 pairs on
     // some SMs and 3 on others (135 us for k_x1 on GB300), while 1024
     // single-row CTAs, 608 resident and the rest taking the SMs that free
-    // first, even the rows out (119 us).  VK_XSPLIT=0 keeps the row pairs.
+    // first, even the rows out (119 us).  At 4096^2 the row pairs stay
+    // ahead (6.12e8 against 6.04e8 grid-pt-steps/s).  VK_XSPLIT=0 keeps the
+    // row pairs at 1024 too.
     c_.xsingle = 0;
     const char* xs_env = std::getenv("VK_XSPLIT");
     if (std::is_same<T, double>::value && nx_ == 1024 && !(xs_env && xs_env[0] == '0')) c_.xsingle = ny_;
