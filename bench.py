@@ -33,9 +33,10 @@ METRIC = "RK4 grid-pt-steps/s at 1024^2"
 UNIT = "grid-pt-steps/s"
 PEAKS_FILE = os.path.join(ROOT, "MEASURED_PEAKS.json")
 FALLBACK_HBM_GBS = 6800.0
-# k_x1<double,1024> DRAM bytes per launch from one ncu capture of this
-# workload (11.36 MB read, 0 written within the launch)
-X1_FP64_1024_DRAM_BYTES = 11361536 + 0
+# DRAM bytes per launch (dram__bytes_read.sum + dram__bytes_write.sum) of the
+# FP64 1024^2 x passes from one ncu capture of this workload
+# (profiles/k_x_fp64_1024_full.md)
+X_FP64_1024_DRAM_BYTES = {"k_x1": 11421184 + 0, "k_x2": 22499328 + 3072}
 
 
 def parse():
@@ -418,7 +419,7 @@ def run_ours(args, rank, world, local_rank):
         "roofline": {"bound": "hbm", "kernel": tag, "achieved": achieved, "peak": peak,
                      "peak_source": peak_kind, "unit": "GB/s",
                      "frac": achieved / peak if achieved else None,
-                     "traffic": X1_FP64_1024_DRAM_BYTES if (tag == "k_x1" and n == 1024) else None,
+                     "traffic": X_FP64_1024_DRAM_BYTES.get(tag) if n == 1024 else None,
                      "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum per launch, "
                                        "one capture of this workload at 1024^2",
                      "algorithmic_bytes_per_launch": nbytes, "launch_ms": per_launch_ms,
