@@ -196,6 +196,14 @@ def test_state_errors():
     with pytest.raises(vk.VkError, match="VK_E_NUMERIC"):
         s.set_psi(bad)
     s.close()
+    # a field large enough for the threaded scan: Inf in the last imaginary part
+    with vk.GPESolver(vk.params_for(1024)) as s:
+        big = np.ones((1024, 1024), complex)
+        big[-1, -1] = complex(1.0, np.inf)
+        with pytest.raises(vk.VkError, match="VK_E_NUMERIC"):
+            s.set_psi(big)
+        big[-1, -1] = 1.0
+        s.set_psi(big)
 
 
 def test_kernel_launch_count_and_timing():
