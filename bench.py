@@ -55,6 +55,19 @@ def parse():
     return ap.parse_args()
 
 
+def replica_throughput(ms_local, world, points, S, K, dist=None, device="cpu"):
+    """Whole-job throughput of `world` independent replicas: all ranks'
+    grid-point steps (points x S RK4 steps x K bench steps each) over the
+    slowest rank's time, the MAX over ranks of the per-rank milliseconds.
+    Returns (value, ms_max)."""
+    import torch
+    t = torch.tensor([float(ms_local)], dtype=torch.float64, device=device)
+    if dist is not None and world > 1:
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    ms_max = float(t.item())
+    return world * points * S * K / (ms_max * 1e-3), ms_max
+
+
 def workload(n, seed):
     from quantumvortices_gb300 import vk
     dx = 2 * math.pi / n
@@ -340,11 +353,7 @@ def run_ours(args, rank, world, local_rank):
     sampler.start()
     ms, launches = timed_loop(s, K, W)
     clocks = sampler.stop()
-    t = torch.tensor([ms], device="cuda", dtype=torch.float64)
-    if dist is not None:
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-    ms_max = float(t.item())
-    value = world * n * n * S * K / (ms_max * 1e-3)
+    value, ms_max = replica_throughput(ms, world, n * n, S, K, dist, "cuda")
 
     # per-kernel times (events around every launch, separate pass)
     s.timing_begin()
