@@ -10,6 +10,8 @@
 //   kernel_bodies_host x2 L ny single|pair +1|-1 DIR  Tc, psi -> Td
 //   kernel_bodies_host y1 L DIR                      Tb -> Tc        (L x L grid)
 //   kernel_bodies_host y2 L STAGE DIR                Td, kpsi, str1, str2 -> kpsi, str1, str2, Ta
+//   kernel_bodies_host y2a L DIR                     Td, kpsi -> kpsi, Ta, part (ARGLE, residual sums)
+//   kernel_bodies_host x2p L ny DIR                  Tc, psi, vpot -> Td (RK4 with a potential)
 #include <cuda_runtime.h>
 #include <cmath>
 #include <cstdio>
@@ -43,6 +45,19 @@ static std::vector<C> load(const char* name, size_t n) {
 static void save(const char* name, const std::vector<C>& v) {
   FILE* f = std::fopen((dir + "/" + name).c_str(), "wb");
   if (!f || std::fwrite(v.data(), sizeof(C), v.size(), f) != v.size()) { std::fprintf(stderr, "write %s\n", name); std::exit(2); }
+  std::fclose(f);
+}
+
+static std::vector<double> load_real(const char* name, size_t n) {
+  std::vector<double> v(n);
+  FILE* f = std::fopen((dir + "/" + name).c_str(), "rb");
+  if (!f || std::fread(v.data(), sizeof(double), n, f) != n) { std::fprintf(stderr, "read %s\n", name); std::exit(2); }
+  std::fclose(f);
+  return v;
+}
+static void save_real(const char* name, const std::vector<double>& v) {
+  FILE* f = std::fopen((dir + "/" + name).c_str(), "wb");
+  if (!f || std::fwrite(v.data(), sizeof(double), v.size(), f) != v.size()) { std::fprintf(stderr, "write %s\n", name); std::exit(2); }
   std::fclose(f);
 }
 
@@ -131,6 +146,24 @@ template <int L> static int run(int argc, char** argv) {
     save("str1.bin", s1);
     save("str2.bin", s2);
     save("Ta.bin", Ta);
+  } else if (pass == "y2a") {
+    const StepConsts c = consts(L, L);
+    const size_t n2 = (size_t)L * L;
+    std::vector<C> Td = load("Td.bin", n2), kpsi = load("kpsi.bin", n2), Ta(n2);
+    std::vector<double> part(3 * (size_t)L);
+    for (int t = 0; t < L; ++t)
+      y2_argle_body<double, L, G1<L, 1>, true>(Td.data(), kpsi.data(), Ta.data(), tw.data(), part.data(), c, t, s.data());
+    save("kpsi.bin", kpsi);
+    save("Ta.bin", Ta);
+    save_real("part.bin", part);
+  } else if (pass == "x2p") {
+    const int ny = std::atoi(argv[3]);
+    const StepConsts c = consts(L, ny);
+    std::vector<C> Tc = load("Tc.bin", (size_t)ny * c.pk), psi = load("psi.bin", (size_t)ny * L), Td((size_t)L * ny);
+    const std::vector<double> vpot = load_real("vpot.bin", (size_t)ny * L);
+    for (int t = 0; t < ny / 2; ++t)
+      x2_body<double, L, G1<L, 2>, +1, true, true>(Tc.data(), psi.data(), vpot.data(), Td.data(), tw.data(), c, t, s.data());
+    save("Td.bin", Td);
   } else {
     return 2;
   }

@@ -7,6 +7,10 @@ restatements of each pass:
   y1  Tb[kx][y] -> F_y, 2/3 disk mask, F^-1_y -> Tc[y][kx]
   y2  Td rows |kx| <= K -> F_y -> RK4 right-hand side and stage update (src/gpe.f90:366-489,
       609-669) -> kpsi, str1, str2, Ta[y][kx] = F^-1_y kpsi
+  y2a all rows of Td -> F_y -> the ARGLE update (src/gpe.f90:181-222)
+      kpsi <- (kpsi + dt (N^ + Omega kpsi)) / (1 + alpha k^2 dt), Ta = F^-1_y kpsi, and the
+      per-row sums |new - old|^2, |old|^2, |new|^2 of the residual
+  x2p the RK4 x2 pass with a potential: Td = F_x ((g p + V) psi)
 
 The x passes run both layouts the GPU uses: row pairs (two real rows per
 complex transform) and single rows (a half-length complex transform).
@@ -166,3 +170,43 @@ def test_y2_rk4(exe, tmp_path, stage):
     assert close(get(tmp_path, "str1.bin", (L, L))[rows], e1)
     assert close(get(tmp_path, "str2.bin", (L, L))[rows], e2)
     assert close(get(tmp_path, "Ta.bin", (L, L))[:, rows], ta)
+
+
+def test_y2_argle_with_residual_sums(exe, tmp_path):
+    L = 128
+    rng = np.random.default_rng(11)
+    Td, kpsi = rand(rng, (L, L)), rand(rng, (L, L))
+    put(tmp_path, "Td.bin", Td)
+    put(tmp_path, "kpsi.bin", kpsi)
+    run(exe, tmp_path, "y2a", L)
+    ksq = kwn(L)[:, None] ** 2 + kwn(L)[None, :] ** 2
+    nh = np.fft.fft(Td, axis=1)
+    new = (kpsi + DT * (nh + OMEGA * kpsi)) / (1.0 + ALPHA * ksq * DT)
+    assert close(get(tmp_path, "kpsi.bin", (L, L)), new)
+    assert close(get(tmp_path, "Ta.bin", (L, L)), (np.fft.ifft(new, axis=1) * L).T)
+    part = np.fromfile(os.path.join(tmp_path, "part.bin")).reshape(L, 3)
+    ref = np.stack([np.sum(np.abs(new - kpsi) ** 2, axis=1), np.sum(np.abs(kpsi) ** 2, axis=1),
+                    np.sum(np.abs(new) ** 2, axis=1)], axis=1)
+    assert np.abs(part - ref).max() <= 1e-12 * np.abs(ref).max()
+
+
+def test_x2_with_potential(exe, tmp_path):
+    L, ny = 128, 32
+    _, K, pk = consts(L)
+    rng = np.random.default_rng(13)
+    Tc = np.zeros((ny, pk), complex)
+    Tc[:, :K + 1] = rand(rng, (ny, K + 1))
+    Tc[:, 0] = Tc[:, 0].real
+    psi = rand(rng, (ny, L))
+    vpot = rng.random((ny, L))
+    put(tmp_path, "Tc.bin", Tc)
+    put(tmp_path, "psi.bin", psi)
+    vpot.tofile(os.path.join(tmp_path, "vpot.bin"))
+    run(exe, tmp_path, "x2p", L, ny)
+    full = np.zeros((ny, L), complex)
+    full[:, :K + 1] = Tc[:, :K + 1]
+    full[:, L - K:] = np.conj(Tc[:, 1:K + 1][:, ::-1])
+    p = np.fft.ifft(full, axis=1).real * L / (L * ny)
+    td = np.fft.fft((G * p + vpot) * psi, axis=1).T
+    rows = np.abs(kwn(L)) <= K
+    assert close(get(tmp_path, "Td.bin", (L, ny))[rows], td[rows])
