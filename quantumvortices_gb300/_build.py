@@ -16,7 +16,13 @@ OUT_DIR = os.path.join(PKG, "_build")
 LIB = os.path.join(PKG, "libvk.so")
 DRIVER = os.path.join(PKG, "vikshobha_gb300")
 
-CU_SRCS = ["vk_f64.cu", "vk_f32.cu", "vk_common.cu", "vk_noalloc.cu", "vk_ens.cu", "vk_nn.cu", "vk_sts.cu"]
+# (source, object tag, extra flags).  The solver is compiled once per precision
+# and row-length class, the ensemble once per precision: the compilations run
+# in parallel, and no single one dominates the build.
+CU_UNITS = ([("vk_solver_tu.cu", f"f{32 if fp32 else 64}.c{c}", [f"-DVK_TU_FP32={fp32}", f"-DVK_TU_CLASS={c}"])
+             for fp32 in (0, 1) for c in range(5)]
+            + [("vk_ens.cu", f"f{32 if fp32 else 64}", [f"-DVK_ENS_FP32={fp32}"]) for fp32 in (0, 1)]
+            + [(s, "", []) for s in ("vk_common.cu", "vk_noalloc.cu", "vk_nn.cu", "vk_sts.cu")])
 CPP_SRCS = ["vk_api.cpp", "vk_host.cpp"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC,-fopenmp",
@@ -52,18 +58,21 @@ def build(verbose: bool = False, jobs: int | None = None) -> str:
     nvcc = _nvcc()
     cxx = os.environ.get("CXX", "g++")
     cmds, objs = [], []
-    for s in CU_SRCS:
-        src, obj = os.path.join(CSRC, s), os.path.join(OUT_DIR, s + ".o")
+    for s, tag, extra in CU_UNITS:
+        src = os.path.join(CSRC, s)
+        obj = os.path.join(OUT_DIR, s + (f".{tag}" if tag else "") + ".o")
         objs.append(obj)
         if _stale(obj, src):
-            cmds.append([nvcc, *NVCC_FLAGS, "-c", src, "-o", obj])
+            cmds.append([nvcc, *NVCC_FLAGS, *extra, "-c", src, "-o", obj])
     for s in CPP_SRCS:
         src, obj = os.path.join(CSRC, s), os.path.join(OUT_DIR, s + ".o")
         objs.append(obj)
         if _stale(obj, src):
             cmds.append([cxx, *CXX_FLAGS, "-c", src, "-o", obj])
     if cmds:
-        with ThreadPoolExecutor(max_workers=jobs or min(8, len(cmds))) as ex:
+        # longest compilations first
+        cmds.sort(key=lambda c: (0 if "vk_solver_tu.cu" in " ".join(c) else 1))
+        with ThreadPoolExecutor(max_workers=jobs or min(os.cpu_count() or 8, len(cmds))) as ex:
             list(ex.map(_run, cmds))
     if cmds or not os.path.exists(LIB):
         _run([nvcc, *ARCH, "-shared", "-o", LIB, *objs, "-Xcompiler", "-fopenmp", "-lgomp"])

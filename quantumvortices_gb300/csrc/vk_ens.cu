@@ -1,4 +1,9 @@
-// vk_ens.cu -- ensemble (batched) stepper, both precisions, and its C ABI.
+// vk_ens.cu -- ensemble (batched) stepper and its C ABI.  Compiled twice:
+// -DVK_ENS_FP32=0 builds the FP64 ensemble and the C ABI, -DVK_ENS_FP32=1 the
+// FP32-bulk ensemble, so the two precisions compile in parallel.
+#ifndef VK_ENS_FP32
+#error "compile with -DVK_ENS_FP32=0|1"
+#endif
 #include <cstring>
 #include <string>
 #include "vk_ensemble.cuh"
@@ -38,10 +43,15 @@ template <typename T> EnsembleBase* make_ensemble(const vk_params* p, int n, int
   *status = VK_OK;
   return x;
 }
-EnsembleBase* make_ensemble_f64(const vk_params* p, int n, int* status) { return make_ensemble<double>(p, n, status); }
+#if VK_ENS_FP32
 EnsembleBase* make_ensemble_f32(const vk_params* p, int n, int* status) { return make_ensemble<float>(p, n, status); }
+#else
+EnsembleBase* make_ensemble_f64(const vk_params* p, int n, int* status) { return make_ensemble<double>(p, n, status); }
+#endif
 
 }  // namespace vk
+
+#if !VK_ENS_FP32
 
 using vk::set_error;
 
@@ -129,3 +139,4 @@ extern "C" int vk_ens_kernel_launches(void* ens, int64_t* count) {
   *count = c->e->launches();
   return VK_OK;
 }
+#endif  // !VK_ENS_FP32

@@ -63,6 +63,41 @@ int kmax_for(int k2max) {
   return k;
 }
 
+// Bit i of a mask: row length 16 << i.  Must match VK_LEN_MASK in vk_solver_tu.cu.
+static const int kLenClassMask[5] = {0x0f, 0x38, 0x70, 0xe0, 0x1c0};
+
+int solver_len_class(int nx, int ny) {
+  auto bit = [](int n) {
+    for (int i = 0; i < 9; ++i)
+      if (n == (16 << i)) return 1 << i;
+    return 0;
+  };
+  const int want = bit(nx) | bit(ny);
+  if (!bit(nx) || !bit(ny)) return -1;
+  for (int c = 0; c < 5; ++c)
+    if ((kLenClassMask[c] & want) == want) return c;
+  return -1;
+}
+
+typedef SolverBase* (*SolverFactory)(const vk_params&, int*);
+static const SolverFactory kF64[5] = {make_solver_f64_c0, make_solver_f64_c1, make_solver_f64_c2,
+                                      make_solver_f64_c3, make_solver_f64_c4};
+static const SolverFactory kF32[5] = {make_solver_f32_c0, make_solver_f32_c1, make_solver_f32_c2,
+                                      make_solver_f32_c3, make_solver_f32_c4};
+
+static SolverBase* make_solver_in_class(const SolverFactory* table, const vk_params& p, int* status) {
+  const int c = solver_len_class(p.nx, p.ny);
+  if (c < 0) {
+    set_error("vk_init: no row-length class holds both nx and ny (classes {16..128}, {128..512}, {256..1024}, "
+              "{512..2048}, {1024..4096})");
+    *status = VK_E_INVALID;
+    return nullptr;
+  }
+  return table[c](p, status);
+}
+SolverBase* make_solver_f64(const vk_params& p, int* status) { return make_solver_in_class(kF64, p, status); }
+SolverBase* make_solver_f32(const vk_params& p, int* status) { return make_solver_in_class(kF32, p, status); }
+
 }  // namespace vk
 
 using vk::set_error;

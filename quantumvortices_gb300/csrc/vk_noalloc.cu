@@ -37,20 +37,26 @@ struct DeviceSlots {
   double2* tw = nullptr;       // device address of g_noalloc_tw
 };
 
+// One slot per device ordinal, in a fixed array: a slot never moves, and the
+// caller gets a copy of its pointers taken under the lock.
+constexpr int kMaxDevices = 64;
 std::mutex g_mu;
-std::vector<DeviceSlots> g_slots;
+DeviceSlots g_slots[kMaxDevices];
 
 // Once per device, with that device current: resolve the arrays' device
 // addresses (the names are host stand-ins in host code) and fill the tables.
-int setup_current_device(DeviceSlots** out) {
+int setup_current_device(DeviceSlots* out) {
   int dev = -1;
   cudaError_t e = cudaGetDevice(&dev);
   if (e != cudaSuccess) {
     set_error(std::string("vk_fft2d_forward_noalloc: cudaGetDevice: ") + cudaGetErrorString(e));
     return VK_E_CUDA;
   }
+  if (dev < 0 || dev >= kMaxDevices) {
+    set_error("vk_fft2d_forward_noalloc: device ordinal beyond the 64 slots of the built-in tables");
+    return VK_E_INVALID;
+  }
   std::lock_guard<std::mutex> g(g_mu);
-  if ((int)g_slots.size() <= dev) g_slots.resize(dev + 1);
   DeviceSlots& s = g_slots[dev];
   if (!s.ready) {
     void* p = nullptr;
@@ -59,13 +65,13 @@ int setup_current_device(DeviceSlots** out) {
       set_error(std::string("vk_fft2d_forward_noalloc: cudaGetSymbolAddress(scratch): ") + cudaGetErrorString(e));
       return VK_E_CUDA;
     }
-    s.scratch = static_cast<double2*>(p);
+    double2* scratch = static_cast<double2*>(p);
     e = cudaGetSymbolAddress(&p, g_noalloc_tw);
     if (e != cudaSuccess) {
       set_error(std::string("vk_fft2d_forward_noalloc: cudaGetSymbolAddress(twiddles): ") + cudaGetErrorString(e));
       return VK_E_CUDA;
     }
-    s.tw = static_cast<double2*>(p);
+    double2* tw = static_cast<double2*>(p);
     std::vector<double> host(2 * (size_t)VK_NOALLOC_TW_TOTAL);
     for (int L = 16; L <= VK_NOALLOC_MAX_LEN; L *= 2) twiddle_table(L, host.data() + 2 * (size_t)(L - 16));
     e = cudaMemcpyToSymbol(g_noalloc_tw, host.data(), sizeof(double2) * VK_NOALLOC_TW_TOTAL);
@@ -73,9 +79,35 @@ int setup_current_device(DeviceSlots** out) {
       set_error(std::string("vk_fft2d_forward_noalloc: cudaMemcpyToSymbol(twiddles): ") + cudaGetErrorString(e));
       return VK_E_CUDA;
     }
+    s.scratch = scratch;
+    s.tw = tw;
     s.ready = true;
   }
-  *out = &s;
+  *out = s;
+  return VK_OK;
+}
+
+// Launches kern through cudaLaunchKernel, whose return code belongs to this
+// launch alone (an error left behind by earlier work of the caller is neither
+// reported nor cleared here).
+template <typename... A>
+int launch_checked(const char* what, void (*kern)(A...), int grid, int block, size_t smem, cudaStream_t st,
+                   A... args) {
+  if (smem > 48 * 1024) {
+    const cudaError_t e =
+        cudaFuncSetAttribute((const void*)kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) {
+      set_error(std::string("vk_fft2d_forward_noalloc: shared-memory attribute of ") + what + ": " +
+                cudaGetErrorString(e));
+      return VK_E_CUDA;
+    }
+  }
+  void* argv[] = {(void*)&args...};
+  const cudaError_t e = cudaLaunchKernel((const void*)kern, dim3(grid), dim3(block), argv, smem, st);
+  if (e != cudaSuccess) {
+    set_error(std::string("vk_fft2d_forward_noalloc: launch of ") + what + ": " + cudaGetErrorString(e));
+    return VK_E_CUDA;
+  }
   return VK_OK;
 }
 
@@ -115,34 +147,27 @@ extern "C" int vk_fft2d_forward_noalloc(const double* psi_dev, double* kpsi_dev,
     set_error("vk_fft2d_forward_noalloc: nx*ny exceeds the built-in scratch of 262144 complex points (4 MiB)");
     return VK_E_INVALID;
   }
-  DeviceSlots* slots = nullptr;
+  DeviceSlots slots;
   int rc = setup_current_device(&slots);
   if (rc) return rc;
   cudaStream_t st = static_cast<cudaStream_t>(stream);
   const double2* in = reinterpret_cast<const double2*>(psi_dev);
   double2* out = reinterpret_cast<double2*>(kpsi_dev);
-  double2* scratch = slots->scratch;
-  const double2* twx = slots->tw + (nx - 16);
-  const double2* twy = slots->tw + (ny - 16);
+  double2* scratch = slots.scratch;
+  const double2* twx = slots.tw + (nx - 16);
+  const double2* twy = slots.tw + (ny - 16);
   with_len_na(nx, [&](auto lc) {
     constexpr int L = decltype(lc)::value;
     typedef GeoX<double, L> G;
-    const size_t sm = sizeof(double2) * G::R * G::LP;
-    if (sm > 48 * 1024) cudaFuncSetAttribute(k_xfwd<double, L>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
-    k_xfwd<double, L><<<ny / G::R, G::NT, sm, st>>>(in, scratch, twx, ny);
+    rc = launch_checked("the x pass", k_xfwd<double, L>, ny / G::R, G::NT, sizeof(double2) * G::R * G::LP, st, in,
+                        scratch, twx, (int)ny);
   });
+  if (rc) return rc;
   with_len_na(ny, [&](auto lc) {
     constexpr int L = decltype(lc)::value;
     typedef GeoY<double, L> G;
-    const size_t sm = sizeof(double2) * G::R * G::LP;
-    if (sm > 48 * 1024)
-      cudaFuncSetAttribute(k_yfwd<double, L, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
-    k_yfwd<double, L, false><<<nx / G::R, G::NT, sm, st>>>(scratch, out, twy, nx, 0, 0.0, 0.0);
+    rc = launch_checked("the y pass", k_yfwd<double, L, false>, nx / G::R, G::NT, sizeof(double2) * G::R * G::LP,
+                        st, (const double2*)scratch, out, twy, (int)nx, 0, 0.0, 0.0);
   });
-  cudaError_t e = cudaGetLastError();
-  if (e != cudaSuccess) {
-    set_error(std::string("vk_fft2d_forward_noalloc: launch: ") + cudaGetErrorString(e));
-    return VK_E_CUDA;
-  }
-  return VK_OK;
+  return rc;
 }

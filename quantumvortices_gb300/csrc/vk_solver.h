@@ -44,9 +44,25 @@ class SolverBase {
   virtual void mark_rk4_done() = 0;
 };
 
-// Factories (one per precision, each in its own translation unit).
+// Factories (one per precision).  They pick the compilation of Solver<T>
+// whose row-length set holds both nx and ny (solver_len_class) and fail with
+// VK_E_INVALID when none does.
 SolverBase* make_solver_f64(const vk_params& p, int* status);
 SolverBase* make_solver_f32(const vk_params& p, int* status);
+// Row-length class of an nx x ny grid: the first of the sets {16, 32, 64, 128},
+// {128, 256, 512}, {256, 512, 1024}, {512, 1024, 2048}, {1024, 2048, 4096}
+// holding both lengths, or -1.  Every grid with nx, ny <= 128 or with
+// max/min <= 4 has one.
+int solver_len_class(int nx, int ny);
+#define VK_DECLARE_SOLVER_CLASS(k)                                   \
+  SolverBase* make_solver_f64_c##k(const vk_params& p, int* status); \
+  SolverBase* make_solver_f32_c##k(const vk_params& p, int* status);
+VK_DECLARE_SOLVER_CLASS(0)
+VK_DECLARE_SOLVER_CLASS(1)
+VK_DECLARE_SOLVER_CLASS(2)
+VK_DECLARE_SOLVER_CLASS(3)
+VK_DECLARE_SOLVER_CLASS(4)
+#undef VK_DECLARE_SOLVER_CLASS
 
 // Ensembles of independent fields stepped by batched persistent kernels.
 class EnsembleBase {

@@ -1,6 +1,18 @@
 // vk_solver_impl.cuh -- Solver<T>: device state and launch sequences.
-// Included once per precision (vk_f64.cu, vk_f32.cu).
+//
+// Included by vk_solver_tu.cu, which is compiled once per (precision, row-length
+// class).  Each compilation defines VK_LEN_MASK (bit i set: row length 16 << i
+// is instantiated) and VK_SOLVER_NS, a distinct inline namespace that keeps
+// every compilation's Solver, with_len and host helpers apart at link time.
+// The kernels each one instantiates are those of its own lengths, so the
+// classes compile in parallel.
 #pragma once
+#ifndef VK_LEN_MASK
+#define VK_LEN_MASK 511
+#endif
+#ifndef VK_SOLVER_NS
+#error "VK_SOLVER_NS must name this compilation's inline namespace"
+#endif
 #include <cuda_runtime.h>
 #include <cmath>
 #include <cstdlib>
@@ -16,6 +28,7 @@
 #include "vk_solver.h"
 
 namespace vk {
+inline namespace VK_SOLVER_NS {
 
 #define VK_CUDA_TRY(expr)                                                              \
   do {                                                                                 \
@@ -28,18 +41,18 @@ namespace vk {
 
 template <int L> using LC = std::integral_constant<int, L>;
 
-// Calls f(LC<n>()) for a supported row length n.
+// Calls f(LC<n>()) for a row length n of this compilation's class.
 template <typename F> bool with_len(int n, F&& f) {
   switch (n) {
-    case 16: f(LC<16>()); return true;
-    case 32: f(LC<32>()); return true;
-    case 64: f(LC<64>()); return true;
-    case 128: f(LC<128>()); return true;
-    case 256: f(LC<256>()); return true;
-    case 512: f(LC<512>()); return true;
-    case 1024: f(LC<1024>()); return true;
-    case 2048: f(LC<2048>()); return true;
-    case 4096: f(LC<4096>()); return true;
+    case 16: if constexpr ((VK_LEN_MASK >> 0) & 1) { f(LC<16>()); return true; } else { return false; }
+    case 32: if constexpr ((VK_LEN_MASK >> 1) & 1) { f(LC<32>()); return true; } else { return false; }
+    case 64: if constexpr ((VK_LEN_MASK >> 2) & 1) { f(LC<64>()); return true; } else { return false; }
+    case 128: if constexpr ((VK_LEN_MASK >> 3) & 1) { f(LC<128>()); return true; } else { return false; }
+    case 256: if constexpr ((VK_LEN_MASK >> 4) & 1) { f(LC<256>()); return true; } else { return false; }
+    case 512: if constexpr ((VK_LEN_MASK >> 5) & 1) { f(LC<512>()); return true; } else { return false; }
+    case 1024: if constexpr ((VK_LEN_MASK >> 6) & 1) { f(LC<1024>()); return true; } else { return false; }
+    case 2048: if constexpr ((VK_LEN_MASK >> 7) & 1) { f(LC<2048>()); return true; } else { return false; }
+    case 4096: if constexpr ((VK_LEN_MASK >> 8) & 1) { f(LC<4096>()); return true; } else { return false; }
     default: return false;
   }
 }
@@ -998,4 +1011,5 @@ class Solver : public SolverBase {
   Diagnostics<T> diag_;
 };
 
+}  // namespace VK_SOLVER_NS
 }  // namespace vk

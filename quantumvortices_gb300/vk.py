@@ -167,6 +167,17 @@ def _dptr(a: np.ndarray):
     return a.ctypes.data_as(C.POINTER(C.c_double))
 
 
+def solver_len_class(nx: int, ny: int) -> int:
+    """Row-length class of an nx x ny grid (vk::solver_len_class): the first of
+    the sets {16..128}, {128..512}, {256..1024}, {512..2048}, {1024..4096}
+    (powers of two) holding both lengths, or -1 (vk_init rejects such grids)."""
+    sets = [(16, 128), (128, 512), (256, 1024), (512, 2048), (1024, 4096)]
+    for c, (lo, hi) in enumerate(sets):
+        if lo <= nx <= hi and lo <= ny <= hi:
+            return c
+    return -1
+
+
 def nshell(nx: int) -> int:
     """nshell = int(1.414*Nx/2.0d0)+1 (src/mod_grid.f90:77)."""
     return int(load_library().vk_nshell(nx))

@@ -266,7 +266,7 @@ def test_async_dump_is_the_field_at_the_dump_point(prec):
 
 
 def test_rk4_parity_fp64_2048():
-    """2048^2 (radix plan 16-16-8, two rows per x-pass CTA): two RK4 steps
+    """2048^2 (radix plan 16-16-8, two rows per x-pass CTA): ten RK4 steps
     against the oracle, relative L2 <= 1e-12."""
     import os
     n = 2048
@@ -274,9 +274,9 @@ def test_rk4_parity_fp64_2048():
     psi0, _ = vk.ic_vortices(n, n, 16, seed=4)
     with vk.GPESolver(p) as s:
         s.set_psi(psi0)
-        s.gpe_rk4(2)
+        s.gpe_rk4(10)
         got = s.get_psi()
     o = Oracle.from_vk_params(p, threads=os.cpu_count())
     o.set_psi(psi0, otoc=True, k_otoc=p.k_otoc_gp, eps_otoc=p.eps_otoc_gp)
-    o.gpe_rk4(2)
+    o.gpe_rk4(10)
     assert rel(got, o.get_psi()) < 1e-12

@@ -128,6 +128,18 @@ def test_init_rejects_bad_parameters():
     p.precision = 7
     with pytest.raises(vk.VkError, match="VK_E_INVALID"):
         vk.GPESolver(p)
+    # grids whose rows fall in different length classes are rejected before
+    # any device work
+    p = vk.params_for(64, 2048)
+    with pytest.raises(vk.VkError, match="row-length class"):
+        vk.GPESolver(p)
+
+
+def test_solver_len_classes():
+    assert vk.solver_len_class(16, 128) == 0 and vk.solver_len_class(128, 64) == 0
+    assert [vk.solver_len_class(n, n) for n in (256, 512, 1024, 2048, 4096)] == [1, 1, 2, 3, 4]
+    assert vk.solver_len_class(1024, 256) == 2 and vk.solver_len_class(4096, 1024) == 4
+    assert vk.solver_len_class(64, 256) == -1 and vk.solver_len_class(16, 4096) == -1
 
 
 def test_ic_vortices_periodic_and_seeded():

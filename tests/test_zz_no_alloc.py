@@ -4,9 +4,12 @@ It exists for callers that cannot call cudaMalloc, e.g. a Fortran code whose
 device arrays belong to an OpenACC / OpenMP-offload runtime: they pass device
 pointers and the library uses a built-in device array as scratch.  The test
 calls it through the C ABI twice in a row on different inputs and checks each
-result against the allocating path (vk_set_psi + vk_get_kpsi of a FP64
-context), within the FFT tolerance used by the other GPU tests (1e-13
-relative).  This file is named to be collected last.
+result against an independent transform, numpy.fft.fft2 transposed to the
+Fourier layout kpsi[kx][ky], within the FFT tolerance of the other GPU tests
+(1e-13 relative), and against the allocating entry point (vk_set_psi +
+vk_get_kpsi).  The shapes include rows of 2048 and 4096 points, whose passes
+need more than 48 KB of shared memory.  This file is named to be collected
+last.
 """
 import ctypes as C
 
@@ -17,6 +20,10 @@ from quantumvortices_gb300 import vk
 
 pytestmark = pytest.mark.gpu
 
+# (nx, ny); the last three reach the built-in limit of 262144 points and need
+# the raised shared-memory limit (x rows of 2048 and 4096, y rows of 4096).
+SHAPES = [(64, 64), (512, 512), (128, 32), (2048, 128), (4096, 64), (64, 4096)]
+
 
 def _noalloc_fn():
     lib = vk.load_library()
@@ -26,7 +33,7 @@ def _noalloc_fn():
     return f
 
 
-def _reference_kpsi(psi):
+def _allocating_kpsi(psi):
     ny, nx = psi.shape
     p = vk.params_for(nx, ny, otoc=False)
     with vk.GPESolver(p) as s:
@@ -34,8 +41,8 @@ def _reference_kpsi(psi):
         return s.get_kpsi()
 
 
-@pytest.mark.parametrize("nx,ny", [(64, 64), (512, 512), (128, 32)])
-def test_noalloc_forward_fft_matches_allocating_path(nx, ny):
+@pytest.mark.parametrize("nx,ny", SHAPES)
+def test_noalloc_forward_fft_matches_numpy(nx, ny):
     torch = pytest.importorskip("torch")
     f = _noalloc_fn()
     rng = np.random.default_rng(nx + 3 * ny)
@@ -48,9 +55,12 @@ def test_noalloc_forward_fft_matches_allocating_path(nx, ny):
         assert rc == 0, vk.load_library().vk_last_error()
         stream.synchronize()
         got = d_out.cpu().numpy().view(np.complex128).reshape(nx, ny)
-        want = _reference_kpsi(psi)
+        want = np.fft.fft2(psi).T  # kpsi[kx][ky], unnormalised forward (sign -1)
         err = np.linalg.norm(got - want) / np.linalg.norm(want)
         assert err < 1e-13, (call, err)
+        if vk.solver_len_class(nx, ny) >= 0:
+            alloc = _allocating_kpsi(psi)
+            assert np.linalg.norm(got - alloc) / np.linalg.norm(alloc) < 1e-13
 
 
 def test_noalloc_rejects_sizes_beyond_scratch():
