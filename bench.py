@@ -34,9 +34,9 @@ UNIT = "grid-pt-steps/s"
 PEAKS_FILE = os.path.join(ROOT, "MEASURED_PEAKS.json")
 FALLBACK_HBM_GBS = 6800.0
 # DRAM bytes per launch (dram__bytes_read.sum + dram__bytes_write.sum) of the
-# FP64 1024^2 x passes from one ncu capture of this workload
-# (profiles/k_x_fp64_1024_full.md)
-X_FP64_1024_DRAM_BYTES = {"k_x1": 11421184 + 0, "k_x2": 22499328 + 3072}
+# FP64 1024^2 passes, recorded from one earlier ncu capture of this workload
+# (not measured by this script: ncu is not run here)
+RECORDED_DRAM_BYTES_1024_FP64 = {"k_x1": 11421184 + 0, "k_x2": 22499328 + 3072}
 
 
 def parse():
@@ -52,6 +52,8 @@ def parse():
     ap.add_argument("--no-ensemble", action="store_true")
     ap.add_argument("--no-4096", action="store_true")
     ap.add_argument("--no-argle", action="store_true")
+    ap.add_argument("--no-particles", action="store_true")
+    ap.add_argument("--no-warmstart", action="store_true")
     return ap.parse_args()
 
 
@@ -264,6 +266,132 @@ def argle_bench(torch, n, psi0):
     return out
 
 
+def particles_bench(torch, K, W, S, flush):
+    """1024^2 FP64 with 16 Gaussian particles (V0 = 10, d = 2 xi,
+    M = 5 pi d^2, positions uniform, velocities N(0, 0.1^2), 64 vortices,
+    dt = 5e-4): RK4 throughput with the particle forces and the particle RK4
+    in every stage, the per-kernel split (the Parseval force pass is
+    k_y1_pot), and one diagnostics call with the particle energies."""
+    from quantumvortices_gb300 import vk
+    n, P = 1024, 16
+    dx = 2 * math.pi / n
+    d = 2.0 * math.sqrt(2.0) * dx
+    p = vk.params_for(n, dt=5e-4, n_particles=P, ppotd=2.0, ppotv0=10.0, gp_mass_part=5.0 * math.pi * d * d)
+    psi0 = workload(n, seed=3)
+    rng = np.random.default_rng(3)
+    s = vk.GPESolver(p)
+    s.set_psi(psi0)
+    s.particles_set(rng.uniform(0, 2 * math.pi, (P, 2)), rng.normal(0, 0.1, (P, 2)), np.zeros((P, 2)))
+    ext = torch.cuda.ExternalStream(s.stream)
+    for _ in range(W):
+        s.gpe_rk4(S)
+    torch.cuda.synchronize()
+    ms = 0.0
+    l0 = s.launches
+    for _ in range(K):
+        with torch.cuda.stream(ext):
+            flush.zero_()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(ext)
+        s.gpe_rk4(S)
+        e1.record(ext)
+        torch.cuda.synchronize()
+        ms += e0.elapsed_time(e1)
+    launches = s.launches - l0
+    s.timing_begin()
+    s.gpe_rk4(S)
+    per = s.timing_end()
+    diag = diagnostics_ms(s)
+    pos, vel, frc = s.particles_get()
+    s.close()
+    step_ms = ms / (K * S)
+    force_ms = per.get("k_y1_pot", (0.0, 1))[0] / S
+    return {"value": n * n * S * K / (ms * 1e-3), "unit": UNIT, "workload": "1024^2 FP64 + 16 Gaussian particles, "
+            "V0=10, d=2xi, M=5 pi d^2, 64 vortices, dt=5e-4", "ms_per_rk4_step": step_ms,
+            "gpu_launches": launches,
+            "force_pass": {"kernel": "k_y1_pot (y transform of rho, dealias, all 16 forces by Parseval, V_tot)",
+                           "ms_per_rk4_step": force_ms, "frac_of_step": force_ms / step_ms},
+            "kernel_ms": {k: round(v[0] / v[1], 5) for k, v in per.items()},
+            "diagnostics_ms": diag, "finite": bool(np.isfinite(pos).all() and np.isfinite(frc).all())}
+
+
+def diagnostics_ms(s, reps=5):
+    """Wall time of one vk_diagnostics call (energies, momentum, norm, the six
+    shell spectra, vortex count, particle energies; results copied to the
+    host), the median of `reps` calls after one untimed call."""
+    s.diagnostics_gpe()
+    ts = []
+    for _ in range(reps):
+        t0 = time.perf_counter()
+        s.diagnostics_gpe()
+        ts.append(time.perf_counter() - t0)
+    return 1e3 * statistics.median(ts)
+
+
+def argle_time_to_residual(torch, n, psi0):
+    """ARGLE wall time (FP64, dt = 1e-3) to a stated residual, checked every
+    `chunk` steps (the checks are inside the time):
+      * vortex_state: the 64-vortex workload to the residual plain ARGLE has
+        after the configured 2000 steps (vortex states never reach 1e-8:
+        vortices drift and annihilate while the residual stays near 1e-1);
+      * vortex_free: a real density-perturbed state, 1 + 0.3 sum of 12 random
+        low-k cosines, to 1e-8 (it relaxes to the uniform ground state)."""
+    from quantumvortices_gb300 import vk
+    out = {"residual_definition": "||kpsi_new - kpsi_old||_2 / (dt ||kpsi_old||_2), FP64"}
+    p = vk.params_for(n, dt=1e-3)
+    rng = np.random.default_rng(5)
+    x = np.arange(n) * 2 * math.pi / n
+    X, Y = np.meshgrid(x, x)
+    pert = np.zeros((n, n))
+    for _ in range(12):
+        kx, ky = rng.integers(0, 5, 2)
+        pert += math.cos(rng.uniform(0, 2 * math.pi)) * np.cos(kx * X + ky * Y + rng.uniform(0, 2 * math.pi))
+    free = (1.0 + 0.3 * pert / np.abs(pert).max()).astype(np.complex128)
+    with vk.GPESolver(p) as s:
+        s.set_psi(psi0)
+        target = s.argle(2000)
+        for name, start, tgt, chunk, cap in (("vortex_state", psi0, target, 50, 4000),
+                                             ("vortex_free", free, 1e-8, 10, 20000)):
+            s.set_psi(start)
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            steps, r = 0, float("inf")
+            while steps < cap:
+                r = s.argle(chunk)
+                steps += chunk
+                if r <= tgt:
+                    break
+            t = time.perf_counter() - t0
+            out[name] = {"target_residual": tgt, "reached": bool(r <= tgt), "residual": r, "steps": steps,
+                         "time_to_residual_s": t}
+    return out
+
+
+def warmstart_bench(n=512, n_train=256, epochs=3, n_eval=8):
+    """The learned ARGLE warm start trained in this process at a reduced size
+    (n_train solver-generated 512^2 states, 8-128 vortices, 1000 FP32 ARGLE
+    steps each) and evaluated on n_eval held-out seeds disjoint from the
+    training seeds: ARGLE iterations saved and wall-time ratio to the residual
+    plain ARGLE reaches after 1000 steps, and the ARGLE functional E - Omega N
+    after equal steps."""
+    from quantumvortices_gb300 import warmstart as ws
+    gen = ws.DataGen(n, 1000)
+    net = ws.WarmStartNet(n, n, 32, 4, seed=1)
+    try:
+        tr = ws.train(net, gen, n_train, epochs, 1e-3, log=lambda *a: None)
+        rows = ws.evaluate(net, gen, list(range(900_000, 900_000 + n_eval)), log=lambda *a: None)
+        summ = ws.summarize(rows)
+    finally:
+        net.close()
+        gen.close()
+    return {"grid": n, "training_states": n_train, "epochs": epochs, "held_out_seeds": n_eval,
+            "reduced_from": "20000 training states / 1000 held-out seeds",
+            "generation_s": tr["gen_s"], "train_s": tr["train_s"], "train_tflops": tr["tensor_tflops"],
+            **{k: summ[k] for k in ("iterations_saved_frac", "time_ratio_warm_over_plain", "time_ratio_median",
+                                     "reached_frac", "rel_grand_diff_same_steps_mean", "grand_lower_frac",
+                                     "rel_energy_diff_same_steps_mean")}}
+
+
 def grid4096_bench(torch, steps=5):
     """One 4096^2 field with 1024 seeded vortices: FP64 and FP32 throughput
     and the FP32-vs-FP64 psi error after 100 RK4 steps."""
@@ -372,6 +500,7 @@ def run_ours(args, rank, world, local_rank):
         if i > 0:
             e2e_times.append(time.perf_counter() - t0)
     e2e_t = statistics.median(e2e_times)
+    diag_ms = diagnostics_ms(s)
     s.close()
 
     # FP32 bulk path: throughput and error against the FP64 path after S steps
@@ -403,6 +532,10 @@ def run_ours(args, rank, world, local_rank):
     ens = None if args.no_ensemble else ensemble_bench(torch, K, W, S)
     g4096 = None if args.no_4096 else grid4096_bench(torch)
     argle = None if args.no_argle else argle_bench(torch, n, psi0)
+    if argle is not None:
+        argle["time_to_residual"] = argle_time_to_residual(torch, n, psi0)
+    parts = None if args.no_particles else particles_bench(torch, K, W, S, flush)
+    warm = None if args.no_warmstart else warmstart_bench()
     if rank != 0:
         return
     dgemm_tf = fp64_peak_tflops(torch)
@@ -426,20 +559,25 @@ def run_ours(args, rank, world, local_rank):
                    "rk4_steps_per_step": S, "parallelism": "replicas" if world > 1 else "single",
                    "l2": "flushed between timed steps (512 MiB write)"},
         "clocks": clocks, "gpu_launches": launches,
-        "roofline": {"bound": "hbm", "kernel": tag, "achieved": achieved, "peak": peak,
-                     "peak_source": peak_kind, "unit": "GB/s",
-                     "frac": achieved / peak if achieved else None,
-                     "traffic": X_FP64_1024_DRAM_BYTES.get(tag) if n == 1024 else None,
-                     "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum per launch, "
-                                       "one capture of this workload at 1024^2",
-                     "algorithmic_bytes_per_launch": nbytes, "launch_ms": per_launch_ms,
-                     "step_canonical_gbs": canonical, "step_canonical_frac": canonical / peak,
-                     "binding": "fp64 pipe (the fields of a 1024^2 step stay in L2)",
-                     "fp64": {"achieved": f64_tf, "peak": dgemm_tf, "unit": "TFLOP/s",
-                              "frac": f64_tf / dgemm_tf if f64_tf else None,
-                              "flops_per_launch": flops,
-                              "peak_source": "cuBLAS DGEMM 4096^3 measured in this run",
-                              "flop_model": "5 L log2 L per L-point complex FFT"}},
+        "roofline": {"bound": "fp64", "kernel": tag,
+                     "achieved": f64_tf, "peak": dgemm_tf, "unit": "TFLOP/s",
+                     "frac": f64_tf / dgemm_tf if f64_tf else None,
+                     "peak_source": "cuBLAS DGEMM 4096^3 measured in this run (no FP64 peak is recorded for "
+                                    "this GPU); the 1024^2 fields of a step stay in L2, and the passes are "
+                                    "bound by the FP64 pipe",
+                     "flops_per_launch": flops, "flop_model": "5 L log2 L per L-point complex FFT",
+                     "launch_ms": per_launch_ms,
+                     "traffic": RECORDED_DRAM_BYTES_1024_FP64.get(tag) if n == 1024 else None,
+                     "traffic_source": "recorded ncu capture (dram__bytes_read.sum + dram__bytes_write.sum per "
+                                       "launch of this kernel at 1024^2), not measured in this run",
+                     "hbm": {"achieved": achieved, "peak": peak, "peak_source": peak_kind, "unit": "GB/s",
+                             "frac": achieved / peak if achieved else None,
+                             "algorithmic_bytes_per_launch": nbytes,
+                             "step_canonical_gbs": canonical, "step_canonical_frac": canonical / peak}},
+        "diagnostics": {"ms_per_call": diag_ms, "grid": n,
+                        "frac_of_rk4_at_cadence_200": diag_ms / (200.0 * step_ms),
+                        "what": "one vk_diagnostics call: energies, momentum, norm, six shell spectra, vortex "
+                                "count, results copied to the host"},
         "kernel_ms": {k: round(v[0] / v[1], 5) for k, v in per.items()},
         "e2e": {"value": n * n * S / e2e_t, "unit": UNIT, "h2d_bytes_per_step": n * n * 16,
                 "d2h_bytes_per_step": n * n * 16},
@@ -447,6 +585,8 @@ def run_ours(args, rank, world, local_rank):
         "ensemble": ens,
         "grid_4096": g4096,
         "argle": argle,
+        "particles": parts,
+        "warmstart": warm,
     }
     out["cpu_baseline"] = cpu_baseline(n, psi0, args.cpu_seconds)
     print(json.dumps(out))
@@ -474,33 +614,36 @@ def cpu_baseline(n, psi0, seconds):
 # ----------------------------------------------------- reference arm --
 
 def run_reference(args, rank):
+    """The CPU FP64 restatement of src/gpe.f90 on all host cores.  Parameters
+    and the seeded state come from the oracle itself (oracle.derived_params,
+    oracle.ic_vortices): this arm loads no product library."""
     if rank != 0:
         return
-    from quantumvortices_gb300 import vk
-    from oracle.oracle import Oracle
+    from oracle import oracle as orc
     n = args.n
     cores = os.cpu_count() or 1
-    p = vk.params_for(n, dt=5e-4)
-    psi0 = workload(n, seed=1)
-    o = Oracle.from_vk_params(p, threads=cores)
+    psi0, _ = orc.ic_vortices(n, n, 64, seed=1, min_sep=4 * math.sqrt(2) * 2 * math.pi / n)
+    o = orc.Oracle(**orc.derived_params(n, dt=5e-4), threads=cores)
     o.set_psi(psi0)
+    S = args.substeps  # RK4 steps per bench step, as in the GPU arm
     for _ in range(args.warmup):
-        o.gpe_rk4(1)
+        o.gpe_rk4(S)
     times = []
     for _ in range(args.steps):
         t0 = time.perf_counter()
-        o.gpe_rk4(1)
+        o.gpe_rk4(S)
         times.append(time.perf_counter() - t0)
     tot = sum(times)
-    value = n * n * args.steps / tot
+    value = n * n * S * args.steps / tot
     out = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * tot / args.steps,
            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
            "data": "synthetic (seeded 64-vortex state)",
            "config": {"workload": f"RK4 {n}^2 plain FP64, 64 vortices, dt=5e-4", "grid": n,
-                      "rk4_steps_per_step": 1},
+                      "rk4_steps_per_step": S, "parallelism": "single",
+                      "l2": "host caches not flushed (CPU arm)"},
            "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port",
-                            "sample": f"1 RK4 step at {n}^2 per bench step; the Fortran+FFTW+MPI "
+                            "sample": f"{S} RK4 steps at {n}^2 per bench step; the Fortran+FFTW+MPI "
                                       "reference cannot be built here (no gfortran, MPI or FFTW), so the "
                                       "oracle restatement runs on all host cores"},
            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}

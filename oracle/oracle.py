@@ -59,6 +59,8 @@ def lib() -> C.CDLL:
             ("vko_set_sgle", None, [vp, C.c_int32, C.c_double, C.c_double, C.c_double, C.c_int32, C.c_double,
                                     C.c_uint64]),
             ("vko_chempot", C.c_double, [vp]),
+            ("vko_ic_vortices", C.c_int32, [C.c_int32, C.c_int32, C.c_int32, C.c_uint64, C.c_double, C.c_double,
+                                            dp, dp]),
         ]:
             f = getattr(L, name)
             f.restype = res
@@ -178,3 +180,32 @@ class Oracle:
         a, b = C.c_int32(), C.c_int32()
         lib().vko_count_vortices(self._h, C.byref(a), C.byref(b))
         return int(a.value), int(b.value)
+
+
+def derived_params(nx, ny=None, dt=1e-3, xi_in=2.0 ** 0.5, csound=1.0, rho_avg=1.0, n_particles=0, ppotd=2.0,
+                   ppotv0=10.0, gp_mass_part=0.0, renorm=False):
+    """Keyword arguments of Oracle for a namelist (restates set_grid,
+    src/mod_grid.f90:79-82, and the derived physics, src/driver.f90:362-370,
+    391-392): xi = xi_in*dx, alpha = csound*xi*sqrt(rho_avg/2),
+    g = csound^2/(2 alpha), omega = g, V0 <- ppotV0*g, d <- ppotd*xi."""
+    ny = ny or nx
+    dx = 2.0 * np.pi / nx
+    xi = xi_in * dx
+    alpha = csound * xi * np.sqrt(rho_avg / 2.0)
+    g = csound * csound / (2.0 * alpha)
+    return dict(nx=nx, ny=ny, dt=dt, alpha=alpha, gstrength=g, omega_chem=g, disp_factor=0.0, xi=xi,
+                n_particles=n_particles, ppot_v0=ppotv0 * g, ppot_d=ppotd * xi, gp_mass_part=gp_mass_part,
+                renorm=renorm)
+
+
+def ic_vortices(nx, ny, n_vort, seed, xi0=None, min_sep=0.0):
+    """Seeded neutral vortex state (vko_ic_vortices); xi0 defaults to
+    sqrt(2)*dx.  Returns (psi[ny, nx], positions[n_vort, 2])."""
+    if xi0 is None:
+        xi0 = 2.0 ** 0.5 * 2.0 * np.pi / nx
+    psi = np.empty((ny, nx), dtype=np.complex128)
+    pos = np.empty((max(n_vort, 1), 2))
+    rc = lib().vko_ic_vortices(nx, ny, n_vort, seed, xi0, min_sep, _d(psi.view(np.float64)), _d(pos))
+    if rc != 0:
+        raise ValueError("vko_ic_vortices: invalid arguments or the vortices cannot be placed")
+    return psi, pos[:n_vort]

@@ -282,6 +282,93 @@ void vko_set_threads(int32_t n) {
 #endif
 }
 
+/* ---- seeded vortex initial state (new component) ---------------------- */
+
+static uint64_t ic_splitmix(uint64_t* state) {
+  uint64_t z = (*state += 0x9E3779B97F4A7C15ull);
+  z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+  z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+  return z ^ (z >> 31);
+}
+
+static double ic_unit(uint64_t* state) { return (double)(ic_splitmix(state) >> 11) / 9007199254740992.0; }
+
+/* periodic difference on [0, 2pi) folded into (-pi, pi] */
+static double ic_fold(double d) {
+  const double pi = 3.14159265358979323846264338327950288;
+  d = fmod(d, 2.0 * pi);
+  if (d > pi) d -= 2.0 * pi;
+  if (d <= -pi) d += 2.0 * pi;
+  return d;
+}
+
+int32_t vko_ic_vortices(int32_t nx, int32_t ny, int32_t n_vort, uint64_t seed, double xi0, double min_sep,
+                        double* psi, double* pos) {
+  const double pi = 3.14159265358979323846264338327950288;
+  if (nx <= 0 || ny <= 0 || n_vort < 0 || (n_vort & 1) || !(xi0 > 0.0) || !psi) return -1;
+  double* vx = (double*)malloc(sizeof(double) * (n_vort + 1));
+  double* vy = (double*)malloc(sizeof(double) * (n_vort + 1));
+  uint64_t st = seed;
+  for (int j = 0; j < n_vort; ++j) {
+    long tries = 0;
+    for (;;) {
+      const double x = 2.0 * pi * ic_unit(&st), y = 2.0 * pi * ic_unit(&st);
+      int far = 1;
+      for (int i = 0; i < j && far; ++i) {
+        const double ex = ic_fold(x - vx[i]), ey = ic_fold(y - vy[i]);
+        far = sqrt(ex * ex + ey * ey) >= min_sep;
+      }
+      if (far) { vx[j] = x; vy[j] = y; break; }
+      if (++tries > 1000000) { free(vx); free(vy); return -1; }
+    }
+  }
+  /* sum of q_j x_j: the linear phase -y S/(2 pi) cancels the theta
+     function's quasi-periodicity along y */
+  double S = 0.0;
+  for (int j = 0; j < n_vort; ++j) S += (j < n_vort / 2 ? 1.0 : -1.0) * vx[j];
+  double q2[10];
+  for (int m = 1; m <= 9; ++m) q2[m] = exp(-2.0 * pi * m);  /* q^{2m}, q = e^{-pi} */
+#pragma omp parallel for schedule(static)
+  for (int y = 0; y < ny; ++y) {
+    const double yy = 2.0 * pi * y / ny;
+    for (int x = 0; x < nx; ++x) {
+      const double xx = 2.0 * pi * x / nx;
+      double amp = 1.0;
+      cx ph = {1.0, 0.0};
+      for (int j = 0; j < n_vort; ++j) {
+        const double ddx = xx - vx[j], ddy = yy - vy[j];
+        const double fx = ic_fold(ddx), fy = ic_fold(ddy);
+        const double r = sqrt(fx * fx + fy * fy) / xi0;
+        amp *= r / sqrt(2.0 + r * r);
+        /* theta_1(v | q), v = (ddx + i ddy)/2, up to a positive factor:
+           sin v * prod_m (1 - q^2m e^{2iv}) (1 - q^2m e^{-2iv}) */
+        cx th = {sin(0.5 * ddx) * cosh(0.5 * ddy), cos(0.5 * ddx) * sinh(0.5 * ddy)};
+        const double c = cos(ddx), sn = sin(ddx), dn = exp(-ddy), up = exp(ddy);
+        for (int m = 1; m <= 9; ++m) {
+          const cx f1 = {1.0 - q2[m] * dn * c, -q2[m] * dn * sn};
+          const cx f2 = {1.0 - q2[m] * up * c, q2[m] * up * sn};
+          th = cmul(th, cmul(f1, f2));
+        }
+        const double mod = hypot(th.re, th.im);
+        cx u = {1.0, 0.0};
+        if (mod > 0.0) { u.re = th.re / mod; u.im = th.im / mod; }
+        if (j >= n_vort / 2) u.im = -u.im;
+        ph = cmul(ph, u);
+      }
+      const cx lin = {cos(-yy * S / (2.0 * pi)), sin(-yy * S / (2.0 * pi))};
+      ph = cmul(ph, lin);
+      const double mod = hypot(ph.re, ph.im);
+      psi[2 * ((size_t)y * nx + x)] = amp * ph.re / mod;
+      psi[2 * ((size_t)y * nx + x) + 1] = amp * ph.im / mod;
+    }
+  }
+  if (pos)
+    for (int j = 0; j < n_vort; ++j) { pos[2 * j] = vx[j]; pos[2 * j + 1] = vy[j]; }
+  free(vx);
+  free(vy);
+  return 0;
+}
+
 static inline int masked(const vko_state* s, int k1, int k2) {
   int ksqr = k1 * k1 + k2 * k2;
   return (double)ksqr >= s->ka2; /* IF (ksqr .GE. kalias**2) */

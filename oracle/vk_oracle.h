@@ -96,6 +96,16 @@ void vko_count_vortices(const vko_state* s, int32_t* n_plus, int32_t* n_minus);
 
 void vko_set_threads(int32_t n);
 
+/* Seeded neutral vortex state (new component, no reference counterpart):
+ * positions from SplitMix64(seed), uniform on [0,2pi)^2 with a periodic
+ * minimum separation, charges +1 for the first half and -1 for the rest;
+ * amplitude prod_j (r_j/xi0)/sqrt(2 + (r_j/xi0)^2), phase from the odd Jacobi
+ * theta function (nome e^{-pi}) with the linear term that makes it periodic.
+ * psi[ny*nx] interleaved complex, pos[2*n_vort].  Returns 0, or -1 when the
+ * arguments are invalid or the vortices cannot be placed. */
+int32_t vko_ic_vortices(int32_t nx, int32_t ny, int32_t n_vort, uint64_t seed, double xi0, double min_sep,
+                        double* psi, double* pos);
+
 #ifdef __cplusplus
 }
 #endif

@@ -73,67 +73,96 @@ __global__ void k_part_tables(PartState ps, PartConsts c) {
   }
 }
 
-// Sequential particle update of one RK4 stage (gp_particle_motion_rk4), or
-// with STAGE == 0 only the force evaluation at the current positions (the
-// diagnostics loop, src/diagnostics.f90:528-533).  One thread.
+// Particle update of one RK4 stage (gp_particle_motion_rk4), or with
+// STAGE == 0 only the force evaluation at the current positions (the
+// diagnostics loop, src/diagnostics.f90:528-533).  One CTA of
+// kPartThreads threads.
+//  1. Fluid forces of all particles: warp w reduces particles w, w + nwarps,
+//     ...; lane l sums the per-CTA Parseval partials of blocks l, l + 32, ...
+//     in increasing order, then a fixed shuffle tree (lane 0's sum is the
+//     same on every run).  Staged in frc.
+//  2. The particles in index order (the reference's order: particle i sees
+//     particles j < i at their updated positions, src/gpe_particle.f90:456-467),
+//     warp 0: lanes take the repulsion terms j = l, l + 32, ..., a shuffle
+//     tree sums them, lane 0 adds the fluid and external forces and updates
+//     particle i before the next one starts.
 __device__ __forceinline__ double ipow_d(double x, int n) {
   double r = 1.0;
   for (int i = 0; i < n; ++i) r *= x;
   return r;
 }
 
-__global__ void k_part_update(PartState ps, PartConsts c, int stage) {
-  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+__device__ __forceinline__ double warp_sum_d(double v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+
+__global__ void __launch_bounds__(kPartThreads) k_part_update(PartState ps, PartConsts c, int stage) {
   const int np = c.np;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarp = blockDim.x >> 5;
   if (stage == 1)
-    for (int i = 0; i < 2 * np; ++i) {
+    for (int i = threadIdx.x; i < 2 * np; i += blockDim.x) {
       ps.tvel[i] = ps.vel[i];
       ps.tpos[i] = ps.pos[i];
     }
   const double fl = -2.0 * c.alpha * c.dvol * c.scale;  // -2 alpha dvol (1/N^2)
-  for (int ip = 0; ip < np; ++ip) {
-    // fluid force: fixed-order sum of the per-CTA Parseval partials
-    double f[2] = {0.0, 0.0};
-    for (int b = 0; b < c.nblk; ++b) {
-      f[0] += ps.fpart[(size_t)b * 2 * np + 2 * ip];
-      f[1] += ps.fpart[(size_t)b * 2 * np + 2 * ip + 1];
-    }
+  for (int ip = warp; ip < np; ip += nwarp) {
     // sum_x d rho V_i = f/N^2 (Parseval); force = -2 alpha dvol * that
-    f[0] *= fl;
-    f[1] *= fl;
+    double f0 = 0.0, f1 = 0.0;
+    for (int b = lane; b < c.nblk; b += 32) {
+      f0 += ps.fpart[(size_t)b * 2 * np + 2 * ip];
+      f1 += ps.fpart[(size_t)b * 2 * np + 2 * ip + 1];
+    }
+    f0 = warp_sum_d(f0);
+    f1 = warp_sum_d(f1);
+    if (lane == 0) {
+      ps.frc[2 * ip] = f0 * fl;
+      ps.frc[2 * ip + 1] = f1 * fl;
+    }
+  }
+  __syncthreads();
+  if (warp != 0) return;
+  for (int ip = 0; ip < np; ++ip) {
     // short-range repulsion with the current positions (shortrange_repulsion, :378-427)
-    double rep[2] = {0.0, 0.0};
+    double r0 = 0.0, r1 = 0.0;
     if (np > 1)
-      for (int j = 0; j < np; ++j) {
+      for (int j = lane; j < np; j += 32) {
         if (j == ip) continue;
         const double x = ps.pos[2 * ip] - ps.pos[2 * j], y = ps.pos[2 * ip + 1] - ps.pos[2 * j + 1];
         const double den = ipow_d(-3.0 + cos(x) + cos(y), 7);
-        rep[0] += -c.rep_factor * sin(x) / den;
-        rep[1] += -c.rep_factor * sin(y) / den;
+        r0 += -c.rep_factor * sin(x) / den;
+        r1 += -c.rep_factor * sin(y) / den;
       }
-    for (int d = 0; d < 2; ++d) {
-      const int i = 2 * ip + d;
-      const double ft = f[d] + rep[d] + ps.f0ext[i];
-      ps.frc[i] = ft;
-      if (stage == 0) continue;
-      const double ku = c.dt * ft / c.mass;
-      const double kq = c.dt * ps.vel[i];
-      ps.ku[(stage - 1) * 2 * np + i] = ku;
-      ps.kq[(stage - 1) * 2 * np + i] = kq;
-      if (stage == 1 || stage == 2) {
-        ps.vel[i] = ps.tvel[i] + 0.5 * ku;
-        ps.pos[i] = ps.tpos[i] + 0.5 * kq;
-      } else if (stage == 3) {
-        ps.vel[i] = ps.tvel[i] + ku;
-        ps.pos[i] = ps.tpos[i] + kq;
-      } else {
-        const double* K1 = ps.ku;
-        const double* Q1 = ps.kq;
-        const size_t o = 2 * (size_t)np;
-        ps.vel[i] = ps.tvel[i] + (1.0 / 6.0) * (K1[i] + 2.0 * K1[o + i] + 2.0 * K1[2 * o + i] + K1[3 * o + i]);
-        ps.pos[i] = ps.tpos[i] + (1.0 / 6.0) * (Q1[i] + 2.0 * Q1[o + i] + 2.0 * Q1[2 * o + i] + Q1[3 * o + i]);
+    r0 = warp_sum_d(r0);
+    r1 = warp_sum_d(r1);
+    if (lane == 0) {
+      const double rep[2] = {r0, r1};
+      for (int d = 0; d < 2; ++d) {
+        const int i = 2 * ip + d;
+        const double ft = ps.frc[i] + rep[d] + ps.f0ext[i];
+        ps.frc[i] = ft;
+        if (stage == 0) continue;
+        const double ku = c.dt * ft / c.mass;
+        const double kq = c.dt * ps.vel[i];
+        ps.ku[(stage - 1) * 2 * np + i] = ku;
+        ps.kq[(stage - 1) * 2 * np + i] = kq;
+        if (stage == 1 || stage == 2) {
+          ps.vel[i] = ps.tvel[i] + 0.5 * ku;
+          ps.pos[i] = ps.tpos[i] + 0.5 * kq;
+        } else if (stage == 3) {
+          ps.vel[i] = ps.tvel[i] + ku;
+          ps.pos[i] = ps.tpos[i] + kq;
+        } else {
+          const double* K1 = ps.ku;
+          const double* Q1 = ps.kq;
+          const size_t o = 2 * (size_t)np;
+          ps.vel[i] = ps.tvel[i] + (1.0 / 6.0) * (K1[i] + 2.0 * K1[o + i] + 2.0 * K1[2 * o + i] + K1[3 * o + i]);
+          ps.pos[i] = ps.tpos[i] + (1.0 / 6.0) * (Q1[i] + 2.0 * Q1[o + i] + 2.0 * Q1[2 * o + i] + Q1[3 * o + i]);
+        }
       }
     }
+    __syncwarp();  // particle ip's new position before particle ip + 1's repulsion
   }
 }
 

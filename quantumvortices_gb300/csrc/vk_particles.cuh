@@ -14,7 +14,8 @@
 // real).  e^{ik.q_i} = ex_i(kx) ey_i(ky) from FP64 tables rebuilt from the
 // stage positions; the same products give V^_tot for the RHS.  The
 // sequential per-particle update (repulsion sees particles j < i at their new
-// positions, :456-467) runs on one thread in FP64.
+// positions, :456-467) runs on one warp in FP64, after the fluid forces of
+// all particles have been reduced by the CTA's warps.
 #pragma once
 #include "vk_kernels.cuh"
 
@@ -235,6 +236,7 @@ __global__ void __launch_bounds__(GeoX<T, L>::NT, GeoX<T, L>::MINB) k_vtot_x(con
 // src/gpe_particle.f90:429-531), or with stage == 0 only the force evaluation
 // at the current positions (diagnostics loop, src/diagnostics.f90:528-533).
 // One thread.
+constexpr int kPartThreads = 256;  // block size of k_part_update
 __global__ void k_part_update(PartState ps, PartConsts c, int stage);
 
 }  // namespace vk

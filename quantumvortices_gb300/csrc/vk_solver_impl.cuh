@@ -431,7 +431,7 @@ class Solver : public SolverBase {
       }
       y2_rk4(stage);
       if (c_.frc) launch_raw("k_rng_bump", k_rng_bump<T>, 1, 1, 0, rngc_);
-      if (np_ > 0) launch_raw("k_part_update", k_part_update, 1, 32, 0, ps_, pc_, stage);
+      if (np_ > 0) launch_raw("k_part_update", k_part_update, 1, kPartThreads, 0, ps_, pc_, stage);
     }
   }
 

@@ -5,8 +5,9 @@ test_gpu_particles.py).
 * 1024^2 with 16 Gaussian particles (V0 = 10, d = 2 xi, M = 5 pi d^2,
   64 vortices, dt = 5e-4): the oracle takes 4 FFTs per particle and stage
   (src/gpe_particle.f90:219-324), the GPU one Parseval pass for all of them.
-  psi relative L2 <= 1e-12, positions and velocities <= 1e-12 absolute,
-  forces <= 1e-9 of the largest force.
+  psi relative L2 <= 1e-12, positions and velocities <= 1e-12 absolute; on
+  the final state (diagnostics), forces <= 1e-9 of the largest force and the
+  particle potential and kinetic energies <= 1e-11 / 1e-12 relative.
 * ARGLE with renormalisation (argle_renorm = 1) at 128^2 and 1024^2:
   kpsi <= 1e-12 and the norm dvol/(nx ny) sum|kpsi|^2 equal to
   Nparticle = rho_avg Lx Ly to 1e-12.
@@ -51,17 +52,23 @@ def test_particles_1024_sixteen_particles_vs_oracle():
         s.particles_set(pos0, vel0, f0)
         s.gpe_rk4(steps)
         got = s.get_psi()
-        pos, vel, frc = s.particles_get()
+        pos, vel, _ = s.particles_get()
+        d = s.diagnostics_gpe()          # evaluates the forces on the final state
+        _, _, frc = s.particles_get()
     o = Oracle.from_vk_params(p, threads=os.cpu_count())
     o.set_psi(psi0, otoc=True, k_otoc=p.k_otoc_gp, eps_otoc=p.eps_otoc_gp)
     o.particles_set(pos0, vel0, f0)
     o.gpe_rk4(steps)
-    opos, ovel, ofrc = o.particles_get()
+    opos, ovel, _ = o.particles_get()
     assert rel(got, o.get_psi()) < 1e-12
     assert np.abs(pos - opos).max() < 1e-12
     assert np.abs(vel - ovel).max() < 1e-12
-    assert np.abs(frc - ofrc).max() <= 1e-9 * np.abs(ofrc).max()
+    sc, _ = o.diagnostics()
+    _, _, ofrc = o.particles_get()
     assert np.abs(ofrc).max() > 0.0
+    assert np.abs(frc - ofrc).max() <= 1e-9 * np.abs(ofrc).max()
+    assert abs(d.eppot - sc[7]) <= 1e-11 * abs(sc[7])
+    assert abs(d.eobj_kin - sc[8]) <= 1e-12 * abs(sc[8])
 
 
 @pytest.mark.parametrize("n,steps", [(128, 50), (1024, 10)])

@@ -253,3 +253,21 @@ def test_nn_oracle_gradient_by_finite_differences():
             assert abs(fd - g[i]) <= 1e-5 * max(1.0, abs(fd)), (i, fd, g[i])
     finally:
         nn.EXACT = False
+
+
+def test_oracle_ic_and_parameters_match_the_product():
+    """The oracle's own vortex IC and parameter derivation (used by the
+    benchmark's reference arm, which loads no product library) give the
+    product's state and parameters."""
+    import math
+    from oracle import oracle as orc
+    from quantumvortices_gb300 import vk
+    for n, nv, seed, ms in [(64, 8, 3, 0.3), (256, 64, 1, 4 * math.sqrt(2) * 2 * math.pi / 256)]:
+        a, pa = orc.ic_vortices(n, n, nv, seed, min_sep=ms)
+        b, pb = vk.ic_vortices(n, n, nv, seed, min_sep=ms)
+        assert np.array_equal(pa, pb)
+        assert np.abs(a - b).max() < 1e-13
+    p = vk.params_for(128, dt=1e-3, n_particles=3, gp_mass_part=2.0)
+    d = orc.derived_params(128, dt=1e-3, n_particles=3, gp_mass_part=2.0)
+    for k in ("alpha", "gstrength", "omega_chem", "xi", "ppot_v0", "ppot_d", "gp_mass_part", "dt"):
+        assert getattr(p, k) == d[k], k
