@@ -25,6 +25,7 @@
 #include "vk_kernels.cuh"
 #include "vk_particles.cuh"
 #include "vk_diag.cuh"
+#include "vk_stage.cuh"
 #include "vk_solver.h"
 
 namespace vk {
@@ -170,6 +171,10 @@ class Solver : public SolverBase {
     c_.xsingle = 0;
     const char* xs_env = std::getenv("VK_XSPLIT");
     if (std::is_same<T, double>::value && nx_ == 1024 && !(xs_env && xs_env[0] == '0')) c_.xsingle = ny_;
+    {
+      int frc = init_fused();
+      if (frc) return frc;
+    }
     if (p_.n_particles > 0) {
       int prc = init_particles();
       if (prc) return prc;
@@ -419,6 +424,10 @@ class Solver : public SolverBase {
   // One RK4 step (gpe_rk4, src/gpe.f90:310-494): four stages of four fused
   // passes, plus the particle tables/update when particles are on.
   void rk4_step(bool from_psi) {
+    if (fused_grid_ > 0 && !c_.frc && np_ == 0) {
+      for (int stage = 1; stage <= 4; ++stage) stage_fused(stage, from_psi && stage == 1);
+      return;
+    }
     for (int stage = 1; stage <= 4; ++stage) {
       x1((from_psi && stage == 1) ? 0 : 1, true);
       if (np_ > 0) {
@@ -657,6 +666,114 @@ class Solver : public SolverBase {
     }
     if (timing_) record_event(tag);
   }
+  // Cooperative launch (all CTAs co-resident; capturable in a graph).
+  template <typename... KA, typename... A>
+  void launch_coop(const char* tag, void (*kern)(KA...), int grid, int block, size_t smem, A... args) {
+    ensure_smem_attr((const void*)kern, smem);
+    if (timing_ && ev_used_ == 0) record_event(nullptr);
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(grid);
+    cfg.blockDim = dim3(block);
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = st_;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeCooperative;
+    at[0].val.cooperative = 1;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    const cudaError_t le = cudaLaunchKernelEx(&cfg, kern, args...);
+    ++launches_;
+    if (le != cudaSuccess && launch_err_ == cudaSuccess) {
+      launch_err_ = le;
+      launch_err_tag_ = tag;
+    }
+    if (timing_) record_event(tag);
+  }
+
+  // ------------------------------------------- persistent stage kernel --
+  // FP32 at 1024^2: each plain RK4 stage is one cooperative launch of
+  // k_stage_rk4 over fused_grid_ CTAs (vk_stage.cuh).  VK_FUSED=0 keeps the
+  // four pass kernels.  VK_SPIN_LIMIT sets how many polls a CTA waits at a
+  // barrier before it gives up (default 2^24, about a second).
+  template <int L> static constexpr bool kFusedLen = std::is_same<T, float>::value && L == 1024;
+  int init_fused() {
+    fused_grid_ = 0;
+    const char* env = std::getenv("VK_FUSED");
+    if (!(std::is_same<T, float>::value && nx_ == 1024 && ny_ == 1024) || (env && env[0] == '0')) return VK_OK;
+    int dev = 0, coop = 0, nsm = 0;
+    VK_CUDA_TRY(cudaGetDevice(&dev));
+    VK_CUDA_TRY(cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev));
+    VK_CUDA_TRY(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
+    if (!coop) return VK_OK;
+    const char* lim = std::getenv("VK_SPIN_LIMIT");
+    spin_limit_ = lim ? std::strtoull(lim, nullptr, 10) : (1ull << 24);
+    with_len(nx_, [&](auto lc) {
+      constexpr int L = decltype(lc)::value;
+      if constexpr (kFusedLen<L>) {
+        typedef typename GeoFused<T, L>::X GX;
+        typedef typename GeoFused<T, L>::Y GY;
+        fused_smem_ = sizeof(C) * std::max(GX::R * GX::LP, GY::R * GY::LP);
+        int occ = 1 << 30;
+        auto fit = [&](const void* fn) {
+          int b = 0;
+          ensure_smem_attr(fn, fused_smem_);
+          if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, fn, GeoFused<T, L>::NT, fused_smem_) != cudaSuccess)
+            b = 0;
+          occ = std::min(occ, b);
+        };
+        fit((const void*)k_stage_rk4<T, L, 1, false>);
+        fit((const void*)k_stage_rk4<T, L, 1, true>);
+        fit((const void*)k_stage_rk4<T, L, 2, true>);
+        fit((const void*)k_stage_rk4<T, L, 3, true>);
+        fit((const void*)k_stage_rk4<T, L, 4, true>);
+        cudaGetLastError();
+        const int tiles = std::max(ny_ / GX::R, (2 * K_ + GY::R) / GY::R);
+        if (occ > 0) fused_grid_ = std::min(occ * nsm, tiles);
+      }
+    });
+    if (fused_grid_ <= 0) return VK_OK;
+    VK_CUDA_TRY(cudaMalloc(&bar_, sizeof(GridBarrier)));
+    VK_CUDA_TRY(cudaMemset(bar_, 0, sizeof(GridBarrier)));
+    return VK_OK;
+  }
+  void stage_fused(int stage, bool from_psi) {
+    with_len(nx_, [&](auto lc) {
+      constexpr int L = decltype(lc)::value;
+      if constexpr (kFusedLen<L>) {
+        Field<T> f;
+        f.psi = psi_; f.kpsi = kpsi_; f.str1 = str1_; f.str2 = str2_;
+        f.Ta = Ta_; f.Tb = Tb_; f.Tc = Tc_; f.Td = Td_;
+        f.twx = twx_; f.twy = twy_; f.c = c_;
+        const int nt = GeoFused<T, L>::NT;
+        const unsigned long long lim = spin_limit_;
+        switch (stage) {
+          case 1:
+            if (from_psi) launch_coop("k_stage_rk4", k_stage_rk4<T, L, 1, false>, fused_grid_, nt, fused_smem_, f, bar_, lim);
+            else launch_coop("k_stage_rk4", k_stage_rk4<T, L, 1, true>, fused_grid_, nt, fused_smem_, f, bar_, lim);
+            break;
+          case 2: launch_coop("k_stage_rk4", k_stage_rk4<T, L, 2, true>, fused_grid_, nt, fused_smem_, f, bar_, lim); break;
+          case 3: launch_coop("k_stage_rk4", k_stage_rk4<T, L, 3, true>, fused_grid_, nt, fused_smem_, f, bar_, lim); break;
+          default: launch_coop("k_stage_rk4", k_stage_rk4<T, L, 4, true>, fused_grid_, nt, fused_smem_, f, bar_, lim); break;
+        }
+      }
+    });
+  }
+  // A barrier that timed out leaves err set: report it once, reset the
+  // barrier and invalidate the field (its contents are partial).
+  int barrier_check() {
+    if (!bar_) return VK_OK;
+    GridBarrier h;
+    VK_CUDA_TRY(cudaMemcpyAsync(&h, bar_, sizeof(h), cudaMemcpyDeviceToHost, st_));
+    VK_CUDA_TRY(cudaStreamSynchronize(st_));
+    if (h.err == 0) return VK_OK;
+    VK_CUDA_TRY(cudaMemsetAsync(bar_, 0, sizeof(GridBarrier), st_));
+    VK_CUDA_TRY(cudaStreamSynchronize(st_));
+    set_error("vk_gpe_rk4: a CTA of the persistent stage kernel gave up waiting at grid barrier " +
+              std::to_string(h.err - 1) + " (the field is not valid; set it again)");
+    have_psi_ = false;
+    return VK_E_CUDA;
+  }
+
   template <typename... KA, typename... A>
   void launch_simple(const char* tag, void (*kern)(KA...), A... args) {
     const int grid = (int)std::min<size_t>((n2_ + 255) / 256, 152 * 16);
@@ -885,7 +1002,7 @@ class Solver : public SolverBase {
     int rc = check_launch();
     if (rc) return rc;
     VK_CUDA_TRY(cudaStreamSynchronize(st_));
-    return VK_OK;
+    return barrier_check();
   }
 
   int upload(const double* host, C* dev) {
@@ -940,6 +1057,7 @@ class Solver : public SolverBase {
     if (stage64_) cudaFree(stage64_);
     if (part_) cudaFree(part_);
     if (sums_) cudaFree(sums_);
+    if (bar_) cudaFree(bar_);
     if (rngc_) cudaFree(rngc_);
     rngc_ = nullptr;
     if (Tg_) cudaFree(Tg_);
@@ -1009,6 +1127,10 @@ class Solver : public SolverBase {
   std::vector<cudaEvent_t> ev_;
   std::vector<const char*> ev_tag_;
   Diagnostics<T> diag_;
+  GridBarrier* bar_ = nullptr;            // persistent stage kernel: barrier state
+  int fused_grid_ = 0;                    //   its CTAs (0: the four pass kernels)
+  size_t fused_smem_ = 0;
+  unsigned long long spin_limit_ = 1ull << 24;
 };
 
 }  // namespace VK_SOLVER_NS
