@@ -367,16 +367,17 @@ def argle_time_to_residual(torch, n, psi0):
     return out
 
 
-def warmstart_bench(n=512, n_train=256, epochs=3, n_eval=8):
+def warmstart_bench(n=512, n_train=512, epochs=6, n_eval=8, batch=8):
     """The learned ARGLE warm start trained in this process at a reduced size
     (n_train solver-generated 512^2 states, 8-128 vortices, 1000 FP32 ARGLE
-    steps each) and evaluated on n_eval held-out seeds disjoint from the
-    training seeds: ARGLE iterations saved and wall-time ratio to the residual
-    plain ARGLE reaches after 1000 steps, and the ARGLE functional E - Omega N
-    after equal steps."""
+    steps each; batches of `batch` images) and evaluated on n_eval held-out
+    seeds disjoint from the training seeds: ARGLE iterations saved and
+    wall-time ratio (features and network included) to the residual plain
+    ARGLE reaches after 1000 steps, and the ARGLE functional E - Omega N after
+    equal steps."""
     from quantumvortices_gb300 import warmstart as ws
     gen = ws.DataGen(n, 1000)
-    net = ws.WarmStartNet(n, n, 32, 4, seed=1)
+    net = ws.WarmStartNet(n, n, 32, 4, seed=1, batch=batch)
     try:
         tr = ws.train(net, gen, n_train, epochs, 1e-3, log=lambda *a: None)
         rows = ws.evaluate(net, gen, list(range(900_000, 900_000 + n_eval)), log=lambda *a: None)
@@ -384,7 +385,7 @@ def warmstart_bench(n=512, n_train=256, epochs=3, n_eval=8):
     finally:
         net.close()
         gen.close()
-    return {"grid": n, "training_states": n_train, "epochs": epochs, "held_out_seeds": n_eval,
+    return {"grid": n, "training_states": n_train, "epochs": epochs, "batch": batch, "held_out_seeds": n_eval,
             "reduced_from": "20000 training states / 1000 held-out seeds",
             "generation_s": tr["gen_s"], "train_s": tr["train_s"], "train_tflops": tr["tensor_tflops"],
             **{k: summ[k] for k in ("iterations_saved_frac", "time_ratio_warm_over_plain", "time_ratio_median",

@@ -205,6 +205,22 @@ int vk_nn_set_params(void* net, const float* host, int64_t n);
 int vk_nn_forward(void* net, const float* in_dev, float* out_dev, void* stream);
 int vk_nn_loss_grad(void* net, const float* in_dev, const float* target_dev, double* loss_out, float* grad_host);
 int vk_nn_train_step(void* net, const float* in_dev, const float* target_dev, float lr, double* loss_out);
+/* Batched training and inference (new).  vk_nn_create_batched sizes the
+ * activations for up to batch_cap images (1..64); vk_nn_set_batch(net, b),
+ * b <= batch_cap, makes vk_nn_forward, vk_nn_loss_grad and vk_nn_train_step
+ * take b images: inputs [b][3][h][w], outputs and targets [b][2][h][w]; the
+ * loss is the mean over the b images (one Adam step per batch).
+ * vk_nn_create is vk_nn_create_batched with batch_cap 1. */
+int vk_nn_create_batched(int32_t h, int32_t w, int32_t base, int32_t levels, int32_t batch_cap, uint64_t seed,
+                         void** net);
+int vk_nn_set_batch(void* net, int32_t batch);
+/* Input features of one image on the device (new): out_dev [3][h][w] FP32
+ * = Re psi, Im psi and the signed vortex-charge density
+ * sum_j q_j exp(-|x - x_j|^2 / (2 width^2)) (periodic distance; q_j = +1 for
+ * the first n_vort/2 vortices, -1 for the rest).  psi_host [h][w] complex128
+ * (x fastest), pos_host [n_vort][2] (x, y), n_vort <= 4096. */
+int vk_nn_features(void* net, const double* psi_host, const double* pos_host, int32_t n_vort, double width,
+                   float* out_dev);
 
 /* Per-kernel timing.  Between vk_timing_begin and vk_timing_end every kernel
  * this context launches is bracketed by CUDA events on the context's stream;

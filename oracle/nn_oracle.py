@@ -156,3 +156,20 @@ def loss_grad(params, inp, target, base, levels):
         flat.append(dw.ravel())
         flat.append(db.ravel())
     return loss, np.concatenate(flat)
+
+
+def features(h, w, pos, psi, width):
+    """[3, h, w] input features (vk_nn_features restated): Re/Im psi and the
+    signed vortex-charge density sum_j q_j exp(-|x - x_j|^2 / (2 width^2))
+    with periodic distances folded into [-pi, pi), q_j = +1 for the first
+    half of pos and -1 for the rest."""
+    nv = len(pos)
+    x = np.arange(w) * 2 * np.pi / w
+    y = np.arange(h) * 2 * np.pi / h
+    X, Y = np.meshgrid(x, y)
+    q = np.zeros((h, w))
+    for j in range(nv):
+        dx = (X - pos[j, 0] + np.pi) % (2 * np.pi) - np.pi
+        dy = (Y - pos[j, 1] + np.pi) % (2 * np.pi) - np.pi
+        q += (1.0 if j < nv // 2 else -1.0) * np.exp(-(dx * dx + dy * dy) / (2 * width * width))
+    return np.stack([psi.real, psi.imag, q])

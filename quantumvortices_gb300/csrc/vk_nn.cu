@@ -47,7 +47,7 @@ __device__ __forceinline__ int wrapi(int v, int n) { return v < 0 ? v + n : (v >
 constexpr int kConvStages = 2;
 
 template <int BN>
-__global__ void __launch_bounds__(128) k_conv(const bf16* __restrict__ in, int H, int W, int Cin,
+__global__ void __launch_bounds__(128) k_conv(const bf16* __restrict__ in, int H, int W, int nimg, int Cin,
                                               const bf16* __restrict__ wgt, const float* __restrict__ bias,
                                               int cout, int relu, bf16* __restrict__ out_bf, int ldo,
                                               float* __restrict__ out_f, int nout, int* __restrict__ err) {
@@ -57,7 +57,7 @@ __global__ void __launch_bounds__(128) k_conv(const bf16* __restrict__ in, int H
   __shared__ __align__(8) uint64_t bar[S];
   __shared__ uint32_t tslot;
   const int tid = threadIdx.x, warp = tid >> 5;
-  const int npix = H * W;
+  const int npix = nimg * H * W;  // the images are stacked: image b holds rows [b H, (b + 1) H)
   const int p0 = blockIdx.x * 128, n0 = blockIdx.y * BN;
   const int KT = 9 * Cin, nck = (KT + 63) / 64;
   constexpr uint32_t NCOL = BN < 32 ? 32 : BN;
@@ -70,13 +70,15 @@ __global__ void __launch_bounds__(128) k_conv(const bf16* __restrict__ in, int H
   const uint32_t idesc = tc::idesc_bf16(128, BN);
   // this thread's A vectors: column kv = tid & 7 of rows tid/8 + 16 j
   const int kv = tid & 7;
-  int py[8], px[8];
+  int py[8], px[8], pyb[8];  // row in the image, column, first row of the image
   bool pin[8];
 #pragma unroll
   for (int j = 0; j < 8; ++j) {
     const int p = p0 + (tid >> 3) + 16 * j;
     pin[j] = p < npix;
-    py[j] = pin[j] ? p / W : 0;
+    const int row = pin[j] ? p / W : 0;
+    pyb[j] = row - row % H;
+    py[j] = row - pyb[j];
     px[j] = pin[j] ? p % W : 0;
   }
   auto load_chunk = [&](int i, int buf) {
@@ -90,7 +92,7 @@ __global__ void __launch_bounds__(128) k_conv(const bf16* __restrict__ in, int H
     for (int j = 0; j < 8; ++j) {
       const int r = (tid >> 3) + 16 * j;
       const bool ok = kin && pin[j];
-      const int src = ok ? wrapi(py[j] + dy, H) * W + wrapi(px[j] + dx, W) : 0;
+      const int src = ok ? (pyb[j] + wrapi(py[j] + dy, H)) * W + wrapi(px[j] + dx, W) : 0;
       tc::cp_async16<true>(sA + (r >> 3) * 1024 + kv * 128 + (r & 7) * 16, in + (size_t)src * Cin + ci, ok ? 16u : 0u);
     }
 #pragma unroll
@@ -209,7 +211,9 @@ __global__ void __launch_bounds__(128) k_conv_rows(const bf16* __restrict__ in, 
   __shared__ __align__(8) uint64_t bar[2];
   __shared__ uint32_t tslot;
   const int tid = threadIdx.x, warp = tid >> 5;
+  // stacked images: rows [y0, y0 + RB) lie in image y0 / H (RB divides H)
   const int x0 = blockIdx.x * 128, y0 = blockIdx.y * RB, n0 = blockIdx.z * BN;
+  const int yb = y0 - y0 % H, yl = y0 - yb;
   if (warp == 0) tc::tmem_alloc(&tslot, NCOL);
   if (tid < 2) tc::mbar_init(&bar[tid]);
   tc::fence_before();
@@ -225,7 +229,7 @@ __global__ void __launch_bounds__(128) k_conv_rows(const bf16* __restrict__ in, 
   }
   tc::cp_async_commit();
   auto load_row = [&](int srow, int buf) {
-    const int j = wrapi(y0 - 1 + srow, H);
+    const int j = yb + wrapi(yl - 1 + srow, H);
     unsigned char* st = sI + buf * STAGE;
     for (int i = tid; i < 3 * 128 * VR; i += 128) {
       const int dx = i / (128 * VR), rem = i - dx * (128 * VR), m = rem / VR, kv = rem - m * VR;
@@ -347,7 +351,7 @@ __device__ __forceinline__ void transpose8x8(const uint4 (&r)[8], uint4 (&t)[8])
 // from the dy blocks they already hold.
 template <int BN, int DEPTH>
 __global__ void __launch_bounds__(128) k_wgrad(const bf16* __restrict__ in, const bf16* __restrict__ dy, int H, int W,
-                                               int Cin, int pix_per_cta, float* __restrict__ dW,
+                                               int nimg, int Cin, int pix_per_cta, float* __restrict__ dW,
                                                float* __restrict__ db, int nb, int* __restrict__ err) {
   constexpr int ABYTES = 128 * 64 * 2, STAGE = ABYTES + BN * 64 * 2;
   constexpr int NBB = (BN + 127) / 128;  // B blocks per thread
@@ -355,7 +359,7 @@ __global__ void __launch_bounds__(128) k_wgrad(const bf16* __restrict__ in, cons
   __shared__ __align__(8) uint64_t bar[2];
   __shared__ uint32_t tslot;
   const int tid = threadIdx.x, warp = tid >> 5;
-  const int npix = H * W, M = 9 * Cin;
+  const int npix = nimg * H * W, M = 9 * Cin;  // stacked images, as in k_conv
   const int m0 = blockIdx.x * 128;
   const int q0 = blockIdx.y * pix_per_cta, q1 = min(npix, q0 + pix_per_cta);
   const int nck = q1 > q0 ? (q1 - q0 + 63) / 64 : 0;
@@ -389,7 +393,8 @@ __global__ void __launch_bounds__(128) k_wgrad(const bf16* __restrict__ in, cons
       uint4 v = make_uint4(0, 0, 0, 0);
       if (rowok && q < q1) {
         const int y = q / W, x = q - y * W;
-        const int src = wrapi(y + ty, H) * W + wrapi(x + tx, W);
+        const int yb = y - y % H;
+        const int src = (yb + wrapi(y - yb + ty, H)) * W + wrapi(x + tx, W);
         v = *reinterpret_cast<const uint4*>(in + (size_t)src * Cin + ci0);
       }
       ra[SL][e] = v;
@@ -516,10 +521,12 @@ __global__ void __launch_bounds__(128) k_wgrad(const bf16* __restrict__ in, cons
 
 // ------------------------------------------------------------ elementwise --
 
-__global__ void k_pack_input(const float* __restrict__ in, bf16* __restrict__ out, int npix, int cin, int cpad) {
-  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < npix * cpad; i += gridDim.x * blockDim.x) {
-    const int p = i / cpad, c = i % cpad;
-    out[i] = __float2bfloat16(c < cin ? in[(size_t)c * npix + p] : 0.f);
+// planar [nimg][cin][npix] FP32 -> NHWC BF16 [nimg * npix][cpad]
+__global__ void k_pack_input(const float* __restrict__ in, bf16* __restrict__ out, int npix, int nimg, int cin,
+                             int cpad) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < nimg * npix * cpad; i += gridDim.x * blockDim.x) {
+    const int p = i / cpad, c = i % cpad, b = p / npix, q = p - b * npix;
+    out[i] = __float2bfloat16(c < cin ? in[((size_t)b * cin + c) * npix + q] : 0.f);
   }
 }
 __global__ void k_pool(const bf16* __restrict__ in, bf16* __restrict__ out, int H, int W, int C) {
@@ -565,17 +572,19 @@ __global__ void k_relu_bwd(const bf16* __restrict__ y, const bf16* __restrict__ 
   for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
     o[i] = __bfloat162float(y[i]) > 0.f ? d[i] : __float2bfloat16(0.f);
 }
-// MSE loss on the head output (FP32 [p][nout]) against planar targets
-// [nout][p]; writes the BF16 gradient [p][cpad] and accumulates the loss.
-__global__ void k_loss(const float* __restrict__ out, const float* __restrict__ tgt, int npix, int nout, int cpad,
-                       bf16* __restrict__ dout, double* __restrict__ loss) {
-  const float inv = 1.f / (float)(npix * nout);
+// MSE loss (mean over the images, pixels and outputs) on the head output
+// (FP32 [p][nout], p over the stacked images) against planar targets
+// [nimg][nout][npix]; writes the BF16 gradient [p][cpad] and accumulates the
+// loss.
+__global__ void k_loss(const float* __restrict__ out, const float* __restrict__ tgt, int npix, int nimg, int nout,
+                       int cpad, bf16* __restrict__ dout, double* __restrict__ loss) {
+  const float inv = 1.f / (float)(nimg * npix * nout);
   double acc = 0.0;
-  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < npix * cpad; i += gridDim.x * blockDim.x) {
-    const int p = i / cpad, c = i % cpad;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < nimg * npix * cpad; i += gridDim.x * blockDim.x) {
+    const int p = i / cpad, c = i % cpad, b = p / npix, q = p - b * npix;
     float g = 0.f;
     if (c < nout) {
-      const float e = out[(size_t)p * nout + c] - tgt[(size_t)c * npix + p];
+      const float e = out[(size_t)p * nout + c] - tgt[((size_t)b * nout + c) * npix + q];
       acc += (double)e * e;
       g = 2.f * e * inv;
     }
@@ -611,11 +620,12 @@ __global__ void k_wgrad_scatter(const float* __restrict__ g, int cout, int cin, 
     grad[i] += g[((size_t)t * cinp + ci) * coutp + co];
   }
 }
-// [p][2] -> planar [2][p]
-__global__ void k_planar2(const float* __restrict__ in, float* __restrict__ out, int npix) {
-  for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < npix; p += gridDim.x * blockDim.x) {
-    out[p] = in[2 * p];
-    out[npix + p] = in[2 * p + 1];
+// [p][2] over the stacked images -> planar [nimg][2][npix]
+__global__ void k_planar2(const float* __restrict__ in, float* __restrict__ out, int npix, int nimg) {
+  for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < nimg * npix; p += gridDim.x * blockDim.x) {
+    const int b = p / npix, q = p - b * npix;
+    out[(size_t)b * 2 * npix + q] = in[2 * p];
+    out[(size_t)b * 2 * npix + npix + q] = in[2 * p + 1];
   }
 }
 __global__ void k_adam(float* __restrict__ p, const float* __restrict__ g, float* __restrict__ m, float* __restrict__ v,
@@ -629,8 +639,44 @@ __global__ void k_adam(float* __restrict__ p, const float* __restrict__ g, float
   }
 }
 
+// --------------------------------------------------------- input features --
+// Per-vortex Gaussian factors of the signed charge density:
+// gx[j][x] = exp(-dx^2/(2 w^2)), gy[j][y] likewise, dx the periodic distance
+// of grid column x (at 2 pi x / W) from vortex j, folded into [-pi, pi).
+__global__ void k_feat_tables(const double* __restrict__ pos, int nv, int H, int W, double inv2w2,
+                              float* __restrict__ gx, float* __restrict__ gy) {
+  const double two_pi = 6.283185307179586476925286766559, pi = 0.5 * two_pi;
+  const int n = nv * (W + H);
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const bool isx = i < nv * W;
+    const int k = isx ? i : i - nv * W;
+    const int len = isx ? W : H, j = k / len, t = k - j * len;
+    const double c = isx ? pos[2 * j] : pos[2 * j + 1];
+    double d = t * (two_pi / len) - c + pi;
+    d = d - two_pi * floor(d / two_pi) - pi;
+    (isx ? gx : gy)[k] = (float)exp(-d * d * inv2w2);
+  }
+}
+// out [3][H][W] planar FP32: Re psi, Im psi, sum_j q_j gx[j][x] gy[j][y] with
+// q_j = +1 for the first half of the vortices and -1 for the rest.
+__global__ void k_features(const double2* __restrict__ psi, const float* __restrict__ gx,
+                           const float* __restrict__ gy, int nv, int H, int W, float* __restrict__ out) {
+  const int npix = H * W;
+  for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < npix; p += gridDim.x * blockDim.x) {
+    const int y = p / W, x = p - y * W;
+    float q = 0.f;
+    for (int j = 0; j < nv; ++j) q = fmaf(j < nv / 2 ? gx[j * W + x] : -gx[j * W + x], gy[j * H + y], q);
+    const double2 v = psi[p];
+    out[p] = (float)v.x;
+    out[npix + p] = (float)v.y;
+    out[2 * npix + p] = q;
+  }
+}
+
 // ------------------------------------------------------------- network --
 
+// One image's h x w x c; the buffer holds the network's batch capacity of
+// images stacked along h (image b in rows [b h, (b + 1) h)).
 struct Tensor {
   bf16* d = nullptr;
   int h = 0, w = 0, c = 0;
@@ -658,6 +704,11 @@ class Net {
   double* loss = nullptr;
   float* out_f = nullptr;     // head output [p][2]
   int64_t steps = 0;
+  int nb = 1, bcap = 1;       // images in the current batch, batch capacity
+  static constexpr int kMaxVortices = 4096;  // vk_nn_features
+  double2* feat_psi = nullptr;
+  double* feat_pos = nullptr;
+  float *feat_gx = nullptr, *feat_gy = nullptr;
   cudaStream_t st = nullptr;
   // row-block kernel for the narrow layers (VK_CONV_ROWS=0 turns it off)
   bool rows_ok_ = [] {
@@ -689,9 +740,10 @@ class Net {
     t.h = h;
     t.w = w;
     t.c = c;
-    t.d = dalloc<bf16>(t.n());
+    t.d = dalloc<bf16>(t.n() * bcap);
     return t;
   }
+  size_t N(const Tensor& t) const { return t.n() * nb; }  // elements of the current batch
   int add_conv(int cin, int cout, bool relu) {
     Conv cv;
     cv.cin = cin;
@@ -707,7 +759,8 @@ class Net {
     return (int)convs.size() - 1;
   }
 
-  int init(int h, int w, int base_ch, int nlev, uint64_t seed) {
+  int init(int h, int w, int base_ch, int nlev, uint64_t seed, int batch_cap) {
+    bcap = nb = batch_cap;
     H = h;
     W = w;
     base = base_ch;
@@ -781,7 +834,11 @@ class Net {
       }
     }
     dhead = tens(H, W, 16);
-    out_f = dalloc<float>((size_t)H * W * 2);
+    out_f = dalloc<float>((size_t)H * W * 2 * bcap);
+    feat_psi = dalloc<double2>((size_t)H * W);
+    feat_pos = dalloc<double>(2 * kMaxVortices);
+    feat_gx = dalloc<float>((size_t)kMaxVortices * W);
+    feat_gy = dalloc<float>((size_t)kMaxVortices * H);
     for (auto* q : allocs)
       if (!q) return VK_E_NOMEM;
     return refresh_weights();
@@ -799,7 +856,7 @@ class Net {
   void conv(const Tensor& in, const bf16* w, int cout_p, int cout, const float* bias, int relu, bf16* out_bf,
             float* out_f32, int nout) {
     if (conv_rows(in, w, cout_p, cout, bias, relu, out_bf, out_f32, nout)) return;
-    const int npix = in.h * in.w;
+    const int npix = nb * in.h * in.w;
     const int tiles = (npix + 127) / 128;
     int bn = std::min(cout_p, 128);
     while (bn > 32 && tiles * (cout_p / bn) < 2 * 152) bn /= 2;
@@ -818,11 +875,11 @@ class Net {
     if (!rows_ok_ || (cin != 16 && cin != 32 && cin != 64) || in.w % 128 != 0 || cout_p > 64) return false;
     int rb = 4;
     int bn = cout_p;
-    auto ctas = [&]() { return (in.w / 128) * (in.h / rb) * (cout_p / bn); };
+    auto ctas = [&]() { return (in.w / 128) * (nb * in.h / rb) * (cout_p / bn); };
     if (ctas() < 2 * 152 && bn > 32) bn /= 2;
     if (ctas() < 2 * 152) rb = 2;
     if (in.h % rb != 0) return false;
-    const dim3 grid(in.w / 128, in.h / rb, cout_p / bn);
+    const dim3 grid(in.w / 128, nb * in.h / rb, cout_p / bn);
 #define VK_ROWS(B, CI, R)                                                                     \
   if (bn == B && cin == CI && rb == R) {                                                      \
     launch_rows<B, CI, R>(grid, in, w, bias, cout, relu, ob, cout_p, of, nout);               \
@@ -855,11 +912,11 @@ class Net {
       cudaFuncSetAttribute(k_conv<BN>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
       attr = true;
     }
-    k_conv<BN><<<grid, 128, smem, st>>>(in.d, in.h, in.w, in.c, w, bias, cout, relu, ob, ldo, of, nout, err);
+    k_conv<BN><<<grid, 128, smem, st>>>(in.d, in.h, in.w, nb, in.c, w, bias, cout, relu, ob, ldo, of, nout, err);
   }
   // dW GEMM (and, with db, the bias gradient of the nb real channels).
-  void wgrad(const Tensor& in, const bf16* dy, int coutp, float* out, float* db, int nb) {
-    const int npix = in.h * in.w, M = 9 * in.c;
+  void wgrad(const Tensor& in, const bf16* dy, int coutp, float* out, float* db, int nbias) {
+    const int npix = nb * in.h * in.w, M = 9 * in.c;
     const int mt = (M + 127) / 128;
     int ppc = 8192;
     while ((npix + ppc - 1) / ppc * mt < 8 * 152 && ppc > 256) ppc /= 2;
@@ -867,28 +924,28 @@ class Net {
     const size_t smem = 2 * (128 * 64 * 2 + (size_t)coutp * 64 * 2);
     cudaMemsetAsync(out, 0, sizeof(float) * (size_t)M * coutp, st);
     switch (coutp) {
-      case 16: launch_wgrad<16, 2>(grid, smem, in, dy, ppc, out, db, nb); break;
-      case 32: launch_wgrad<32, 2>(grid, smem, in, dy, ppc, out, db, nb); break;
-      case 64: launch_wgrad<64, 2>(grid, smem, in, dy, ppc, out, db, nb); break;
-      case 128: launch_wgrad<128, 2>(grid, smem, in, dy, ppc, out, db, nb); break;
-      default: launch_wgrad<256, 1>(grid, smem, in, dy, ppc, out, db, nb); break;
+      case 16: launch_wgrad<16, 2>(grid, smem, in, dy, ppc, out, db, nbias); break;
+      case 32: launch_wgrad<32, 2>(grid, smem, in, dy, ppc, out, db, nbias); break;
+      case 64: launch_wgrad<64, 2>(grid, smem, in, dy, ppc, out, db, nbias); break;
+      case 128: launch_wgrad<128, 2>(grid, smem, in, dy, ppc, out, db, nbias); break;
+      default: launch_wgrad<256, 1>(grid, smem, in, dy, ppc, out, db, nbias); break;
     }
   }
   template <int BN, int DEPTH>
-  void launch_wgrad(dim3 grid, size_t smem, const Tensor& in, const bf16* dy, int ppc, float* out, float* db, int nb) {
+  void launch_wgrad(dim3 grid, size_t smem, const Tensor& in, const bf16* dy, int ppc, float* out, float* db, int nbias) {
     static bool attr = false;
     if (!attr) {
       cudaFuncSetAttribute(k_wgrad<BN, DEPTH>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
       attr = true;
     }
-    k_wgrad<BN, DEPTH><<<grid, 128, smem, st>>>(in.d, dy, in.h, in.w, in.c, ppc, out, db, nb, err);
+    k_wgrad<BN, DEPTH><<<grid, 128, smem, st>>>(in.d, dy, in.h, in.w, nb, in.c, ppc, out, db, nbias, err);
   }
   static int blocks(size_t n) { return (int)std::min<size_t>((n + 255) / 256, 152 * 16); }
 
   // Forward pass; returns the head output in out_f [p][2].
   void forward(const float* input) {
     const int npix = H * W;
-    k_pack_input<<<blocks((size_t)npix * 16), 256, 0, st>>>(input, x0.d, npix, 3, 16);
+    k_pack_input<<<blocks((size_t)nb * npix * 16), 256, 0, st>>>(input, x0.d, npix, nb, 3, 16);
     int ci = 0;
     const Tensor* cur = &x0;
     for (int l = 0; l < levels; ++l) {
@@ -897,16 +954,16 @@ class Net {
       const Conv& c2 = convs[ci++];
       conv(a[l], c2.wb, c2.coutp, c2.cout, param + c2.boff, 1, s[l].d, nullptr, 0);
       if (l + 1 < levels) {
-        k_pool<<<blocks(p[l].n()), 256, 0, st>>>(s[l].d, p[l].d, s[l].h, s[l].w, s[l].c);
+        k_pool<<<blocks(N(p[l])), 256, 0, st>>>(s[l].d, p[l].d, nb * s[l].h, s[l].w, s[l].c);
         cur = &p[l];
       }
     }
     const Tensor* dec = &s[levels - 1];
     for (int l = levels - 2; l >= 0; --l) {
-      k_up<<<blocks(u[l].n()), 256, 0, st>>>(dec->d, u[l].d, u[l].h, u[l].w, u[l].c);
+      k_up<<<blocks(N(u[l])), 256, 0, st>>>(dec->d, u[l].d, nb * u[l].h, u[l].w, u[l].c);
       const Conv& c1 = convs[ci++];
       conv(u[l], c1.wb, c1.coutp, c1.cout, param + c1.boff, 1, c[l].d, nullptr, 0);
-      k_add<<<blocks(e[l].n()), 256, 0, st>>>(c[l].d, s[l].d, e[l].d, e[l].n());
+      k_add<<<blocks(N(e[l])), 256, 0, st>>>(c[l].d, s[l].d, e[l].d, N(e[l]));
       const Conv& c2 = convs[ci++];
       conv(e[l], c2.wb, c2.coutp, c2.cout, param + c2.boff, 1, d[l].d, nullptr, 0);
       dec = &d[l];
@@ -918,7 +975,7 @@ class Net {
   // Backward of conv `cv` whose input is `in` and (post-activation) output
   // `out`: dpost -> (ReLU mask) -> wgrad (+bias grad) -> dgrad into din.
   void conv_bwd(const Conv& cv, const Tensor& in, const bf16* out, const bf16* dpost, bf16* dpre_scratch, bf16* din) {
-    const size_t nout = (size_t)in.h * in.w * cv.coutp;
+    const size_t nout = (size_t)nb * in.h * in.w * cv.coutp;
     const bf16* dpre = dpost;
     if (cv.relu) {
       k_relu_bwd<<<blocks(nout), 256, 0, st>>>(out, dpost, dpre_scratch, nout);
@@ -942,7 +999,7 @@ class Net {
     const int npix = H * W;
     cudaMemsetAsync(grad, 0, sizeof(float) * nparam, st);
     cudaMemsetAsync(loss, 0, sizeof(double), st);
-    k_loss<<<blocks((size_t)npix * 16), 256, 0, st>>>(out_f, target, npix, 2, 16, dhead.d, loss);
+    k_loss<<<blocks((size_t)nb * npix * 16), 256, 0, st>>>(out_f, target, npix, nb, 2, 16, dhead.d, loss);
     int ci = (int)convs.size() - 1;
     // head
     const Tensor* dec = levels > 1 ? &d[0] : &s[0];
@@ -955,8 +1012,8 @@ class Net {
       conv_bwd(convs[ci--], u[l], c[l].d, g3[l].d, g2[l].d, g1[l].d);  // g1[l] = d u[l] (channels base<<(l+1))
       // up backward -> gradient of the coarser decoder output (or s[levels-1])
       bf16* gnext = g1[l + 1].d;
-      k_up_bwd<<<blocks((size_t)(H >> (l + 1)) * (W >> (l + 1)) * (base << (l + 1))), 256, 0, st>>>(
-          g1[l].d, gnext, H >> l, W >> l, base << (l + 1));
+      k_up_bwd<<<blocks((size_t)nb * (H >> (l + 1)) * (W >> (l + 1)) * (base << (l + 1))), 256, 0, st>>>(
+          g1[l].d, gnext, nb * (H >> l), W >> l, base << (l + 1));
       // stash d e[l] for the encoder skip in g3[l] (kept), continue with gnext
       gcur = gnext;
     }
@@ -967,8 +1024,8 @@ class Net {
       if (l < levels - 1) {
         // d s[l] = pool_bwd(d p[l]) + d e[l] (the skip, stashed in g3[l]);
         // d p[l] sits in g2[l], so the result goes to g1[l]
-        k_pool_bwd<<<blocks(s[l].n()), 256, 0, st>>>(gcur, g1[l].d, s[l].h, s[l].w, s[l].c);
-        k_add<<<blocks(s[l].n()), 256, 0, st>>>(g1[l].d, g3[l].d, g1[l].d, s[l].n());
+        k_pool_bwd<<<blocks(N(s[l])), 256, 0, st>>>(gcur, g1[l].d, nb * s[l].h, s[l].w, s[l].c);
+        k_add<<<blocks(N(s[l])), 256, 0, st>>>(g1[l].d, g3[l].d, g1[l].d, N(s[l]));
         ds = g1[l].d;
       }
       const int cs = 2 * l + 1, ca = 2 * l;
@@ -1030,14 +1087,20 @@ Net* as_net(void* h) {
 }  // namespace
 
 extern "C" int vk_nn_create(int32_t h, int32_t w, int32_t base, int32_t levels, uint64_t seed, void** net) {
-  if (!net || h <= 0 || w <= 0 || base < 16 || base % 16 || levels < 1 || levels > 5 || (h >> (levels - 1)) < 2 ||
+  return vk_nn_create_batched(h, w, base, levels, 1, seed, net);
+}
+
+extern "C" int vk_nn_create_batched(int32_t h, int32_t w, int32_t base, int32_t levels, int32_t batch_cap,
+                                    uint64_t seed, void** net) {
+  if (!net || batch_cap < 1 || batch_cap > 64 || h <= 0 || w <= 0 || base < 16 || base % 16 || levels < 1 || levels > 5 || (h >> (levels - 1)) < 2 ||
       (w >> (levels - 1)) < 2 || (h % (1 << (levels - 1))) || (w % (1 << (levels - 1))) || (base << (levels - 1)) > 256) {
-    set_error("vk_nn_create: need h, w divisible by 2^(levels-1), base a multiple of 16, base*2^(levels-1) <= 256");
+    set_error("vk_nn_create: need h, w divisible by 2^(levels-1), base a multiple of 16, base*2^(levels-1) <= 256, "
+              "batch capacity 1..64");
     return VK_E_INVALID;
   }
   *net = nullptr;
   Net* n = new Net();
-  const int rc = n->init(h, w, base, levels, seed);
+  const int rc = n->init(h, w, base, levels, seed, batch_cap);
   if (rc != VK_OK) {
     delete n;
     set_error("vk_nn_create: allocation failed");
@@ -1045,6 +1108,34 @@ extern "C" int vk_nn_create(int32_t h, int32_t w, int32_t base, int32_t levels, 
   }
   *net = new NetCtx{kNetMagic, n};
   return n->check();
+}
+
+extern "C" int vk_nn_set_batch(void* net, int32_t batch) {
+  Net* x = as_net(net);
+  if (!x) return VK_E_INVALID;
+  if (batch < 1 || batch > x->bcap) { set_error("vk_nn_set_batch: batch outside 1..capacity"); return VK_E_INVALID; }
+  x->nb = batch;
+  return VK_OK;
+}
+
+extern "C" int vk_nn_features(void* net, const double* psi_host, const double* pos_host, int32_t n_vort,
+                              double width, float* out_dev) {
+  Net* x = as_net(net);
+  if (!x || !psi_host || !out_dev || (n_vort > 0 && !pos_host) || n_vort < 0 || n_vort > Net::kMaxVortices ||
+      !(width > 0)) {
+    set_error("vk_nn_features: bad argument (null pointer, vortex count outside 0..4096 or width <= 0)");
+    return VK_E_INVALID;
+  }
+  const int npix = x->H * x->W;
+  cudaMemcpyAsync(x->feat_psi, psi_host, sizeof(double2) * npix, cudaMemcpyHostToDevice, x->st);
+  if (n_vort > 0) {
+    cudaMemcpyAsync(x->feat_pos, pos_host, sizeof(double) * 2 * n_vort, cudaMemcpyHostToDevice, x->st);
+    vk::nn::k_feat_tables<<<Net::blocks((size_t)n_vort * (x->W + x->H)), 256, 0, x->st>>>(
+        x->feat_pos, n_vort, x->H, x->W, 1.0 / (2.0 * width * width), x->feat_gx, x->feat_gy);
+  }
+  vk::nn::k_features<<<Net::blocks((size_t)npix), 256, 0, x->st>>>(x->feat_psi, x->feat_gx, x->feat_gy, n_vort,
+                                                                    x->H, x->W, out_dev);
+  return x->check();
 }
 
 extern "C" int vk_nn_destroy(void* net) {
@@ -1085,7 +1176,7 @@ extern "C" int vk_nn_forward(void* net, const float* in_dev, float* out_dev, voi
   (void)stream;
   x->forward(in_dev);
   const int npix = x->H * x->W;
-  vk::nn::k_planar2<<<Net::blocks((size_t)npix), 256, 0, x->st>>>(x->out_f, out_dev, npix);
+  vk::nn::k_planar2<<<Net::blocks((size_t)x->nb * npix), 256, 0, x->st>>>(x->out_f, out_dev, npix, x->nb);
   return x->check();
 }
 

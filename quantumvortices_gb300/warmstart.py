@@ -18,13 +18,21 @@ from . import vk
 
 
 class WarmStartNet:
-    def __init__(self, h: int, w: int, base: int = 32, levels: int = 4, seed: int = 1):
+    """The network; batch > 1 sizes it for batches of that many images
+    (forward / loss_grad / train_step then take the images set by
+    set_batch, [b][3][h][w] inputs and [b][2][h][w] targets)."""
+
+    def __init__(self, h: int, w: int, base: int = 32, levels: int = 4, seed: int = 1, batch: int = 1):
         self.lib = vk.load_library()
         L = self.lib
         dp, vp = C.POINTER(C.c_double), C.c_void_p
         fp = C.POINTER(C.c_float)
         for name, res, args in [
             ("vk_nn_create", C.c_int, [C.c_int32, C.c_int32, C.c_int32, C.c_int32, C.c_uint64, C.POINTER(vp)]),
+            ("vk_nn_create_batched", C.c_int, [C.c_int32, C.c_int32, C.c_int32, C.c_int32, C.c_int32, C.c_uint64,
+                                               C.POINTER(vp)]),
+            ("vk_nn_set_batch", C.c_int, [vp, C.c_int32]),
+            ("vk_nn_features", C.c_int, [vp, dp, dp, C.c_int32, C.c_double, C.c_void_p]),
             ("vk_nn_destroy", C.c_int, [vp]),
             ("vk_nn_num_params", C.c_int, [vp, C.POINTER(C.c_int64)]),
             ("vk_nn_get_params", C.c_int, [vp, fp, C.c_int64]),
@@ -36,8 +44,9 @@ class WarmStartNet:
             f = getattr(L, name)
             f.restype, f.argtypes = res, args
         self.h, self.w, self.base, self.levels = h, w, base, levels
+        self.capacity, self.batch = batch, batch
         hnd = C.c_void_p()
-        vk._check(L.vk_nn_create(h, w, base, levels, seed, C.byref(hnd)), "vk_nn_create")
+        vk._check(L.vk_nn_create_batched(h, w, base, levels, batch, seed, C.byref(hnd)), "vk_nn_create_batched")
         self._h = hnd
         n = C.c_int64()
         vk._check(L.vk_nn_num_params(self._h, C.byref(n)), "vk_nn_num_params")
@@ -53,6 +62,19 @@ class WarmStartNet:
             self.close()
         except Exception:
             pass
+
+    def set_batch(self, b: int) -> None:
+        vk._check(self.lib.vk_nn_set_batch(self._h, int(b)), "vk_nn_set_batch")
+        self.batch = int(b)
+
+    def features(self, psi: np.ndarray, pos: np.ndarray, width: float, out_dev) -> None:
+        """Input features of one image on the GPU (vk_nn_features): out_dev, a
+        CUDA float32 tensor [3,h,w], gets Re/Im psi and the signed Gaussian
+        vortex-charge density of the positions pos[n, 2] (+ for the first half)."""
+        a = np.ascontiguousarray(psi, dtype=np.complex128)
+        q = np.ascontiguousarray(pos, dtype=np.float64).reshape(-1, 2)
+        vk._check(self.lib.vk_nn_features(self._h, vk._dptr(a.view(np.float64)), vk._dptr(q), len(q), float(width),
+                                          out_dev.data_ptr()), "vk_nn_features")
 
     def get_params(self) -> np.ndarray:
         a = np.empty(self.nparam, dtype=np.float32)
@@ -81,42 +103,9 @@ class WarmStartNet:
         return float(loss.value) if want_loss else None
 
 
-def features(n: int, pos: np.ndarray, psi_ansatz: np.ndarray, width: float) -> np.ndarray:
-    """[3, n, n]: Re/Im of the ansatz and a signed vortex-charge density
-    (periodic Gaussians of the given width, + for the first half of `pos`)."""
-    nv = len(pos)
-    x = np.arange(n) * 2 * np.pi / n
-    X, Y = np.meshgrid(x, x)
-    q = np.zeros((n, n))
-    for j in range(nv):
-        dx = (X - pos[j, 0] + np.pi) % (2 * np.pi) - np.pi
-        dy = (Y - pos[j, 1] + np.pi) % (2 * np.pi) - np.pi
-        q += (1.0 if j < nv // 2 else -1.0) * np.exp(-(dx * dx + dy * dy) / (2 * width * width))
-    return np.stack([psi_ansatz.real, psi_ansatz.imag, q]).astype(np.float32)
-
-
 def _torch():
     import torch  # device memory and plumbing only; the network runs in libvk
     return torch
-
-
-def features_device(n: int, pos: np.ndarray, psi_ansatz, width: float):
-    """features() on the GPU with torch tensors (psi_ansatz: complex numpy)."""
-    torch = _torch()
-    nv = len(pos)
-    x = torch.arange(n, device="cuda", dtype=torch.float32) * (2 * math.pi / n)
-    q = torch.zeros((n, n), device="cuda", dtype=torch.float32)
-    if nv:
-        px = torch.tensor(pos[:, 0], device="cuda", dtype=torch.float32)[:, None]
-        py = torch.tensor(pos[:, 1], device="cuda", dtype=torch.float32)[:, None]
-        sg = torch.tensor([1.0 if j < nv // 2 else -1.0 for j in range(nv)], device="cuda")[:, None, None]
-        dx = torch.remainder(x[None, :] - px + math.pi, 2 * math.pi) - math.pi   # [nv, n] along x
-        dy = torch.remainder(x[None, :] - py + math.pi, 2 * math.pi) - math.pi   # [nv, n] along y
-        gx = torch.exp(-dx * dx / (2 * width * width))
-        gy = torch.exp(-dy * dy / (2 * width * width))
-        q = (sg * gy[:, :, None] * gx[:, None, :]).sum(0)
-    a = torch.from_numpy(np.stack([psi_ansatz.real, psi_ansatz.imag]).astype(np.float32)).cuda()
-    return torch.cat([a, q[None]], 0).contiguous()
 
 
 class DataGen:
@@ -134,15 +123,19 @@ class DataGen:
         pos = self.solver.set_psi_vortices(nv, seed, self.xi0, min_sep=4 * self.xi0)
         return pos, self.solver.get_psi()
 
-    def sample(self, nv: int, seed: int):
+    def sample(self, nv: int, seed: int, net: "WarmStartNet"):
+        """(features [3,n,n], relaxed - ansatz [2,n,n]) as CUDA float32 tensors;
+        the features come from the network's feature kernel."""
         torch = _torch()
         pos, psi0 = self.ansatz(nv, seed)
         self.solver.argle(self.relax)
-        # relaxed state = F^-1[kpsi] (psi itself is one step behind after ARGLE)
-        kpsi = self.solver.get_kpsi()
-        relaxed = np.fft.ifft2(kpsi.T)
-        feat = features_device(self.n, pos, psi0, self.width)
-        tgt = torch.from_numpy(np.stack([(relaxed - psi0).real, (relaxed - psi0).imag]).astype(np.float32)).cuda()
+        # relaxed state = F^-1[kpsi] (psi itself is one step behind after
+        # ARGLE): vk_set_kpsi transforms it on the device
+        self.solver.set_kpsi(self.solver.get_kpsi())
+        d = self.solver.get_psi() - psi0
+        feat = torch.empty((3, self.n, self.n), dtype=torch.float32, device="cuda")
+        net.features(psi0, pos, self.width, feat)
+        tgt = torch.from_numpy(np.stack([d.real, d.imag]).astype(np.float32)).cuda()
         return feat, tgt
 
     def close(self):
@@ -153,35 +146,59 @@ def vortex_count(rng) -> int:
     return int(rng.integers(4, 65)) * 2  # 8..128, even (neutral)
 
 
-def train(net: WarmStartNet, gen: DataGen, n_train: int, epochs: int, lr: float, seed0: int = 10_000,
-          log=print):
-    """Generates n_train samples (seeds seed0..seed0+n_train-1) and trains."""
+def generate(net: WarmStartNet, gen: DataGen, n_train: int, seed0: int = 10_000, log=print):
+    """n_train solver-generated samples (seeds seed0..seed0+n_train-1), kept on
+    the GPU as float16 [n_train, 3, n, n] features and [n_train, 2, n, n]
+    targets (the network rounds its input to BF16 anyway)."""
     torch = _torch()
     rng = np.random.default_rng(seed0)
-    data = []
+    n = gen.n
+    feats = torch.empty((n_train, 3, n, n), dtype=torch.float16, device="cuda")
+    tgts = torch.empty((n_train, 2, n, n), dtype=torch.float16, device="cuda")
     t0 = time.perf_counter()
     for i in range(n_train):
-        data.append(gen.sample(vortex_count(rng), seed0 + i))
+        f, t = gen.sample(vortex_count(rng), seed0 + i, net)
+        feats[i] = f
+        tgts[i] = t
     torch.cuda.synchronize()
     tgen = time.perf_counter() - t0
-    log(f"generated {n_train} ARGLE-relaxed {gen.n}^2 samples in {tgen:.1f} s")
+    log(f"generated {n_train} ARGLE-relaxed {n}^2 samples in {tgen:.1f} s")
+    return feats, tgts, tgen
+
+
+def train(net: WarmStartNet, gen: DataGen, n_train: int, epochs: int, lr: float, seed0: int = 10_000,
+          log=print, data=None):
+    """Generates n_train samples (or takes data = (feats, tgts, gen_s)) and
+    trains with batches of net.capacity images: one Adam step per batch, the
+    learning rate halved every epoch."""
+    torch = _torch()
+    feats, tgts, tgen = data if data is not None else generate(net, gen, n_train, seed0, log)
+    n_train = feats.shape[0]
+    B = net.capacity
+    net.set_batch(B)
+    rng = np.random.default_rng(seed0 + 1)
     t0 = time.perf_counter()
     hist = []
-    order = np.arange(n_train)
+    nstep = 0
     for ep in range(epochs):
-        rng.shuffle(order)
-        tot = 0.0
-        for k, i in enumerate(order):
-            l = net.train_step(data[i][0], data[i][1], lr * (0.5 ** ep), want_loss=(k % 16 == 0))
+        order = torch.from_numpy(rng.permutation(n_train)).cuda()
+        tot, cnt = 0.0, 0
+        for k in range(0, n_train - B + 1, B):
+            idx = order[k:k + B]
+            xb = feats.index_select(0, idx).float()
+            yb = tgts.index_select(0, idx).float()
+            l = net.train_step(xb, yb, lr * (0.5 ** ep), want_loss=(nstep % 16 == 0))
+            nstep += 1
             if l is not None:
                 tot += l
-        hist.append(tot / max(1, (n_train + 15) // 16))
+                cnt += 1
+        hist.append(tot / max(1, cnt))
         log(f"epoch {ep}: mean sampled loss {hist[-1]:.4e}")
     torch.cuda.synchronize()
     ts = time.perf_counter() - t0
-    fl = train_flops(net)
-    return {"gen_s": tgen, "train_s": ts, "loss": hist, "flops_per_step": fl,
-            "tensor_tflops": fl * n_train * epochs / ts / 1e12}
+    fl = train_flops(net) * B
+    return {"gen_s": tgen, "train_s": ts, "loss": hist, "flops_per_step": fl, "batch": B, "steps": nstep,
+            "tensor_tflops": fl * nstep / ts / 1e12}
 
 
 def train_flops(net: WarmStartNet) -> float:
@@ -245,7 +262,9 @@ def evaluate(net: WarmStartNet, gen: DataGen, seeds, log=print):
     out = []
     s = gen.solver
     n = gen.n
+    net.set_batch(1)
     corr = torch.empty((2, n, n), device="cuda", dtype=torch.float32)
+    feat = torch.empty((3, n, n), device="cuda", dtype=torch.float32)
     for seed in seeds:
         nv = vortex_count(rng)
         pos, psi0 = gen.ansatz(nv, seed)
@@ -254,9 +273,9 @@ def evaluate(net: WarmStartNet, gen: DataGen, seeds, log=print):
         e_plain, f_plain = d.etot, _grand(d)
         gen.ansatz(nv, seed)
         k_plain, _ = steps_to(s, r_target, gen.relax)
-        feat = features_device(n, pos, psi0, gen.width)
         torch.cuda.synchronize()
         t0 = time.perf_counter()
+        net.features(psi0, pos, gen.width, feat)
         net.forward(feat, corr)
         c = corr.cpu().numpy()
         t_net = time.perf_counter() - t0
@@ -316,10 +335,11 @@ def main(argv=None):
     ap.add_argument("--base", type=int, default=32)
     ap.add_argument("--levels", type=int, default=4)
     ap.add_argument("--lr", type=float, default=1e-3)
+    ap.add_argument("--batch", type=int, default=8)
     ap.add_argument("--out", default=None)
     a = ap.parse_args(argv)
     gen = DataGen(a.n, a.relax)
-    net = WarmStartNet(a.n, a.n, a.base, a.levels, seed=1)
+    net = WarmStartNet(a.n, a.n, a.base, a.levels, seed=1, batch=a.batch)
     tr = train(net, gen, a.train, a.epochs, a.lr)
     held = list(range(900_000, 900_000 + a.eval))  # disjoint from the training seeds
     rows = evaluate(net, gen, held)

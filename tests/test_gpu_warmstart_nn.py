@@ -1,6 +1,8 @@
 """tcgen05 BF16 network kernels (forward, data and weight gradients) against
 the CPU restatement oracle/nn_oracle.py, which mirrors the BF16 rounding
-points; tolerances are relative L2: output 1e-2, gradient 2e-2 (BF16)."""
+points; tolerances are relative L2: output 3e-3, full gradient 1e-2 (BF16
+products, FP32 sums in another order).  Batched calls against single-image
+calls, and the feature kernel against its numpy restatement."""
 import numpy as np
 import pytest
 
@@ -30,7 +32,7 @@ def test_forward_matches_oracle(h, base, levels):
     out = torch.empty((2, h, h), dtype=torch.float32, device="cuda")
     net.forward(di, out)
     ref, _ = nn_oracle.forward(net.get_params().astype(np.float64), inp.astype(np.float64), base, levels)
-    assert rel(out.cpu().numpy(), ref) < 1e-2
+    assert rel(out.cpu().numpy(), ref) < 3e-3
     net.close()
 
 
@@ -41,8 +43,8 @@ def test_gradient_matches_oracle(h, base, levels):
     loss, g = net.loss_grad(di, dt)
     rloss, rg = nn_oracle.loss_grad(net.get_params().astype(np.float64), inp.astype(np.float64),
                                     tgt.astype(np.float64), base, levels)
-    assert abs(loss - rloss) <= 1e-2 * rloss
-    assert rel(g, rg) < 2e-2
+    assert abs(loss - rloss) <= 3e-3 * rloss
+    assert rel(g, rg) < 1e-2
     # per layer
     o = 0
     for ci, co, _ in nn_oracle.layers(base, levels):
@@ -76,11 +78,11 @@ def test_row_block_conv_matches_oracle(h, base, levels):
     net.forward(di, out)
     prm = net.get_params().astype(np.float64)
     ref, _ = nn_oracle.forward(prm, inp.astype(np.float64), base, levels)
-    assert rel(out.cpu().numpy(), ref) < 1e-2
+    assert rel(out.cpu().numpy(), ref) < 3e-3
     loss, g = net.loss_grad(di, dt)
     rloss, rg = nn_oracle.loss_grad(prm, inp.astype(np.float64), tgt.astype(np.float64), base, levels)
-    assert abs(loss - rloss) <= 1e-2 * rloss
-    assert rel(g, rg) < 2e-2
+    assert abs(loss - rloss) <= 3e-3 * rloss
+    assert rel(g, rg) < 1e-2
     net.close()
 
 
@@ -106,3 +108,45 @@ def test_row_block_conv_matches_generic_kernel_at_512():
         net.close()
     (o0, l0, g0), (o1, l1, g1) = res
     assert rel(o1, o0) < 1e-3 and abs(l1 - l0) <= 1e-3 * l0 and rel(g1, g0) < 1e-3
+
+
+@pytest.mark.parametrize("h,base,levels", [(64, 16, 3), (128, 32, 2)])
+def test_batched_calls_match_single_image_calls(h, base, levels):
+    """A batch of 3 images: each image's output equals its single-image
+    forward, and the batch gradient is the mean of the single-image
+    gradients (the batch loss is the mean over the images)."""
+    torch = pytest.importorskip("torch")
+    net = WarmStartNet(h, h, base, levels, seed=13, batch=3)
+    data = [_data(h, seed=20 + i) for i in range(3)]
+    xb = torch.stack([d[2] for d in data]).contiguous()
+    yb = torch.stack([d[3] for d in data]).contiguous()
+    out = torch.empty((3, 2, h, h), dtype=torch.float32, device="cuda")
+    net.forward(xb, out)
+    lb, gb = net.loss_grad(xb, yb)
+    net.set_batch(1)
+    one = torch.empty((2, h, h), dtype=torch.float32, device="cuda")
+    gs, ls = [], []
+    for i, d in enumerate(data):
+        net.forward(d[2], one)
+        assert rel(out[i].cpu().numpy(), one.cpu().numpy()) < 1e-5
+        l1, g1 = net.loss_grad(d[2], d[3])
+        ls.append(l1)
+        gs.append(g1)
+    assert abs(lb - np.mean(ls)) <= 1e-5 * lb
+    assert rel(gb, np.mean(gs, axis=0)) < 1e-4
+    net.close()
+
+
+def test_feature_kernel_matches_numpy():
+    torch = pytest.importorskip("torch")
+    h = 128
+    net = WarmStartNet(h, h, 16, 2, seed=1)
+    rng = np.random.default_rng(6)
+    psi = rng.standard_normal((h, h)) + 1j * rng.standard_normal((h, h))
+    pos = rng.uniform(0, 2 * np.pi, (10, 2))
+    width = 2 * np.sqrt(2) * 2 * np.pi / h
+    out = torch.empty((3, h, h), dtype=torch.float32, device="cuda")
+    net.features(psi, pos, width, out)
+    ref = nn_oracle.features(h, h, pos, psi, width)
+    assert rel(out.cpu().numpy(), ref) < 1e-6
+    net.close()
