@@ -328,7 +328,7 @@ __device__ __forceinline__ void x1_body(const cplx<T>* __restrict__ Ta, cplx<T>*
     const int p = e / L, x = e % L;
     const C a = s[(2 * p) * G::LP + pidx(x)], b = s[(2 * p + 1) * G::LP + pidx(x)];
     const T bg = T(c.rho_bg);
-    z[q] = mkc<T>(a.x * a.x + a.y * a.y - bg, b.x * b.x + b.y * b.y - bg);
+    z[q] = mkc<T>(fma(a.x, a.x, fma(a.y, a.y, -bg)), fma(b.x, b.x, fma(b.y, b.y, -bg)));
   }
   __syncthreads();
 #pragma unroll
@@ -393,7 +393,7 @@ __device__ __forceinline__ void x1_single_body(const cplx<T>* __restrict__ Ta, c
   for (int q = 0; q < PER; ++q) {
     const int n = threadIdx.x + q * G::NT;
     const C a = s[pidx(2 * n)], b = s[pidx(2 * n + 1)];
-    z[q] = mkc<T>(a.x * a.x + a.y * a.y - bg, b.x * b.x + b.y * b.y - bg);
+    z[q] = mkc<T>(fma(a.x, a.x, fma(a.y, a.y, -bg)), fma(b.x, b.x, fma(b.y, b.y, -bg)));
   }
   __syncthreads();
 #pragma unroll
@@ -490,16 +490,14 @@ __device__ __forceinline__ void x2_body(const cplx<T>* __restrict__ Tc, const cp
   fft_rows<T, L, NPAIR, G::NT, +1, G::NT>(s, tw);
   constexpr int PER = G::R * L / G::NT;
   C nv[PER];
-  const T gs = T(SIGN * c.g);
-  const T scale = T(c.scale);
+  const T gsc = T(SIGN * c.g * c.scale);  // g and the 1/(nx ny) of the inverse transform
 #pragma unroll
   for (int q = 0; q < PER; ++q) {
     const int e = threadIdx.x + q * G::NT;
     const int r = e / L, x = e % L;
     const C z = s[(r >> 1) * G::LP + pidx(x)];
-    const T pg = ((r & 1) == 0 ? z.x : z.y) * scale;  // P_G[|psi|^2](x, y0+r)
     const C ps = psi[(size_t)(y0 + r) * L + x];
-    const T gp = gs * pg;
+    const T gp = gsc * ((r & 1) == 0 ? z.x : z.y);  // SIGN g P_G[|psi|^2](x, y0+r)
     C n = mkc<T>(gp * ps.x, gp * ps.y);
     if (POT) {
       const T v = T(SIGN) * vpot[(size_t)(y0 + r) * L + x];
@@ -563,15 +561,13 @@ __device__ __forceinline__ void x2_single_body(const cplx<T>* __restrict__ Tc, c
   fft_rows<T, H, 1, NH, +1, G::NT, 2>(s, tw);
   constexpr int PER = L / G::NT;
   C nv[PER];
-  const T gs = T(SIGN * c.g);
-  const T scale = T(c.scale);
+  const T gsc = T(SIGN * c.g * c.scale);  // g and the 1/(nx ny) of the inverse transform
 #pragma unroll
   for (int q = 0; q < PER; ++q) {
     const int x = threadIdx.x + q * G::NT;
     const C z = s[pidx(x >> 1)];
-    const T pg = ((x & 1) == 0 ? z.x : z.y) * scale;  // P_G[|psi|^2](x, y)
     const C ps = psi[(size_t)y * L + x];
-    const T gp = gs * pg;
+    const T gp = gsc * ((x & 1) == 0 ? z.x : z.y);  // SIGN g P_G[|psi|^2](x, y)
     C n = mkc<T>(gp * ps.x, gp * ps.y);
     if (POT) {
       const T v = T(SIGN) * vpot[(size_t)y * L + x];
