@@ -37,8 +37,10 @@ template <typename T, int LL, int RL> struct GeoB {
     default: break;                                 \
   }
 
-template <typename T, int RL, bool FROM_T>
-__global__ void __launch_bounds__(RL / 16) kb_x1(const Field<T>* __restrict__ F, const int2* __restrict__ items, int n) {
+// MB > 1: the compiler keeps the registers low enough for MB CTAs per SM
+// (a variant the autotuner times against the uncapped one).
+template <typename T, int RL, bool FROM_T, int MB = 1>
+__global__ void __launch_bounds__(RL / 16, MB) kb_x1(const Field<T>* __restrict__ F, const int2* __restrict__ items, int n) {
   extern __shared__ __align__(16) unsigned char smraw[];
   cplx<T>* s = reinterpret_cast<cplx<T>*>(smraw);
   for (int it = blockIdx.x; it < n; it += gridDim.x) {
@@ -49,8 +51,8 @@ __global__ void __launch_bounds__(RL / 16) kb_x1(const Field<T>* __restrict__ F,
   }
 }
 
-template <typename T, int RL>
-__global__ void __launch_bounds__(RL / 16) kb_y1(const Field<T>* __restrict__ F, const int2* __restrict__ items, int n) {
+template <typename T, int RL, int MB = 1>
+__global__ void __launch_bounds__(RL / 16, MB) kb_y1(const Field<T>* __restrict__ F, const int2* __restrict__ items, int n) {
   extern __shared__ __align__(16) unsigned char smraw[];
   cplx<T>* s = reinterpret_cast<cplx<T>*>(smraw);
   for (int it = blockIdx.x; it < n; it += gridDim.x) {
@@ -61,8 +63,8 @@ __global__ void __launch_bounds__(RL / 16) kb_y1(const Field<T>* __restrict__ F,
   }
 }
 
-template <typename T, int RL>
-__global__ void __launch_bounds__(RL / 16) kb_x2(const Field<T>* __restrict__ F, const int2* __restrict__ items, int n) {
+template <typename T, int RL, int MB = 1>
+__global__ void __launch_bounds__(RL / 16, MB) kb_x2(const Field<T>* __restrict__ F, const int2* __restrict__ items, int n) {
   extern __shared__ __align__(16) unsigned char smraw[];
   cplx<T>* s = reinterpret_cast<cplx<T>*>(smraw);
   for (int it = blockIdx.x; it < n; it += gridDim.x) {
@@ -74,8 +76,8 @@ __global__ void __launch_bounds__(RL / 16) kb_x2(const Field<T>* __restrict__ F,
   }
 }
 
-template <typename T, int RL, int STAGE>
-__global__ void __launch_bounds__(RL / 16) kb_y2(const Field<T>* __restrict__ F, const int2* __restrict__ items, int n) {
+template <typename T, int RL, int STAGE, int MB = 1>
+__global__ void __launch_bounds__(RL / 16, MB) kb_y2(const Field<T>* __restrict__ F, const int2* __restrict__ items, int n) {
   extern __shared__ __align__(16) unsigned char smraw[];
   cplx<T>* s = reinterpret_cast<cplx<T>*>(smraw);
   for (int it = blockIdx.x; it < n; it += gridDim.x) {
@@ -115,6 +117,10 @@ class Ensemble {
   // work lists per pass kind and tile variant: [kind][variant]
   int2* dItems[EP_N][2] = {};
   int nItems[EP_N][2] = {};
+  // tile variants: 0 and 1 the tile sizes below (registers uncapped), 2 the
+  // tile of variant 0 with the registers capped for more CTAs per SM
+  static constexpr int NVAR = 3;
+  static int list_of(int v) { return v == 2 ? 0 : v; }
   int variant[EP_N] = {0, 0, 0, 0, 0};
   int grid[EP_N] = {0, 0, 0, 0, 0};
   int sms = 152;
@@ -167,8 +173,8 @@ class Ensemble {
     if (st) cudaStreamDestroy(st);
   }
 
-  static int rows_x(int L, int v) { return XRL[v] / L; }
-  static int rows_y(int L, int v) { return YRL[v] / L; }
+  static int rows_x(int L, int v) { return XRL[list_of(v)] / L; }
+  static int rows_y(int L, int v) { return YRL[list_of(v)] / L; }
 
   int build_lists() {
     for (int kind = 0; kind < EP_N; ++kind)
@@ -203,14 +209,18 @@ class Ensemble {
 
   template <typename K> void launch(K kern, int g, int threads, size_t smem, int kind, int v) {
     ensure_smem_attr((const void*)kern, smem);
-    kern<<<g, threads, smem, st>>>(dF, dItems[kind][v], nItems[kind][v]);
+    kern<<<g, threads, smem, st>>>(dF, dItems[kind][list_of(v)], nItems[kind][list_of(v)]);
     ++launches;
   }
 
   void pass(int kind, int stage, bool from_t, int v, int g) {
     constexpr size_t E = sizeof(C);
     if (kind == EP_X1) {
-      if (v == 0) {
+      if (v == 2) {
+        const size_t sm = E * 2048 * 17 / 16;
+        if (from_t) launch(kb_x1<T, 2048, true, 3>, g, 128, sm, kind, v);
+        else launch(kb_x1<T, 2048, false, 3>, g, 128, sm, kind, v);
+      } else if (v == 0) {
         const size_t sm = E * 2048 * 17 / 16;
         if (from_t) launch(kb_x1<T, 2048, true>, g, 128, sm, kind, v);
         else launch(kb_x1<T, 2048, false>, g, 128, sm, kind, v);
@@ -220,13 +230,24 @@ class Ensemble {
         else launch(kb_x1<T, 4096, false>, g, 256, sm, kind, v);
       }
     } else if (kind == EP_Y1) {
-      if (v == 0) launch(kb_y1<T, 1024>, g, 64, E * 1024 * 17 / 16, kind, v);
+      if (v == 2) launch(kb_y1<T, 1024, 6>, g, 64, E * 1024 * 17 / 16, kind, v);
+      else if (v == 0) launch(kb_y1<T, 1024>, g, 64, E * 1024 * 17 / 16, kind, v);
       else launch(kb_y1<T, 2048>, g, 128, E * 2048 * 17 / 16, kind, v);
     } else if (kind == EP_X2) {
-      if (v == 0) launch(kb_x2<T, 2048>, g, 128, E * 2048 * 17 / 16, kind, v);
+      if (v == 2) launch(kb_x2<T, 2048, 3>, g, 128, E * 2048 * 17 / 16, kind, v);
+      else if (v == 0) launch(kb_x2<T, 2048>, g, 128, E * 2048 * 17 / 16, kind, v);
       else launch(kb_x2<T, 4096>, g, 256, E * 4096 * 17 / 16, kind, v);
     } else if (kind == EP_Y2) {
       const size_t sm0 = E * 1024 * 17 / 16, sm1 = E * 2048 * 17 / 16;
+      if (v == 2) {
+        switch (stage) {
+          case 1: launch(kb_y2<T, 1024, 1, 6>, g, 64, sm0, kind, v); break;
+          case 2: launch(kb_y2<T, 1024, 2, 6>, g, 64, sm0, kind, v); break;
+          case 3: launch(kb_y2<T, 1024, 3, 6>, g, 64, sm0, kind, v); break;
+          default: launch(kb_y2<T, 1024, 4, 6>, g, 64, sm0, kind, v); break;
+        }
+        return;
+      }
       switch (stage) {
         case 1: v == 0 ? launch(kb_y2<T, 1024, 1>, g, 64, sm0, kind, v) : launch(kb_y2<T, 2048, 1>, g, 128, sm1, kind, v); break;
         case 2: v == 0 ? launch(kb_y2<T, 1024, 2>, g, 64, sm0, kind, v) : launch(kb_y2<T, 2048, 2>, g, 128, sm1, kind, v); break;
@@ -234,7 +255,7 @@ class Ensemble {
         default: v == 0 ? launch(kb_y2<T, 1024, 4>, g, 64, sm0, kind, v) : launch(kb_y2<T, 2048, 4>, g, 128, sm1, kind, v); break;
       }
     } else {
-      if (v == 0) launch(kb_xinv<T, 2048>, g, 128, E * 2048 * 17 / 16, kind, v);
+      if (v != 1) launch(kb_xinv<T, 2048>, g, 128, E * 2048 * 17 / 16, kind, v);
       else launch(kb_xinv<T, 4096>, g, 256, E * 4096 * 17 / 16, kind, v);
     }
   }
@@ -260,7 +281,7 @@ class Ensemble {
     report.clear();
     for (int kind = 0; kind < EP_N; ++kind) {
       float best = 1e30f;
-      for (int v = 0; v < 2; ++v)
+      for (int v = 0; v < (kind == EP_XINV ? 2 : NVAR); ++v)
         for (int k = 0; k < 4; ++k) {
           const int g = sms * per_sm[k];
           pass(kind, 2, true, v, g);  // warm
@@ -277,9 +298,9 @@ class Ensemble {
           }
         }
       char buf[160];
-      snprintf(buf, sizeof(buf), "%s: tile %d points, %d CTAs (%.1f us/launch); ", names[kind],
-               (kind == EP_Y1 || kind == EP_Y2) ? YRL[variant[kind]] : XRL[variant[kind]], grid[kind],
-               1e3f * best / 3.f);
+      snprintf(buf, sizeof(buf), "%s: tile %d points%s, %d CTAs (%.1f us/launch); ", names[kind],
+               (kind == EP_Y1 || kind == EP_Y2) ? YRL[list_of(variant[kind])] : XRL[list_of(variant[kind])],
+               variant[kind] == 2 ? " (registers capped)" : "", grid[kind], 1e3f * best / 3.f);
       report += buf;
     }
     cudaEventDestroy(a);
