@@ -20,7 +20,10 @@ from . import vk
 class WarmStartNet:
     """The network; batch > 1 sizes it for batches of that many images
     (forward / loss_grad / train_step then take the images set by
-    set_batch, [b][3][h][w] inputs and [b][2][h][w] targets)."""
+    set_batch, [b][3][h][w] inputs and [b][2][h][w] targets).  The network
+    runs on its own CUDA stream and every call returns with that stream
+    synchronised; tensors produced by torch kernels must be complete (e.g.
+    torch.cuda.current_stream().synchronize()) before they are passed in."""
 
     def __init__(self, h: int, w: int, base: int = 32, levels: int = 4, seed: int = 1, batch: int = 1):
         self.lib = vk.load_library()
@@ -160,6 +163,8 @@ def generate(net: WarmStartNet, gen: DataGen, n_train: int, seed0: int = 10_000,
         f, t = gen.sample(vortex_count(rng), seed0 + i, net)
         feats[i] = f
         tgts[i] = t
+        # the copies must finish before the network stream reuses f's memory
+        torch.cuda.current_stream().synchronize()
     torch.cuda.synchronize()
     tgen = time.perf_counter() - t0
     log(f"generated {n_train} ARGLE-relaxed {n}^2 samples in {tgen:.1f} s")
@@ -187,6 +192,8 @@ def train(net: WarmStartNet, gen: DataGen, n_train: int, epochs: int, lr: float,
             idx = order[k:k + B]
             xb = feats.index_select(0, idx).float()
             yb = tgts.index_select(0, idx).float()
+            # the network runs on its own stream: the batch must be complete
+            torch.cuda.current_stream().synchronize()
             l = net.train_step(xb, yb, lr * (0.5 ** ep), want_loss=(nstep % 16 == 0))
             nstep += 1
             if l is not None:

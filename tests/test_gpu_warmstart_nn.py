@@ -60,6 +60,7 @@ def test_training_reduces_loss():
     net = WarmStartNet(64, 64, 16, 3, seed=7)
     inp, _, di, _ = _data(64, seed=2)
     dt = (0.5 * di[:2]).contiguous()
+    torch.cuda.synchronize()  # the network reads it on its own stream
     l0 = net.train_step(di, dt, 2e-3, want_loss=True)
     for _ in range(150):
         last = net.train_step(di, dt, 2e-3, want_loss=True)
@@ -120,6 +121,7 @@ def test_batched_calls_match_single_image_calls(h, base, levels):
     data = [_data(h, seed=20 + i) for i in range(3)]
     xb = torch.stack([d[2] for d in data]).contiguous()
     yb = torch.stack([d[3] for d in data]).contiguous()
+    torch.cuda.synchronize()  # the network reads them on its own stream
     out = torch.empty((3, 2, h, h), dtype=torch.float32, device="cuda")
     net.forward(xb, out)
     lb, gb = net.loss_grad(xb, yb)
