@@ -101,24 +101,46 @@ __device__ __forceinline__ double warp_sum_d(double v) {
 __global__ void __launch_bounds__(kPartThreads) k_part_update(PartState ps, PartConsts c, int stage) {
   const int np = c.np;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarp = blockDim.x >> 5;
-  if (stage == 1)
-    for (int i = threadIdx.x; i < 2 * np; i += blockDim.x) {
-      ps.tvel[i] = ps.vel[i];
-      ps.tpos[i] = ps.pos[i];
+  // Up to kPartSmemMax particles the state lives in shared memory for the
+  // sequential loop (the launch passes part_update_smem(np) bytes); above
+  // that the loop reads and writes global memory directly.
+  extern __shared__ double psm[];
+  const bool sm = np <= kPartSmemMax;
+  const size_t n2 = 2 * (size_t)np;
+  double* pos = sm ? psm : ps.pos;
+  double* vel = sm ? psm + n2 : ps.vel;
+  double* tpos = sm ? psm + 2 * n2 : ps.tpos;
+  double* tvel = sm ? psm + 3 * n2 : ps.tvel;
+  double* f0 = sm ? psm + 4 * n2 : ps.f0ext;
+  double* frc = sm ? psm + 5 * n2 : ps.frc;
+  for (int i = threadIdx.x; i < 2 * np; i += blockDim.x) {
+    if (sm) {
+      pos[i] = ps.pos[i];
+      vel[i] = ps.vel[i];
+      f0[i] = ps.f0ext[i];
+      if (stage != 1) {
+        tpos[i] = ps.tpos[i];
+        tvel[i] = ps.tvel[i];
+      }
     }
+    if (stage == 1) {
+      tvel[i] = vel[i];
+      tpos[i] = pos[i];
+    }
+  }
   const double fl = -2.0 * c.alpha * c.dvol * c.scale;  // -2 alpha dvol (1/N^2)
   for (int ip = warp; ip < np; ip += nwarp) {
     // sum_x d rho V_i = f/N^2 (Parseval); force = -2 alpha dvol * that
-    double f0 = 0.0, f1 = 0.0;
+    double g0 = 0.0, g1 = 0.0;
     for (int b = lane; b < c.nblk; b += 32) {
-      f0 += ps.fpart[(size_t)b * 2 * np + 2 * ip];
-      f1 += ps.fpart[(size_t)b * 2 * np + 2 * ip + 1];
+      g0 += ps.fpart[(size_t)b * n2 + 2 * ip];
+      g1 += ps.fpart[(size_t)b * n2 + 2 * ip + 1];
     }
-    f0 = warp_sum_d(f0);
-    f1 = warp_sum_d(f1);
+    g0 = warp_sum_d(g0);
+    g1 = warp_sum_d(g1);
     if (lane == 0) {
-      ps.frc[2 * ip] = f0 * fl;
-      ps.frc[2 * ip + 1] = f1 * fl;
+      frc[2 * ip] = g0 * fl;
+      frc[2 * ip + 1] = g1 * fl;
     }
   }
   __syncthreads();
@@ -129,7 +151,7 @@ __global__ void __launch_bounds__(kPartThreads) k_part_update(PartState ps, Part
     if (np > 1)
       for (int j = lane; j < np; j += 32) {
         if (j == ip) continue;
-        const double x = ps.pos[2 * ip] - ps.pos[2 * j], y = ps.pos[2 * ip + 1] - ps.pos[2 * j + 1];
+        const double x = pos[2 * ip] - pos[2 * j], y = pos[2 * ip + 1] - pos[2 * j + 1];
         const double den = ipow_d(-3.0 + cos(x) + cos(y), 7);
         r0 += -c.rep_factor * sin(x) / den;
         r1 += -c.rep_factor * sin(y) / den;
@@ -140,30 +162,39 @@ __global__ void __launch_bounds__(kPartThreads) k_part_update(PartState ps, Part
       const double rep[2] = {r0, r1};
       for (int d = 0; d < 2; ++d) {
         const int i = 2 * ip + d;
-        const double ft = ps.frc[i] + rep[d] + ps.f0ext[i];
-        ps.frc[i] = ft;
+        const double ft = frc[i] + rep[d] + f0[i];
+        frc[i] = ft;
         if (stage == 0) continue;
         const double ku = c.dt * ft / c.mass;
-        const double kq = c.dt * ps.vel[i];
-        ps.ku[(stage - 1) * 2 * np + i] = ku;
-        ps.kq[(stage - 1) * 2 * np + i] = kq;
+        const double kq = c.dt * vel[i];
+        ps.ku[(stage - 1) * n2 + i] = ku;
+        ps.kq[(stage - 1) * n2 + i] = kq;
         if (stage == 1 || stage == 2) {
-          ps.vel[i] = ps.tvel[i] + 0.5 * ku;
-          ps.pos[i] = ps.tpos[i] + 0.5 * kq;
+          vel[i] = tvel[i] + 0.5 * ku;
+          pos[i] = tpos[i] + 0.5 * kq;
         } else if (stage == 3) {
-          ps.vel[i] = ps.tvel[i] + ku;
-          ps.pos[i] = ps.tpos[i] + kq;
+          vel[i] = tvel[i] + ku;
+          pos[i] = tpos[i] + kq;
         } else {
           const double* K1 = ps.ku;
           const double* Q1 = ps.kq;
-          const size_t o = 2 * (size_t)np;
-          ps.vel[i] = ps.tvel[i] + (1.0 / 6.0) * (K1[i] + 2.0 * K1[o + i] + 2.0 * K1[2 * o + i] + K1[3 * o + i]);
-          ps.pos[i] = ps.tpos[i] + (1.0 / 6.0) * (Q1[i] + 2.0 * Q1[o + i] + 2.0 * Q1[2 * o + i] + Q1[3 * o + i]);
+          vel[i] = tvel[i] + (1.0 / 6.0) * (K1[i] + 2.0 * K1[n2 + i] + 2.0 * K1[2 * n2 + i] + K1[3 * n2 + i]);
+          pos[i] = tpos[i] + (1.0 / 6.0) * (Q1[i] + 2.0 * Q1[n2 + i] + 2.0 * Q1[2 * n2 + i] + Q1[3 * n2 + i]);
         }
       }
     }
     __syncwarp();  // particle ip's new position before particle ip + 1's repulsion
   }
+  if (sm)
+    for (int i = lane; i < 2 * np; i += 32) {
+      ps.pos[i] = pos[i];
+      ps.vel[i] = vel[i];
+      ps.frc[i] = frc[i];
+      if (stage == 1) {
+        ps.tpos[i] = tpos[i];
+        ps.tvel[i] = tvel[i];
+      }
+    }
 }
 
 // Seeded neutral vortex state on the device (FP64), same mathematics as the

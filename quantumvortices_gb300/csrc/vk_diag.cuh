@@ -442,7 +442,7 @@ struct Diagnostics {
     });
     S_.launch_raw("k_spec_reduce", k_spec_reduce, (6 * nsh_ + 255) / 256, 256, 0, (const double*)hpart_, K + 1,
                   nsh_, spec_);
-    if (S_.np_ > 0) S_.launch_raw("k_part_update", k_part_update, 1, kPartThreads, 0, S_.ps_, S_.pc_, 0);
+    if (S_.np_ > 0) S_.launch_raw("k_part_update", k_part_update, 1, kPartThreads, part_update_smem(S_.np_), S_.ps_, S_.pc_, 0);
     // 6. vortex count
     if (cudaMemsetAsync(cnt_, 0, 2 * sizeof(int), S_.st_) != cudaSuccess) {
       set_error("vk_diagnostics: memset failed");

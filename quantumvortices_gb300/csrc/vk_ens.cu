@@ -18,11 +18,13 @@ class EnsembleImpl : public EnsembleBase {
  public:
   Ensemble<T> e;
   int set_psi(int m, const double* psi) override {
-    if (cudaStreamSynchronize(e.st) != cudaSuccess) { set_error("vk_ens: stream error"); return VK_E_CUDA; }
+    const int rc = e.barrier_check();  // synchronises the ensemble stream
+    if (rc) return rc;
     return e.owned[m]->set_psi(psi);
   }
   int get_psi(int m, double* psi) override {
-    if (cudaStreamSynchronize(e.st) != cudaSuccess) { set_error("vk_ens: stream error"); return VK_E_CUDA; }
+    const int rc = e.barrier_check();
+    if (rc) return rc;
     return e.owned[m]->get_psi(psi);
   }
   int rk4(int nsteps) override { return e.rk4(nsteps); }

@@ -11,14 +11,19 @@
 //
 // Autotuner: at set-up it times, on the (still zero) ensemble buffers, every
 // compiled tile variant (x passes RL = 2048 or 4096 points, y passes
-// RL = 1024 or 2048) at 1, 2, 4 and 8 CTAs per SM, per pass kind, and keeps
-// the fastest.
+// RL = 1024 or 2048, each also with the registers capped for more CTAs per
+// SM) at 1, 2, 4 and 8 CTAs per SM, per pass kind, and keeps the fastest.
+// It then times one RK4 step of those four pass kernels per stage against
+// one persistent kernel per stage (kb_stage: the four pass loops in one
+// cooperative launch, bounded grid-wide barriers between them) and steps
+// with the faster.
 #pragma once
 #include <algorithm>
 #include <string>
 #include <vector>
 #include "vk_kernels.cuh"
 #include "vk_solver.h"
+#include "vk_stage.cuh"
 #include <type_traits>
 
 namespace vk {
@@ -101,6 +106,47 @@ __global__ void __launch_bounds__(RL / 16) kb_xinv(const Field<T>* __restrict__ 
   }
 }
 
+// One RK4 stage of every member in one cooperative launch: the four pass
+// loops of the kernels above with grid-wide barriers between them; every
+// pass takes tiles of RL points, so one block size serves all four.
+template <typename T, int RL, int STAGE, bool FROM_T>
+__global__ void __launch_bounds__(RL / 16) kb_stage(const Field<T>* __restrict__ F, const int2* __restrict__ ix,
+                                                   int nix, const int2* __restrict__ iy1, int niy1,
+                                                   const int2* __restrict__ iy2, int niy2, GridBarrier* bar,
+                                                   unsigned long long limit) {
+  extern __shared__ __align__(16) unsigned char smraw[];
+  cplx<T>* s = reinterpret_cast<cplx<T>*>(smraw);
+  for (int it = blockIdx.x; it < nix; it += gridDim.x) {
+    const int2 w = ix[it];
+    const Field<T>& f = F[w.x];
+    VK_ENS_SWITCH(f.c.nx, (x1_body<T, L, GeoB<T, L, RL>, FROM_T, true>(f.Ta, f.psi, f.Tb, f.twx, f.c, w.y, s)));
+    __syncthreads();
+  }
+  if (!grid_sync(bar, limit, 3 * (STAGE - 1))) return;
+  for (int it = blockIdx.x; it < niy1; it += gridDim.x) {
+    const int2 w = iy1[it];
+    const Field<T>& f = F[w.x];
+    VK_ENS_SWITCH(f.c.ny, (y1_body<T, L, GeoB<T, L, RL>>(f.Tb, f.Tc, f.twy, f.c, w.y, s)));
+    __syncthreads();
+  }
+  if (!grid_sync(bar, limit, 3 * (STAGE - 1) + 1)) return;
+  for (int it = blockIdx.x; it < nix; it += gridDim.x) {
+    const int2 w = ix[it];
+    const Field<T>& f = F[w.x];
+    VK_ENS_SWITCH(f.c.nx, (x2_body<T, L, GeoB<T, L, RL>, +1, true, false>(f.Tc, f.psi, (const T*)nullptr, f.Td,
+                                                                            f.twx, f.c, w.y, s)));
+    __syncthreads();
+  }
+  if (!grid_sync(bar, limit, 3 * (STAGE - 1) + 2)) return;
+  for (int it = blockIdx.x; it < niy2; it += gridDim.x) {
+    const int2 w = iy2[it];
+    const Field<T>& f = F[w.x];
+    VK_ENS_SWITCH(f.c.ny, (y2_rk4_body<T, L, GeoB<T, L, RL>, STAGE>(f.Td, f.kpsi, f.str1, f.str2, f.Ta, f.twy, f.c,
+                                                                      w.y, s)));
+    __syncthreads();
+  }
+}
+
 // Pass kinds the autotuner decides separately.
 enum EnsPass { EP_X1 = 0, EP_Y1, EP_X2, EP_Y2, EP_XINV, EP_N };
 
@@ -128,6 +174,12 @@ class Ensemble {
   cudaGraphExec_t gstep = nullptr;
   int64_t launches = 0, gstep_n = 0;
   std::string report;
+  // persistent stage kernel (kb_stage, tiles of kFusedRL points)
+  static constexpr int kFusedRL = 2048;
+  GridBarrier* bar = nullptr;
+  int fused_grid = 0;
+  bool fused = false;
+  unsigned long long spin_limit = 1ull << 24;
 
   static constexpr int XRL[2] = {2048, 4096};
   static constexpr int YRL[2] = {1024, 2048};
@@ -170,6 +222,7 @@ class Ensemble {
       for (auto* b : a)
         if (b) cudaFree(b);
     if (dF) cudaFree(dF);
+    if (bar) cudaFree(bar);
     if (st) cudaStreamDestroy(st);
   }
 
@@ -260,7 +313,84 @@ class Ensemble {
     }
   }
 
+  template <int STAGE, bool FROM_T> void launch_stage() {
+    constexpr int RL = kFusedRL;
+    // x lists of tile variant 0 and y lists of variant 1 hold RL-point tiles
+    static_assert(XRL[0] == RL && YRL[1] == RL, "fused tiles");
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(fused_grid);
+    cfg.blockDim = dim3(RL / 16);
+    cfg.dynamicSmemBytes = sizeof(C) * RL * 17 / 16;
+    cfg.stream = st;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeCooperative;
+    at[0].val.cooperative = 1;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    cudaLaunchKernelEx(&cfg, kb_stage<T, RL, STAGE, FROM_T>, (const Field<T>*)dF, (const int2*)dItems[EP_X1][0],
+                       nItems[EP_X1][0], (const int2*)dItems[EP_Y1][1], nItems[EP_Y1][1],
+                       (const int2*)dItems[EP_Y2][1], nItems[EP_Y2][1], bar, spin_limit);
+    ++launches;
+  }
+  void step_fused(bool first) {
+    if (first) launch_stage<1, false>();
+    else launch_stage<1, true>();
+    launch_stage<2, true>();
+    launch_stage<3, true>();
+    launch_stage<4, true>();
+  }
+  // Sets fused_grid (0 when a cooperative launch of kb_stage is not possible).
+  int init_fused() {
+    int dev = 0, coop = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev);
+    const char* lim = std::getenv("VK_SPIN_LIMIT");
+    if (lim) spin_limit = std::strtoull(lim, nullptr, 10);
+    if (!coop) return VK_OK;
+    const size_t smem = sizeof(C) * kFusedRL * 17 / 16;
+    int occ = 1 << 30;
+    auto fit = [&](const void* fn) {
+      int b = 0;
+      ensure_smem_attr(fn, smem);
+      if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, fn, kFusedRL / 16, smem) != cudaSuccess) b = 0;
+      occ = std::min(occ, b);
+    };
+    fit((const void*)kb_stage<T, kFusedRL, 1, false>);
+    fit((const void*)kb_stage<T, kFusedRL, 1, true>);
+    fit((const void*)kb_stage<T, kFusedRL, 2, true>);
+    fit((const void*)kb_stage<T, kFusedRL, 3, true>);
+    fit((const void*)kb_stage<T, kFusedRL, 4, true>);
+    cudaGetLastError();
+    if (occ <= 0) return VK_OK;
+    fused_grid = occ * sms;
+    if (cudaMalloc(&bar, sizeof(GridBarrier)) != cudaSuccess || cudaMemset(bar, 0, sizeof(GridBarrier)) != cudaSuccess) {
+      set_error("vk_ens_init: barrier allocation failed");
+      return VK_E_NOMEM;
+    }
+    return VK_OK;
+  }
+  // A barrier wait that ran out: report it once and reset the barrier.
+  int barrier_check() {
+    if (!bar) return VK_OK;
+    GridBarrier h;
+    if (cudaMemcpyAsync(&h, bar, sizeof(h), cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+        cudaStreamSynchronize(st) != cudaSuccess) {
+      set_error("vk_ens: stream error");
+      return VK_E_CUDA;
+    }
+    if (h.err == 0) return VK_OK;
+    cudaMemsetAsync(bar, 0, sizeof(GridBarrier), st);
+    cudaStreamSynchronize(st);
+    set_error("vk_ens: a CTA of the persistent stage kernel gave up waiting at grid barrier " +
+              std::to_string(h.err - 1) + " (the members' fields are not valid; set them again)");
+    return VK_E_CUDA;
+  }
+
   void step(bool first) {
+    if (fused) {
+      step_fused(first);
+      return;
+    }
     for (int stage = 1; stage <= 4; ++stage) {
       pass(EP_X1, stage, !(first && stage == 1), variant[EP_X1], grid[EP_X1]);
       pass(EP_Y1, stage, true, variant[EP_Y1], grid[EP_Y1]);
@@ -301,6 +431,37 @@ class Ensemble {
       snprintf(buf, sizeof(buf), "%s: tile %d points%s, %d CTAs (%.1f us/launch); ", names[kind],
                (kind == EP_Y1 || kind == EP_Y2) ? YRL[list_of(variant[kind])] : XRL[list_of(variant[kind])],
                variant[kind] == 2 ? " (registers capped)" : "", grid[kind], 1e3f * best / 3.f);
+      report += buf;
+    }
+    // one RK4 step: the chosen pass kernels against the persistent stage kernel
+    int rc = init_fused();
+    if (rc) {
+      cudaEventDestroy(a);
+      cudaEventDestroy(b);
+      return rc;
+    }
+    if (fused_grid > 0) {
+      float tsep = 0.f, tfus = 0.f;
+      for (int f = 0; f < 2; ++f) {
+        fused = f == 1;
+        step(false);  // warm
+        cudaEventRecord(a, st);
+        for (int r = 0; r < 2; ++r) step(false);
+        cudaEventRecord(b, st);
+        cudaEventSynchronize(b);
+        cudaEventElapsedTime(f ? &tfus : &tsep, a, b);
+      }
+      const char* env = std::getenv("VK_FUSED");
+      fused = env ? env[0] != '0' : tfus < tsep;
+      rc = barrier_check();
+      if (rc) {
+        cudaEventDestroy(a);
+        cudaEventDestroy(b);
+        return rc;
+      }
+      char buf[200];
+      snprintf(buf, sizeof(buf), "step: pass kernels %.1f us, persistent stage kernel (%d CTAs) %.1f us -> %s",
+               1e3f * tsep / 2.f, fused_grid, 1e3f * tfus / 2.f, fused ? "persistent" : "pass kernels");
       report += buf;
     }
     cudaEventDestroy(a);

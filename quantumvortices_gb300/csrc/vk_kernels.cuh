@@ -328,7 +328,7 @@ __device__ __forceinline__ void x1_body(const cplx<T>* __restrict__ Ta, cplx<T>*
     const int p = e / L, x = e % L;
     const C a = s[(2 * p) * G::LP + pidx(x)], b = s[(2 * p + 1) * G::LP + pidx(x)];
     const T bg = T(c.rho_bg);
-    z[q] = mkc<T>(fma(a.x, a.x, fma(a.y, a.y, -bg)), fma(b.x, b.x, fma(b.y, b.y, -bg)));
+    z[q] = mkc<T>(a.x * a.x + a.y * a.y - bg, b.x * b.x + b.y * b.y - bg);
   }
   __syncthreads();
 #pragma unroll
@@ -393,7 +393,7 @@ __device__ __forceinline__ void x1_single_body(const cplx<T>* __restrict__ Ta, c
   for (int q = 0; q < PER; ++q) {
     const int n = threadIdx.x + q * G::NT;
     const C a = s[pidx(2 * n)], b = s[pidx(2 * n + 1)];
-    z[q] = mkc<T>(fma(a.x, a.x, fma(a.y, a.y, -bg)), fma(b.x, b.x, fma(b.y, b.y, -bg)));
+    z[q] = mkc<T>(a.x * a.x + a.y * a.y - bg, b.x * b.x + b.y * b.y - bg);
   }
   __syncthreads();
 #pragma unroll

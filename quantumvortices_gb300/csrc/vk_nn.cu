@@ -1192,16 +1192,14 @@ extern "C" int vk_nn_loss_grad(void* net, const float* in_dev, const float* targ
   return x->check();
 }
 
-// One Adam step on the MSE loss of one sample.
+// One Adam step on the MSE loss of the current batch.  Returns with the
+// network's stream synchronised, so the caller may reuse the input buffers.
 extern "C" int vk_nn_train_step(void* net, const float* in_dev, const float* target_dev, float lr, double* loss_out) {
   Net* x = as_net(net);
   if (!x || !in_dev || !target_dev) { set_error("vk_nn_train_step: null argument"); return VK_E_INVALID; }
   x->forward(in_dev);
   x->backward(target_dev);
   x->adam(lr);
-  if (loss_out) {
-    cudaMemcpyAsync(loss_out, x->loss, sizeof(double), cudaMemcpyDeviceToHost, x->st);
-    return x->check();
-  }
-  return VK_OK;
+  if (loss_out) cudaMemcpyAsync(loss_out, x->loss, sizeof(double), cudaMemcpyDeviceToHost, x->st);
+  return x->check();
 }

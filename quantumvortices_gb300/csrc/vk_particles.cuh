@@ -237,6 +237,9 @@ __global__ void __launch_bounds__(GeoX<T, L>::NT, GeoX<T, L>::MINB) k_vtot_x(con
 // at the current positions (diagnostics loop, src/diagnostics.f90:528-533).
 // One thread.
 constexpr int kPartThreads = 256;  // block size of k_part_update
+constexpr int kPartSmemMax = 512;  // particles whose state k_part_update keeps in shared memory
+// Dynamic shared memory of a k_part_update launch for np particles.
+inline size_t part_update_smem(int np) { return np <= kPartSmemMax ? sizeof(double) * 12 * (size_t)np : 0; }
 __global__ void k_part_update(PartState ps, PartConsts c, int stage);
 
 }  // namespace vk

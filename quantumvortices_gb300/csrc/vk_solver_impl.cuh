@@ -440,7 +440,7 @@ class Solver : public SolverBase {
       }
       y2_rk4(stage);
       if (c_.frc) launch_raw("k_rng_bump", k_rng_bump<T>, 1, 1, 0, rngc_);
-      if (np_ > 0) launch_raw("k_part_update", k_part_update, 1, kPartThreads, 0, ps_, pc_, stage);
+      if (np_ > 0) launch_raw("k_part_update", k_part_update, 1, kPartThreads, part_update_smem(np_), ps_, pc_, stage);
     }
   }
 
@@ -691,15 +691,18 @@ class Solver : public SolverBase {
   }
 
   // ------------------------------------------- persistent stage kernel --
-  // FP32 at 1024^2: each plain RK4 stage is one cooperative launch of
-  // k_stage_rk4 over fused_grid_ CTAs (vk_stage.cuh).  VK_FUSED=0 keeps the
-  // four pass kernels.  VK_SPIN_LIMIT sets how many polls a CTA waits at a
+  // FP32 at 1024^2 with VK_FUSED=1: each plain RK4 stage is one cooperative
+  // launch of k_stage_rk4 over fused_grid_ CTAs (vk_stage.cuh).  Off by
+  // default: on GB300 a stage took 65.9 us against 56.5 us for the four pass
+  // kernels (4.17e9 against 6.21e9 grid-pt-steps/s), because the x bodies'
+  // registers leave 8 warps per SM for the y passes, which run 16 as
+  // separate kernels.  VK_SPIN_LIMIT sets how many polls a CTA waits at a
   // barrier before it gives up (default 2^24, about a second).
   template <int L> static constexpr bool kFusedLen = std::is_same<T, float>::value && L == 1024;
   int init_fused() {
     fused_grid_ = 0;
     const char* env = std::getenv("VK_FUSED");
-    if (!(std::is_same<T, float>::value && nx_ == 1024 && ny_ == 1024) || (env && env[0] == '0')) return VK_OK;
+    if (!(std::is_same<T, float>::value && nx_ == 1024 && ny_ == 1024) || !(env && env[0] == '1')) return VK_OK;
     int dev = 0, coop = 0, nsm = 0;
     VK_CUDA_TRY(cudaGetDevice(&dev));
     VK_CUDA_TRY(cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev));
