@@ -14,6 +14,7 @@
 //   wgrad     dW[tap*Cin+ci, co] = sum_pixel in[pixel+off(tap), ci] dY[pixel, co]
 // (off(tap) = (tap/3-1, tap%3-1), periodic).  No reference counterpart: the
 // reference has no machine learning.
+#include <cuda.h>
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
 #include <cmath>
@@ -33,6 +34,7 @@ namespace nn {
 typedef __nv_bfloat16 bf16;
 
 __device__ __forceinline__ int wrapi(int v, int n) { return v < 0 ? v + n : (v >= n ? v - n : v); }
+__device__ __forceinline__ bool ld_err_nonzero(const int* err) { return *(volatile const int*)err != 0; }
 
 // ------------------------------------------------------------------ conv --
 // Implicit-GEMM convolution, one CTA = 128 output pixels x BN output
@@ -181,6 +183,158 @@ __global__ void __launch_bounds__(128) k_conv(const bf16* __restrict__ in, int H
   tc::fence_before();
   __syncthreads();
   if (warp == 0) tc::tmem_dealloc(taddr, NCOL);
+}
+
+// TMA-fed convolution for Cin a multiple of 64.  The input is first copied
+// into a periodically padded image stack [nimg][H+2][W+2][Cin] (k_pad), so
+// that every tap of a 128-pixel tile is one rectangular box: TMA loads it
+// (box {64 channels, BW pixels, 128/BW rows}, BW = min(W, 128)) straight into
+// the 128-byte swizzle layout, and the weight tile (box {64, BN} of the
+// [coutp][9 Cin] weight matrix) beside it.  The K loop runs over (tap,
+// 64-channel chunk) in the order of k_conv, through an S-stage ring: thread 0
+// issues the loads on the stage's "full" mbarrier, thread 32 waits for it,
+// issues the chunk's four K = 16 MMAs and commits them to the stage's "empty"
+// mbarrier, which frees the stage for the load S chunks ahead.  Every wait is
+// bounded; after a timeout the CTA waits (bounded) for its loads and MMAs in
+// flight, frees its tensor memory and leaves the error word set.
+template <int BN, int S>
+__global__ void __launch_bounds__(128) k_conv_tma(const __grid_constant__ CUtensorMap tmA,
+                                                  const __grid_constant__ CUtensorMap tmB, int H, int W, int nimg,
+                                                  int Cin, const float* __restrict__ bias, int cout, int relu,
+                                                  bf16* __restrict__ out_bf, int ldo, float* __restrict__ out_f,
+                                                  int nout, int* __restrict__ err) {
+  constexpr int ABYTES = 128 * 128, BBYTES = BN * 128, STAGE = ABYTES + BBYTES;
+  static_assert(STAGE % 1024 == 0, "1024-byte aligned stages");
+  extern __shared__ __align__(1024) unsigned char smraw[];
+  __shared__ __align__(8) uint64_t full[S], empty[S], done;
+  __shared__ uint32_t tslot;
+  __shared__ int s_loaded;
+  // the 128-byte swizzle needs 1024-byte aligned tiles
+  unsigned char* sm = smraw + ((1024 - (tc::smem_u32(smraw) & 1023)) & 1023);
+  const int tid = threadIdx.x, warp = tid >> 5;
+  const int npix = nimg * H * W;
+  const int p0 = blockIdx.x * 128, n0 = blockIdx.y * BN;
+  const int BW = W < 128 ? W : 128, BH = 128 / BW;
+  const int row = p0 / W, x0 = p0 - row * W, b = row / H, y0 = row - b * H;
+  const int cch = Cin / 64, nck = 9 * cch;
+  constexpr uint32_t NCOL = BN < 32 ? 32 : BN;
+  if (warp == 0) tc::tmem_alloc(&tslot, NCOL);
+  if (tid == 0) {
+    for (int i = 0; i < S; ++i) {
+      tc::mbar_init(&full[i]);
+      tc::mbar_init(&empty[i]);
+    }
+    tc::mbar_init(&done);
+    s_loaded = 0;
+  }
+  tc::fence_before();
+  __syncthreads();
+  tc::fence_after();
+  const uint32_t taddr = tslot;
+  const uint32_t idesc = tc::idesc_bf16(128, BN);
+  bool ok = true;
+  if (tid == 0) {
+    // producer: chunk i = (tap, channel chunk) into stage i % S
+    int i = 0;
+    for (; i < nck && ok; ++i) {
+      const int st = i % S;
+      if (i >= S) ok = tc::mbar_wait(&empty[st], ((i - S) / S) & 1, err);
+      if (!ok) break;
+      const int tap = i / cch, c0 = 64 * (i - tap * cch);
+      const int dy = tap / 3 - 1, dx = tap % 3 - 1;
+      unsigned char* sA = sm + st * STAGE;
+      tc::mbar_arrive_expect_tx(&full[st], STAGE);
+      tc::tma_load_4d(sA, &tmA, &full[st], c0, x0 + 1 + dx, y0 + 1 + dy, b);
+      tc::tma_load_2d(sA + ABYTES, &tmB, &full[st], tap * Cin + c0, n0);
+    }
+    s_loaded = i;
+  } else if (tid == 32) {
+    // MMA issuer
+    for (int i = 0; i < nck && ok; ++i) {
+      const int st = i % S;
+      ok = tc::mbar_wait(&full[st], (i / S) & 1, err);
+      if (!ok) break;
+      tc::fence_after();
+      const uint32_t a0 = tc::smem_u32(sm + st * STAGE);
+#pragma unroll
+      for (int j = 0; j < 4; ++j) {
+        const uint64_t ad = tc::smem_desc_sw128(a0 + 32 * j);
+        const uint64_t bd = tc::smem_desc_sw128(a0 + ABYTES + 32 * j);
+        tc::mma(taddr, ad, bd, idesc, (i > 0 || j > 0) ? 1u : 0u);
+      }
+      tc::commit(&empty[st]);
+    }
+    tc::commit(&done);  // arrives when every MMA issued above has finished
+  }
+  __syncthreads();
+  // every thread: the MMAs done (bounded), then the epilogue
+  ok = tc::mbar_wait(&done, 0, err) && ok;
+  if (tid == 0 && ld_err_nonzero(err)) {
+    // a wait ran out somewhere: let this CTA's loads land before its shared
+    // memory goes away (bounded waits on the stages still in flight)
+    const int loaded = s_loaded;
+    for (int i = loaded - S < 0 ? 0 : loaded - S; i < loaded; ++i) tc::mbar_wait(&full[i % S], (i / S) & 1, err);
+  }
+  tc::fence_after();
+  if (__syncthreads_and(ok)) {
+    const int r = 32 * warp + (tid & 31);
+    const int p = p0 + r;
+    constexpr int NC = BN < 32 ? 16 : 32;
+#pragma unroll 1
+    for (int c0 = 0; c0 < BN; c0 += NC) {
+      float v[32];
+      const uint32_t ta = taddr + ((uint32_t)(32 * warp) << 16) + c0;
+      if (NC == 16) tc::tmem_ld16(ta, v);
+      else tc::tmem_ld32(ta, v);
+      if (p < npix) {
+#pragma unroll
+        for (int j = 0; j < NC; ++j) {
+          const int c = n0 + c0 + j;
+          float a = v[j] + ((bias && c < cout) ? bias[c] : 0.f);
+          if (relu) a = fmaxf(a, 0.f);
+          v[j] = a;
+        }
+        if (out_bf) {
+#pragma unroll
+          for (int q = 0; q < NC / 8; ++q) {
+            uint4 w;
+            __nv_bfloat162 h0 = __floats2bfloat162_rn(v[8 * q + 0], v[8 * q + 1]);
+            __nv_bfloat162 h1 = __floats2bfloat162_rn(v[8 * q + 2], v[8 * q + 3]);
+            __nv_bfloat162 h2 = __floats2bfloat162_rn(v[8 * q + 4], v[8 * q + 5]);
+            __nv_bfloat162 h3 = __floats2bfloat162_rn(v[8 * q + 6], v[8 * q + 7]);
+            w.x = *reinterpret_cast<uint32_t*>(&h0);
+            w.y = *reinterpret_cast<uint32_t*>(&h1);
+            w.z = *reinterpret_cast<uint32_t*>(&h2);
+            w.w = *reinterpret_cast<uint32_t*>(&h3);
+            *reinterpret_cast<uint4*>(out_bf + (size_t)p * ldo + n0 + c0 + 8 * q) = w;
+          }
+        }
+        if (out_f)
+          for (int j = 0; j < NC; ++j)
+            if (n0 + c0 + j < nout) out_f[(size_t)p * nout + n0 + c0 + j] = v[j];
+      }
+    }
+  }
+  tc::fence_before();
+  __syncthreads();
+  if (warp == 0) tc::tmem_dealloc(taddr, NCOL);
+}
+
+// Periodic padding: out[b][y][x][c] = in[b][(y-1) mod H][(x-1) mod W][c] on
+// the (H+2) x (W+2) stack, 16-byte vectors (C a multiple of 8).
+__global__ void k_pad(const bf16* __restrict__ in, bf16* __restrict__ out, int H, int W, int C, int nimg) {
+  const int cv = C / 8, Wp = W + 2, Hp = H + 2;
+  const size_t n = (size_t)nimg * Hp * Wp * cv;
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+    const int v = (int)(i % cv);
+    size_t t = i / cv;
+    const int x = (int)(t % Wp);
+    t /= Wp;
+    const int y = (int)(t % Hp), b = (int)(t / Hp);
+    const int ys = y == 0 ? H - 1 : (y == H + 1 ? 0 : y - 1), xs = x == 0 ? W - 1 : (x == W + 1 ? 0 : x - 1);
+    reinterpret_cast<uint4*>(out)[i] =
+        reinterpret_cast<const uint4*>(in)[(((size_t)b * H + ys) * W + xs) * cv + v];
+  }
 }
 
 // Row-block convolution for the narrow layers (Cin <= 64, W a multiple of
@@ -692,6 +846,20 @@ struct Conv {
 
 static int pad16(int c) { return (c + 15) / 16 * 16; }
 
+// cuTensorMapEncodeTiled from the driver, looked up through the runtime (no
+// link-time dependency on libcuda).
+typedef CUresult (*EncodeTiled)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
+                                const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
+                                CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+static EncodeTiled encode_tiled_fn() {
+  void* f = nullptr;
+  cudaDriverEntryPointQueryResult q;
+  if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &f, 12000, cudaEnableDefault, &q) != cudaSuccess ||
+      q != cudaDriverEntryPointSuccess)
+    return nullptr;
+  return reinterpret_cast<EncodeTiled>(f);
+}
+
 class Net {
  public:
   int H, W, base, levels;
@@ -715,6 +883,13 @@ class Net {
     const char* e = std::getenv("VK_CONV_ROWS");
     return !(e && e[0] == '0');
   }();
+  // TMA-fed convolution for inputs of 64k channels (VK_CONV_TMA=1 turns it on)
+  bool tma_ok_ = [] {
+    const char* e = std::getenv("VK_CONV_TMA");
+    return e && e[0] == '1';
+  }();
+  bf16* padbuf = nullptr;  // periodically padded input of k_conv_tma
+  size_t padbuf_n = 0;
   std::vector<void*> allocs;
   // activations (forward) per level and gradient scratch
   Tensor x0;
@@ -834,6 +1009,11 @@ class Net {
       }
     }
     dhead = tens(H, W, 16);
+    // largest padded input of a TMA convolution: level l holds at most
+    // base << (l + 1) channels (the upsampled decoder input)
+    for (int l = 0; l < levels; ++l)
+      padbuf_n = std::max(padbuf_n, (size_t)bcap * ((H >> l) + 2) * ((W >> l) + 2) * (size_t)(base << (l + 1)));
+    padbuf = dalloc<bf16>(padbuf_n);
     out_f = dalloc<float>((size_t)H * W * 2 * bcap);
     feat_psi = dalloc<double2>((size_t)H * W);
     feat_pos = dalloc<double>(2 * kMaxVortices);
@@ -855,6 +1035,7 @@ class Net {
   // channels split into blocks of BN so that small levels still fill the GPU.
   void conv(const Tensor& in, const bf16* w, int cout_p, int cout, const float* bias, int relu, bf16* out_bf,
             float* out_f32, int nout) {
+    if (conv_tma(in, w, cout_p, cout, bias, relu, out_bf, out_f32, nout)) return;
     if (conv_rows(in, w, cout_p, cout, bias, relu, out_bf, out_f32, nout)) return;
     const int npix = nb * in.h * in.w;
     const int tiles = (npix + 127) / 128;
@@ -867,6 +1048,59 @@ class Net {
       case 64: launch_conv<64>(grid, in, w, bias, cout, relu, out_bf, cout_p, out_f32, nout); break;
       default: launch_conv<128>(grid, in, w, bias, cout, relu, out_bf, cout_p, out_f32, nout); break;
     }
+  }
+  // The TMA-fed kernel when enabled and the shape allows it: Cin a multiple
+  // of 64, and 128-pixel tiles that are whole rows or whole row groups of one
+  // image.
+  bool conv_tma(const Tensor& in, const bf16* w, int cout_p, int cout, const float* bias, int relu, bf16* ob,
+                float* of, int nout) {
+    const int Hh = in.h, Ww = in.w, C = in.c;
+    if (!tma_ok_ || C % 64 != 0 || Hh * Ww < 128) return false;
+    if (!(Ww % 128 == 0 || (128 % Ww == 0 && Hh % (128 / Ww) == 0))) return false;
+    if ((size_t)nb * (Hh + 2) * (Ww + 2) * C > padbuf_n) return false;
+    static EncodeTiled enc = encode_tiled_fn();
+    if (!enc) return false;
+    k_pad<<<blocks((size_t)nb * (Hh + 2) * (Ww + 2) * C / 8), 256, 0, st>>>(in.d, padbuf, Hh, Ww, C, nb);
+    const int tiles = nb * Hh * Ww / 128;
+    int bn = std::min(cout_p, 128);
+    while (bn > 32 && tiles * (cout_p / bn) < 2 * 152) bn /= 2;
+    if (cout_p % bn != 0) return false;
+    CUtensorMap ta, tb;
+    const int bw = Ww < 128 ? Ww : 128;
+    const cuuint64_t gA[4] = {(cuuint64_t)C, (cuuint64_t)Ww + 2, (cuuint64_t)Hh + 2, (cuuint64_t)nb};
+    const cuuint64_t sA[3] = {(cuuint64_t)C * 2, (cuuint64_t)(Ww + 2) * C * 2, (cuuint64_t)(Hh + 2) * (Ww + 2) * C * 2};
+    const cuuint32_t bA[4] = {64, (cuuint32_t)bw, (cuuint32_t)(128 / bw), 1};
+    const cuuint32_t e4[4] = {1, 1, 1, 1};
+    const cuuint64_t gB[2] = {(cuuint64_t)9 * C, (cuuint64_t)cout_p};
+    const cuuint64_t sB[1] = {(cuuint64_t)9 * C * 2};
+    const cuuint32_t bB[2] = {64, (cuuint32_t)bn};
+    if (enc(&ta, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 4, padbuf, gA, sA, bA, e4, CU_TENSOR_MAP_INTERLEAVE_NONE,
+            CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+            CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS ||
+        enc(&tb, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, const_cast<bf16*>(w), gB, sB, bB, e4,
+            CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+            CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
+      return false;
+    const dim3 grid(tiles, cout_p / bn);
+    switch (bn) {
+      case 32: launch_tma<32>(grid, ta, tb, in, bias, cout, relu, ob, cout_p, of, nout); break;
+      case 64: launch_tma<64>(grid, ta, tb, in, bias, cout, relu, ob, cout_p, of, nout); break;
+      default: launch_tma<128>(grid, ta, tb, in, bias, cout, relu, ob, cout_p, of, nout); break;
+    }
+    return true;
+  }
+  static constexpr int kTmaStages = 4;
+  template <int BN>
+  void launch_tma(dim3 grid, const CUtensorMap& ta, const CUtensorMap& tb, const Tensor& in, const float* bias,
+                  int cout, int relu, bf16* ob, int ldo, float* of, int nout) {
+    const size_t smem = (size_t)kTmaStages * (128 * 128 + BN * 128) + 1024;
+    static bool attr = false;
+    if (!attr) {
+      cudaFuncSetAttribute(k_conv_tma<BN, kTmaStages>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+      attr = true;
+    }
+    k_conv_tma<BN, kTmaStages><<<grid, 128, smem, st>>>(ta, tb, in.h, in.w, nb, in.c, bias, cout, relu, ob, ldo, of,
+                                                         nout, err);
   }
   // The row-block kernel for narrow layers when the shape allows it.
   bool conv_rows(const Tensor& in, const bf16* w, int cout_p, int cout, const float* bias, int relu, bf16* ob,

@@ -71,14 +71,16 @@ __device__ __forceinline__ bool grid_sync(GridBarrier* b, unsigned long long lim
 // Geometry of the persistent stage kernel: x tiles of R rows and y tiles with
 // one block size.  FP32 at L = 1024: x tiles of two rows with one warp per
 // row in the row transforms (the x kernels' layout at half the height) and
-// the y kernels' one-column tiles; 64 threads, four CTAs per SM.
+// the y kernels' one-column tiles; 64 threads, six CTAs per SM (registers
+// capped at 168: the x bodies alone would take 255, which left four CTAs and
+// measured slower than the separate pass kernels).
 template <typename T, int LL> struct GeoFused;
 template <> struct GeoFused<float, 1024> {
   struct X {
-    static constexpr int L = 1024, R = 2, LP = padded(1024), NT = 64, MINB = 4;
+    static constexpr int L = 1024, R = 2, LP = padded(1024), NT = 64, MINB = 6;
   };
   typedef GeoY<float, 1024> Y;
-  static constexpr int NT = 64, MINB = 4;
+  static constexpr int NT = 64, MINB = 6;
 };
 
 // One RK4 stage of one field in one launch (plain RHS: no particles, no

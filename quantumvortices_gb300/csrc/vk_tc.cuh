@@ -1,7 +1,8 @@
 // vk_tc.cuh -- tcgen05 (5th-generation tensor core) building blocks for sm_103a.
 //
 // One CTA of 128 threads owns a 128 x BN FP32 accumulator in tensor memory
-// (TMEM lanes = rows, columns = BN).  Operand tiles are written to shared
+// (TMEM lanes = rows, columns = BN).  Operand tiles are either loaded by TMA
+// in the 128-byte swizzle layout (smem_desc_sw128) or written to shared
 // memory by the threads in the no-swizzle K-major core-matrix layout
 // (8 rows x 16 bytes per core matrix; element (r, k) of a tile with CK
 // columns at (r/8)*(CK/8)*128 + (k/8)*128 + (r%8)*16 + (k%8)*2), described to
@@ -35,6 +36,22 @@ __device__ __forceinline__ uint64_t smem_desc(uint32_t addr, uint32_t lbo, uint3
   return d;
 }
 
+// Descriptor of a K-major tile in the 128-byte swizzle layout that a TMA
+// load with CU_TENSOR_MAP_SWIZZLE_128B writes: rows of 128 bytes (64 BF16),
+// 8-row groups 1024 bytes apart (SBO), the 16-byte chunks of row r XOR-ed
+// with r % 8.  The tile must start on a 1024-byte boundary; a K = 16 slice
+// at byte offset 32 j of the row is addressed by advancing the start address
+// by 32 j bytes.
+__device__ __forceinline__ uint64_t smem_desc_sw128(uint32_t addr) {
+  uint64_t d = 0;
+  d |= (uint64_t)((addr & 0x3FFFF) >> 4);
+  d |= (uint64_t)1 << 16;             // LBO (unused for swizzled K-major)
+  d |= (uint64_t)(1024 >> 4) << 32;   // SBO: next 8-row group
+  d |= (uint64_t)1 << 46;             // descriptor version for tcgen05
+  d |= (uint64_t)2 << 61;             // 128-byte swizzle
+  return d;
+}
+
 // kind::f16 instruction descriptor: D = F32, A = B = BF16, both K-major.
 __device__ __forceinline__ uint32_t idesc_bf16(int m, int n) {
   return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(n >> 3) << 17) | ((uint32_t)(m >> 4) << 24);
@@ -54,6 +71,27 @@ __device__ __forceinline__ void fence_async_smem() { asm volatile("fence.proxy.a
 __device__ __forceinline__ void mbar_init(uint64_t* bar) {
   asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(1));
   asm volatile("fence.mbarrier_init.release.cluster;");
+}
+
+// mbarrier expecting one arrival plus `bytes` of TMA transactions.
+__device__ __forceinline__ void mbar_arrive_expect_tx(uint64_t* bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes) : "memory");
+}
+// TMA tile loads (global -> shared) completing on an mbarrier.  The tensor
+// map lives in kernel parameter space (__grid_constant__).
+__device__ __forceinline__ void tma_load_2d(void* dst, const void* tmap, uint64_t* bar, int c0, int c1) {
+  asm volatile(
+      "cp.async.bulk.tensor.2d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%3, %4}], [%2];"
+      ::"r"(smem_u32(dst)), "l"(tmap), "r"(smem_u32(bar)), "r"(c0), "r"(c1)
+      : "memory");
+}
+__device__ __forceinline__ void tma_load_4d(void* dst, const void* tmap, uint64_t* bar, int c0, int c1, int c2,
+                                            int c3) {
+  asm volatile(
+      "cp.async.bulk.tensor.4d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%3, %4, %5, "
+      "%6}], [%2];" ::"r"(smem_u32(dst)),
+      "l"(tmap), "r"(smem_u32(bar)), "r"(c0), "r"(c1), "r"(c2), "r"(c3)
+      : "memory");
 }
 
 __device__ __forceinline__ void mma(uint32_t taddr, uint64_t ad, uint64_t bd, uint32_t idesc, uint32_t acc) {

@@ -156,3 +156,31 @@ def test_feature_kernel_matches_numpy():
     ref = nn_oracle.features(h, h, pos, psi, width)
     assert rel(out.cpu().numpy(), ref) < 1e-6
     net.close()
+
+
+@pytest.mark.parametrize("h,base,levels", [(128, 32, 3), (64, 32, 4)])
+def test_tma_conv_matches_cp_async_conv(h, base, levels):
+    """Layers whose input has 64k channels run on the TMA-fed kernel
+    (VK_CONV_TMA=1: periodic padding, TMA tiles in the 128-byte swizzle
+    layout, 4-stage mbarrier ring); the same K order as the cp.async kernel,
+    so forward outputs and gradients agree to FP32 rounding (a batch of 2)."""
+    import os
+    torch = pytest.importorskip("torch")
+    data = [_data(h, seed=30 + i) for i in range(2)]
+    xb = torch.stack([d[2] for d in data]).contiguous()
+    yb = torch.stack([d[3] for d in data]).contiguous()
+    torch.cuda.synchronize()
+    res = []
+    for flag in ("0", "1"):
+        os.environ["VK_CONV_TMA"] = flag
+        try:
+            net = WarmStartNet(h, h, base, levels, seed=9, batch=2)
+        finally:
+            os.environ.pop("VK_CONV_TMA", None)
+        out = torch.empty((2, 2, h, h), dtype=torch.float32, device="cuda")
+        net.forward(xb, out)
+        loss, g = net.loss_grad(xb, yb)
+        res.append((out.cpu().numpy(), loss, g))
+        net.close()
+    (o0, l0, g0), (o1, l1, g1) = res
+    assert rel(o1, o0) < 1e-5 and abs(l1 - l0) <= 1e-5 * l0 and rel(g1, g0) < 1e-4
