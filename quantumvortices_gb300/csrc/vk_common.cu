@@ -75,17 +75,21 @@ __global__ void k_part_tables(PartState ps, PartConsts c) {
 
 // Particle update of one RK4 stage (gp_particle_motion_rk4), or with
 // STAGE == 0 only the force evaluation at the current positions (the
-// diagnostics loop, src/diagnostics.f90:528-533).  One CTA of
-// kPartThreads threads.
-//  1. Fluid forces of all particles: warp w reduces particles w, w + nwarps,
-//     ...; lane l sums the per-CTA Parseval partials of blocks l, l + 32, ...
-//     in increasing order, then a fixed shuffle tree (lane 0's sum is the
-//     same on every run).  Staged in frc.
-//  2. The particles in index order (the reference's order: particle i sees
-//     particles j < i at their updated positions, src/gpe_particle.f90:456-467),
-//     warp 0: lanes take the repulsion terms j = l, l + 32, ..., a shuffle
-//     tree sums them, lane 0 adds the fluid and external forces and updates
-//     particle i before the next one starts.
+// diagnostics loop, src/diagnostics.f90:528-533).  One CTA of kPartThreads.
+//
+// The reference updates the particles one after another, and particle i's
+// repulsion sees particles j < i at their new positions (:456-467).  A
+// particle's new position depends only on its velocity before the update
+// (k_q = dt v), not on any force, so all new positions are computed first;
+// then every particle's force is independent of the others' and one warp
+// per particle evaluates it:
+//  1. fluid forces: warp w sums the per-CTA Parseval partials of particles
+//     w, w + nwarps, ...: lane l over blocks l, l + 32, ... in increasing
+//     order, then a fixed shuffle tree (lane 0's sum is the same every run);
+//  2. new positions of all particles;
+//  3. per particle: the repulsion terms over j (new positions for j < i, the
+//     old ones for j > i and for i itself) on the lanes and a shuffle tree,
+//     then lane 0 adds the fluid and external forces and updates the velocity.
 __device__ __forceinline__ double ipow_d(double x, int n) {
   double r = 1.0;
   for (int i = 0; i < n; ++i) r *= x;
@@ -101,9 +105,10 @@ __device__ __forceinline__ double warp_sum_d(double v) {
 __global__ void __launch_bounds__(kPartThreads) k_part_update(PartState ps, PartConsts c, int stage) {
   const int np = c.np;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarp = blockDim.x >> 5;
-  // Up to kPartSmemMax particles the state lives in shared memory for the
-  // sequential loop (the launch passes part_update_smem(np) bytes); above
-  // that the loop reads and writes global memory directly.
+  // Up to kPartSmemMax particles the state lives in shared memory (the launch
+  // passes part_update_smem(np) bytes); above that in global memory, with
+  // the new positions in the tab_x scratch (rebuilt from the positions
+  // before every force pass).
   extern __shared__ double psm[];
   const bool sm = np <= kPartSmemMax;
   const size_t n2 = 2 * (size_t)np;
@@ -113,6 +118,7 @@ __global__ void __launch_bounds__(kPartThreads) k_part_update(PartState ps, Part
   double* tvel = sm ? psm + 3 * n2 : ps.tvel;
   double* f0 = sm ? psm + 4 * n2 : ps.f0ext;
   double* frc = sm ? psm + 5 * n2 : ps.frc;
+  double* posn = sm ? psm + 6 * n2 : ps.tab_x;
   for (int i = threadIdx.x; i < 2 * np; i += blockDim.x) {
     if (sm) {
       pos[i] = ps.pos[i];
@@ -144,14 +150,31 @@ __global__ void __launch_bounds__(kPartThreads) k_part_update(PartState ps, Part
     }
   }
   __syncthreads();
-  if (warp != 0) return;
-  for (int ip = 0; ip < np; ++ip) {
-    // short-range repulsion with the current positions (shortrange_repulsion, :378-427)
+  // new positions (k_q = dt v with the velocity before this stage's update)
+  for (int i = threadIdx.x; i < 2 * np; i += blockDim.x) {
+    double q = pos[i];
+    if (stage > 0) {
+      const double kq = c.dt * vel[i];
+      ps.kq[(stage - 1) * n2 + i] = kq;
+      if (stage == 1 || stage == 2) q = tpos[i] + 0.5 * kq;
+      else if (stage == 3) q = tpos[i] + kq;
+      else {
+        const double* Q1 = ps.kq;
+        q = tpos[i] + (1.0 / 6.0) * (Q1[i] + 2.0 * Q1[n2 + i] + 2.0 * Q1[2 * n2 + i] + kq);
+      }
+    }
+    posn[i] = q;
+  }
+  __syncthreads();
+  for (int ip = warp; ip < np; ip += nwarp) {
+    // short-range repulsion (shortrange_repulsion, :378-427): particles
+    // j < ip at their new positions, the others and ip itself at the old ones
     double r0 = 0.0, r1 = 0.0;
     if (np > 1)
       for (int j = lane; j < np; j += 32) {
         if (j == ip) continue;
-        const double x = pos[2 * ip] - pos[2 * j], y = pos[2 * ip + 1] - pos[2 * j + 1];
+        const double* qj = j < ip ? posn : pos;
+        const double x = pos[2 * ip] - qj[2 * j], y = pos[2 * ip + 1] - qj[2 * j + 1];
         const double den = ipow_d(-3.0 + cos(x) + cos(y), 7);
         r0 += -c.rep_factor * sin(x) / den;
         r1 += -c.rep_factor * sin(y) / den;
@@ -166,28 +189,20 @@ __global__ void __launch_bounds__(kPartThreads) k_part_update(PartState ps, Part
         frc[i] = ft;
         if (stage == 0) continue;
         const double ku = c.dt * ft / c.mass;
-        const double kq = c.dt * vel[i];
         ps.ku[(stage - 1) * n2 + i] = ku;
-        ps.kq[(stage - 1) * n2 + i] = kq;
-        if (stage == 1 || stage == 2) {
-          vel[i] = tvel[i] + 0.5 * ku;
-          pos[i] = tpos[i] + 0.5 * kq;
-        } else if (stage == 3) {
-          vel[i] = tvel[i] + ku;
-          pos[i] = tpos[i] + kq;
-        } else {
+        if (stage == 1 || stage == 2) vel[i] = tvel[i] + 0.5 * ku;
+        else if (stage == 3) vel[i] = tvel[i] + ku;
+        else {
           const double* K1 = ps.ku;
-          const double* Q1 = ps.kq;
-          vel[i] = tvel[i] + (1.0 / 6.0) * (K1[i] + 2.0 * K1[n2 + i] + 2.0 * K1[2 * n2 + i] + K1[3 * n2 + i]);
-          pos[i] = tpos[i] + (1.0 / 6.0) * (Q1[i] + 2.0 * Q1[n2 + i] + 2.0 * Q1[2 * n2 + i] + Q1[3 * n2 + i]);
+          vel[i] = tvel[i] + (1.0 / 6.0) * (K1[i] + 2.0 * K1[n2 + i] + 2.0 * K1[2 * n2 + i] + ku);
         }
       }
     }
-    __syncwarp();  // particle ip's new position before particle ip + 1's repulsion
   }
-  if (sm)
-    for (int i = lane; i < 2 * np; i += 32) {
-      ps.pos[i] = pos[i];
+  __syncthreads();
+  for (int i = threadIdx.x; i < 2 * np; i += blockDim.x) {
+    ps.pos[i] = posn[i];
+    if (sm) {
       ps.vel[i] = vel[i];
       ps.frc[i] = frc[i];
       if (stage == 1) {
@@ -195,6 +210,7 @@ __global__ void __launch_bounds__(kPartThreads) k_part_update(PartState ps, Part
         ps.tvel[i] = tvel[i];
       }
     }
+  }
 }
 
 // Seeded neutral vortex state on the device (FP64), same mathematics as the

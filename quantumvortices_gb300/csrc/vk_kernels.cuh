@@ -67,7 +67,7 @@ VK_GEO(GeoY, double, 128, 2, 8) VK_GEO(GeoY, double, 256, 1, 8) VK_GEO(GeoY, dou
 VK_GEOE(GeoY, double, 1024, 1, 5, 8) VK_GEO(GeoY, double, 2048, 1, 4) VK_GEO(GeoY, double, 4096, 1, 2)
 VK_GEO(GeoX, float, 16, 16, 4) VK_GEO(GeoX, float, 32, 16, 4) VK_GEO(GeoX, float, 64, 16, 4)
 VK_GEO(GeoX, float, 128, 8, 4) VK_GEO(GeoX, float, 256, 4, 4) VK_GEO(GeoX, float, 512, 2, 8)
-VK_GEOE(GeoX, float, 1024, 4, 4, 32) VK_GEO(GeoX, float, 2048, 2, 2) VK_GEO(GeoX, float, 4096, 2, 1)
+VK_GEOE(GeoX, float, 1024, 4, 2, 32) VK_GEO(GeoX, float, 2048, 2, 2) VK_GEO(GeoX, float, 4096, 2, 1)
 VK_GEO(GeoY, float, 16, 16, 4) VK_GEO(GeoY, float, 32, 8, 8) VK_GEO(GeoY, float, 64, 4, 8)
 VK_GEO(GeoY, float, 128, 2, 8) VK_GEO(GeoY, float, 256, 1, 8) VK_GEO(GeoY, float, 512, 1, 8)
 VK_GEO(GeoY, float, 1024, 1, 8) VK_GEO(GeoY, float, 2048, 1, 4) VK_GEO(GeoY, float, 4096, 1, 2)

@@ -13,9 +13,9 @@
 // summed over the half plane kx in [0,K] with weight 2 for kx > 0 (rho, V
 // real).  e^{ik.q_i} = ex_i(kx) ey_i(ky) from FP64 tables rebuilt from the
 // stage positions; the same products give V^_tot for the RHS.  The
-// sequential per-particle update (repulsion sees particles j < i at their new
-// positions, :456-467) runs on one warp in FP64, after the fluid forces of
-// all particles have been reduced by the CTA's warps.
+// per-particle update (repulsion sees particles j < i at their new
+// positions, :456-467) runs in one CTA in FP64: the new positions do not
+// depend on the forces, so every particle's force is evaluated in parallel.
 #pragma once
 #include "vk_kernels.cuh"
 
@@ -239,7 +239,7 @@ __global__ void __launch_bounds__(GeoX<T, L>::NT, GeoX<T, L>::MINB) k_vtot_x(con
 constexpr int kPartThreads = 256;  // block size of k_part_update
 constexpr int kPartSmemMax = 512;  // particles whose state k_part_update keeps in shared memory
 // Dynamic shared memory of a k_part_update launch for np particles.
-inline size_t part_update_smem(int np) { return np <= kPartSmemMax ? sizeof(double) * 12 * (size_t)np : 0; }
+inline size_t part_update_smem(int np) { return np <= kPartSmemMax ? sizeof(double) * 14 * (size_t)np : 0; }
 __global__ void k_part_update(PartState ps, PartConsts c, int stage);
 
 }  // namespace vk
