@@ -580,6 +580,8 @@ def run_ours(args, rank, world, local_rank):
                         "what": "one vk_diagnostics call: energies, momentum, norm, six shell spectra, vortex "
                                 "count, results copied to the host"},
         "kernel_ms": {k: round(v[0] / v[1], 5) for k, v in per.items()},
+        "kernel_ms_note": "per launch, from a separate pass with an event pair around every launch and no CUDA "
+                          "graph; their sum reads a few percent above the graph-replayed step time",
         "e2e": {"value": n * n * S / e2e_t, "unit": UNIT, "h2d_bytes_per_step": n * n * 16,
                 "d2h_bytes_per_step": n * n * 16},
         "fp32": fp32,

@@ -185,13 +185,15 @@ __global__ void __launch_bounds__(128) k_conv(const bf16* __restrict__ in, int H
   if (warp == 0) tc::tmem_dealloc(taddr, NCOL);
 }
 
-// TMA-fed convolution for Cin a multiple of 64.  The input is first copied
-// into a periodically padded image stack [nimg][H+2][W+2][Cin] (k_pad), so
-// that every tap of a 128-pixel tile is one rectangular box: TMA loads it
-// (box {64 channels, BW pixels, 128/BW rows}, BW = min(W, 128)) straight into
-// the 128-byte swizzle layout, and the weight tile (box {64, BN} of the
-// [coutp][9 Cin] weight matrix) beside it.  The K loop runs over (tap,
-// 64-channel chunk) in the order of k_conv, through an S-stage ring: thread 0
+// TMA-fed convolution, Cin a multiple of CK (64, or 16/32 for the narrow
+// layers).  The input is first copied into a periodically padded image stack
+// [nimg][H+2][W+2][Cin] (k_pad), so that every tap of a 128-pixel tile is one
+// rectangular box: TMA loads it (box {CK channels, BW pixels, 128/BW rows},
+// BW = min(W, 128)) straight into the swizzle layout of rows of CK channels
+// (2 CK bytes: the 128-, 64- or 32-byte swizzle), and the weight tile (box
+// {CK, BN} of the [coutp][9 Cin] weight matrix) beside it.  The K loop runs
+// over (tap, CK-channel chunk), for CK = 64 in the order of k_conv, through
+// an S-stage ring: thread 0
 // issues the loads on the stage's "full" mbarrier, thread 32 waits for it,
 // issues the chunk's four K = 16 MMAs and commits them to the stage's "empty"
 // mbarrier, which frees the stage for the load S chunks ahead.  Every wait is
@@ -199,14 +201,14 @@ __global__ void __launch_bounds__(128) k_conv(const bf16* __restrict__ in, int H
 // flight, frees its tensor memory and leaves the error word set.  On GB300
 // the 512^2 training step (batches of 8) ran at 88 TFLOP/s with it against
 // 81 without.
-template <int BN, int S>
+template <int BN, int S, int CK>
 __global__ void __launch_bounds__(128) k_conv_tma(const __grid_constant__ CUtensorMap tmA,
                                                   const __grid_constant__ CUtensorMap tmB, int H, int W, int nimg,
                                                   int Cin, const float* __restrict__ bias, int cout, int relu,
                                                   bf16* __restrict__ out_bf, int ldo, float* __restrict__ out_f,
                                                   int nout, int* __restrict__ err) {
-  constexpr int ABYTES = 128 * 128, BBYTES = BN * 128, STAGE = ABYTES + BBYTES;
-  static_assert(STAGE % 1024 == 0, "1024-byte aligned stages");
+  constexpr int ABYTES = 128 * CK * 2, BBYTES = BN * CK * 2, STAGE = ABYTES + BBYTES;
+  static_assert(ABYTES % (16 * CK) == 0 && STAGE % (16 * CK) == 0, "tiles on swizzle-atom boundaries");
   extern __shared__ __align__(1024) unsigned char smraw[];
   __shared__ __align__(8) uint64_t full[S], empty[S], done;
   __shared__ uint32_t tslot;
@@ -218,7 +220,7 @@ __global__ void __launch_bounds__(128) k_conv_tma(const __grid_constant__ CUtens
   const int p0 = blockIdx.x * 128, n0 = blockIdx.y * BN;
   const int BW = W < 128 ? W : 128, BH = 128 / BW;
   const int row = p0 / W, x0 = p0 - row * W, b = row / H, y0 = row - b * H;
-  const int cch = Cin / 64, nck = 9 * cch;
+  const int cch = Cin / CK, nck = 9 * cch;
   constexpr uint32_t NCOL = BN < 32 ? 32 : BN;
   if (warp == 0) tc::tmem_alloc(&tslot, NCOL);
   if (tid == 0) {
@@ -242,7 +244,7 @@ __global__ void __launch_bounds__(128) k_conv_tma(const __grid_constant__ CUtens
       const int st = i % S;
       if (i >= S) ok = tc::mbar_wait(&empty[st], ((i - S) / S) & 1, err);
       if (!ok) break;
-      const int tap = i / cch, c0 = 64 * (i - tap * cch);
+      const int tap = i / cch, c0 = CK * (i - tap * cch);
       const int dy = tap / 3 - 1, dx = tap % 3 - 1;
       unsigned char* sA = sm + st * STAGE;
       tc::mbar_arrive_expect_tx(&full[st], STAGE);
@@ -259,9 +261,9 @@ __global__ void __launch_bounds__(128) k_conv_tma(const __grid_constant__ CUtens
       tc::fence_after();
       const uint32_t a0 = tc::smem_u32(sm + st * STAGE);
 #pragma unroll
-      for (int j = 0; j < 4; ++j) {
-        const uint64_t ad = tc::smem_desc_sw128(a0 + 32 * j);
-        const uint64_t bd = tc::smem_desc_sw128(a0 + ABYTES + 32 * j);
+      for (int j = 0; j < CK / 16; ++j) {
+        const uint64_t ad = tc::smem_desc_swk<CK>(a0 + 32 * j);
+        const uint64_t bd = tc::smem_desc_swk<CK>(a0 + ABYTES + 32 * j);
         tc::mma(taddr, ad, bd, idesc, (i > 0 || j > 0) ? 1u : 0u);
       }
       tc::commit(&empty[st]);
@@ -890,6 +892,11 @@ class Net {
     const char* e = std::getenv("VK_CONV_TMA");
     return !(e && e[0] == '0');
   }();
+  // ... and for the narrow layers (16 or 32 input channels) too with VK_CONV_TMA_NARROW=1
+  bool tma_narrow_ = [] {
+    const char* e = std::getenv("VK_CONV_TMA_NARROW");
+    return e && e[0] == '1';
+  }();
   bf16* padbuf = nullptr;  // periodically padded input of k_conv_tma
   size_t padbuf_n = 0;
   std::vector<void*> allocs;
@@ -1057,7 +1064,8 @@ class Net {
   bool conv_tma(const Tensor& in, const bf16* w, int cout_p, int cout, const float* bias, int relu, bf16* ob,
                 float* of, int nout) {
     const int Hh = in.h, Ww = in.w, C = in.c;
-    if (!tma_ok_ || C % 64 != 0 || Hh * Ww < 128) return false;
+    const int ck = C % 64 == 0 ? 64 : (C % 32 == 0 ? 32 : 16);
+    if (!tma_ok_ || (ck < 64 && !tma_narrow_) || C % 16 != 0 || Hh * Ww < 128) return false;
     if (!(Ww % 128 == 0 || (128 % Ww == 0 && Hh % (128 / Ww) == 0))) return false;
     if ((size_t)nb * (Hh + 2) * (Ww + 2) * C > padbuf_n) return false;
     static EncodeTiled enc = encode_tiled_fn();
@@ -1066,43 +1074,51 @@ class Net {
     const int tiles = nb * Hh * Ww / 128;
     int bn = std::min(cout_p, 128);
     while (bn > 32 && tiles * (cout_p / bn) < 2 * 152) bn /= 2;
-    if (cout_p % bn != 0) return false;
+    if (cout_p % bn != 0 || bn < 16) return false;
     CUtensorMap ta, tb;
     const int bw = Ww < 128 ? Ww : 128;
     const cuuint64_t gA[4] = {(cuuint64_t)C, (cuuint64_t)Ww + 2, (cuuint64_t)Hh + 2, (cuuint64_t)nb};
     const cuuint64_t sA[3] = {(cuuint64_t)C * 2, (cuuint64_t)(Ww + 2) * C * 2, (cuuint64_t)(Hh + 2) * (Ww + 2) * C * 2};
-    const cuuint32_t bA[4] = {64, (cuuint32_t)bw, (cuuint32_t)(128 / bw), 1};
+    const cuuint32_t bA[4] = {(cuuint32_t)ck, (cuuint32_t)bw, (cuuint32_t)(128 / bw), 1};
     const cuuint32_t e4[4] = {1, 1, 1, 1};
     const cuuint64_t gB[2] = {(cuuint64_t)9 * C, (cuuint64_t)cout_p};
     const cuuint64_t sB[1] = {(cuuint64_t)9 * C * 2};
-    const cuuint32_t bB[2] = {64, (cuuint32_t)bn};
-    if (enc(&ta, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 4, padbuf, gA, sA, bA, e4, CU_TENSOR_MAP_INTERLEAVE_NONE,
-            CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
-            CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS ||
+    const cuuint32_t bB[2] = {(cuuint32_t)ck, (cuuint32_t)bn};
+    const CUtensorMapSwizzle sw = ck == 64 ? CU_TENSOR_MAP_SWIZZLE_128B
+                                           : (ck == 32 ? CU_TENSOR_MAP_SWIZZLE_64B : CU_TENSOR_MAP_SWIZZLE_32B);
+    if (enc(&ta, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 4, padbuf, gA, sA, bA, e4, CU_TENSOR_MAP_INTERLEAVE_NONE, sw,
+            CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS ||
         enc(&tb, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, const_cast<bf16*>(w), gB, sB, bB, e4,
-            CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+            CU_TENSOR_MAP_INTERLEAVE_NONE, sw, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
             CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
       return false;
     const dim3 grid(tiles, cout_p / bn);
-    switch (bn) {
-      case 32: launch_tma<32>(grid, ta, tb, in, bias, cout, relu, ob, cout_p, of, nout); break;
-      case 64: launch_tma<64>(grid, ta, tb, in, bias, cout, relu, ob, cout_p, of, nout); break;
-      default: launch_tma<128>(grid, ta, tb, in, bias, cout, relu, ob, cout_p, of, nout); break;
-    }
+    auto go = [&](auto ckc) {
+      constexpr int CK = decltype(ckc)::value;
+      switch (bn) {
+        case 16: launch_tma<16, CK>(grid, ta, tb, in, bias, cout, relu, ob, cout_p, of, nout); break;
+        case 32: launch_tma<32, CK>(grid, ta, tb, in, bias, cout, relu, ob, cout_p, of, nout); break;
+        case 64: launch_tma<64, CK>(grid, ta, tb, in, bias, cout, relu, ob, cout_p, of, nout); break;
+        default: launch_tma<128, CK>(grid, ta, tb, in, bias, cout, relu, ob, cout_p, of, nout); break;
+      }
+    };
+    if (ck == 64) go(std::integral_constant<int, 64>());
+    else if (ck == 32) go(std::integral_constant<int, 32>());
+    else go(std::integral_constant<int, 16>());
     return true;
   }
   static constexpr int kTmaStages = 4;
-  template <int BN>
+  template <int BN, int CK>
   void launch_tma(dim3 grid, const CUtensorMap& ta, const CUtensorMap& tb, const Tensor& in, const float* bias,
                   int cout, int relu, bf16* ob, int ldo, float* of, int nout) {
-    const size_t smem = (size_t)kTmaStages * (128 * 128 + BN * 128) + 1024;
+    const size_t smem = (size_t)kTmaStages * (128 * CK * 2 + BN * CK * 2) + 1024;
     static bool attr = false;
     if (!attr) {
-      cudaFuncSetAttribute(k_conv_tma<BN, kTmaStages>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+      cudaFuncSetAttribute(k_conv_tma<BN, kTmaStages, CK>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
       attr = true;
     }
-    k_conv_tma<BN, kTmaStages><<<grid, 128, smem, st>>>(ta, tb, in.h, in.w, nb, in.c, bias, cout, relu, ob, ldo, of,
-                                                         nout, err);
+    k_conv_tma<BN, kTmaStages, CK><<<grid, 128, smem, st>>>(ta, tb, in.h, in.w, nb, in.c, bias, cout, relu, ob, ldo,
+                                                             of, nout, err);
   }
   // The row-block kernel for narrow layers when the shape allows it.
   bool conv_rows(const Tensor& in, const bf16* w, int cout_p, int cout, const float* bias, int relu, bf16* ob,

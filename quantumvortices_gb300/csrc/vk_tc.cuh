@@ -52,6 +52,21 @@ __device__ __forceinline__ uint64_t smem_desc_sw128(uint32_t addr) {
   return d;
 }
 
+// The same for rows of CK BF16 (CK = 16, 32, 64: the 32-, 64- or 128-byte
+// swizzle of a TMA box whose inner extent is CK elements); 8-row groups are
+// 8 * 2 CK bytes apart, and the tile starts on that boundary.
+template <int CK> __device__ __forceinline__ uint64_t smem_desc_swk(uint32_t addr) {
+  static_assert(CK == 16 || CK == 32 || CK == 64, "swizzle span");
+  constexpr uint64_t mode = CK == 64 ? 2 : (CK == 32 ? 4 : 6);
+  uint64_t d = 0;
+  d |= (uint64_t)((addr & 0x3FFFF) >> 4);
+  d |= (uint64_t)1 << 16;
+  d |= (uint64_t)((16 * CK) >> 4) << 32;
+  d |= (uint64_t)1 << 46;
+  d |= mode << 61;
+  return d;
+}
+
 // kind::f16 instruction descriptor: D = F32, A = B = BF16, both K-major.
 __device__ __forceinline__ uint32_t idesc_bf16(int m, int n) {
   return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(n >> 3) << 17) | ((uint32_t)(m >> 4) << 24);

@@ -158,14 +158,18 @@ def test_feature_kernel_matches_numpy():
     net.close()
 
 
-@pytest.mark.parametrize("h,base,levels", [(128, 32, 3), (64, 32, 4)])
-def test_tma_conv_matches_cp_async_conv(h, base, levels):
+@pytest.mark.parametrize("h,base,levels,narrow", [(128, 32, 3, False), (64, 32, 4, False), (128, 16, 3, True)])
+def test_tma_conv_matches_cp_async_conv(h, base, levels, narrow):
     """Layers whose input has 64k channels run on the TMA-fed kernel
     (VK_CONV_TMA=1: periodic padding, TMA tiles in the 128-byte swizzle
-    layout, 4-stage mbarrier ring); the same K order as the cp.async kernel,
-    so forward outputs and gradients agree to FP32 rounding (a batch of 2)."""
+    layout, 4-stage mbarrier ring), and with VK_CONV_TMA_NARROW=1 the 16- and
+    32-channel layers too (32- and 64-byte swizzle); the K order is that of
+    the cp.async kernels, so forward outputs and gradients agree to FP32
+    rounding (a batch of 2)."""
     import os
     torch = pytest.importorskip("torch")
+    if narrow:
+        os.environ["VK_CONV_TMA_NARROW"] = "1"
     data = [_data(h, seed=30 + i) for i in range(2)]
     xb = torch.stack([d[2] for d in data]).contiguous()
     yb = torch.stack([d[3] for d in data]).contiguous()
@@ -182,5 +186,6 @@ def test_tma_conv_matches_cp_async_conv(h, base, levels):
         loss, g = net.loss_grad(xb, yb)
         res.append((out.cpu().numpy(), loss, g))
         net.close()
+    os.environ.pop("VK_CONV_TMA_NARROW", None)
     (o0, l0, g0), (o1, l1, g1) = res
     assert rel(o1, o0) < 1e-5 and abs(l1 - l0) <= 1e-5 * l0 and rel(g1, g0) < 1e-4
