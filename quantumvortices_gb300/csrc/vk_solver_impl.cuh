@@ -171,6 +171,8 @@ class Solver : public SolverBase {
     c_.xsingle = 0;
     const char* xs_env = std::getenv("VK_XSPLIT");
     if (std::is_same<T, double>::value && nx_ == 1024 && !(xs_env && xs_env[0] == '0')) c_.xsingle = ny_;
+    // VK_XSPLIT=1: single rows in every x pass with nx >= 128 (timing comparisons)
+    if (xs_env && xs_env[0] == '1' && nx_ >= 128) c_.xsingle = ny_;
     {
       int frc = init_fused();
       if (frc) return frc;
