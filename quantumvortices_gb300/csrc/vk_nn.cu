@@ -324,6 +324,163 @@ __global__ void __launch_bounds__(128) k_conv_tma(const __grid_constant__ CUtens
   if (warp == 0) tc::tmem_dealloc(taddr, NCOL);
 }
 
+// Channel-major copies for the TMA-fed weight gradient.  A block moves a
+// 32-pixel x 32-channel tile through shared memory (coalesced on both sides).
+// SHIFT = false: NHWC [nimg][H][W][C] -> [nimg][C][H][W]; with db, also
+// db[c] += sum over the pixels of in[.][c] for c < nbias (the bias gradient).
+// SHIFT = true: the three x-shifted, y-padded copies
+// out[dx][nimg][C][H+2][W] = in[.][(y - 1) mod H][(x + dx - 1) mod W][.],
+// dx = 0, 1, 2, so that every tap of a 64-pixel row chunk starts on a 64-pixel
+// boundary (TMA wants the innermost coordinate on a 16-byte boundary).
+template <bool SHIFT>
+__global__ void __launch_bounds__(256) k_chw(const bf16* __restrict__ in, bf16* __restrict__ out, int H, int W, int C,
+                                             int nimg, float* __restrict__ db, int nbias) {
+  __shared__ float t[34][33];
+  __shared__ float red[8][32];
+  const int Hp = SHIFT ? H + 2 : H;
+  const int xt = blockIdx.x * 32, c0 = blockIdx.y * 32;
+  const int b = blockIdx.z / Hp, yp = blockIdx.z - b * Hp;
+  const int ys = SHIFT ? (yp == 0 ? H - 1 : (yp == H + 1 ? 0 : yp - 1)) : yp;
+  const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
+  constexpr int NX = SHIFT ? 34 : 32;  // pixels xt - 1 .. xt + 32 when shifted
+  float acc = 0.f;
+  for (int i = ty; i < NX; i += 8) {
+    int xs = SHIFT ? xt - 1 + i : xt + i;
+    xs = xs < 0 ? xs + W : (xs >= W ? xs - W : xs);
+    float v = 0.f;
+    if (c0 + tx < C) v = __bfloat162float(in[(((size_t)b * H + ys) * W + xs) * C + c0 + tx]);
+    if (!SHIFT) acc += v;
+    t[i][tx] = v;
+  }
+  if (db) red[ty][tx] = acc;
+  __syncthreads();
+  for (int j = ty; j < 32; j += 8) {
+    const int c = c0 + j, x = xt + tx;
+    if (c >= C) continue;
+    if (SHIFT) {
+      const size_t plane = (size_t)nimg * C * Hp * W;
+#pragma unroll
+      for (int dx = 0; dx < 3; ++dx)
+        out[dx * plane + (((size_t)b * C + c) * Hp + yp) * W + x] = __float2bfloat16(t[tx + dx][j]);
+    } else {
+      out[(((size_t)b * C + c) * Hp + yp) * W + x] = __float2bfloat16(t[tx][j]);
+    }
+  }
+  if (db && ty == 0 && c0 + tx < nbias) {
+    float s2 = 0.f;
+    for (int k = 0; k < 8; ++k) s2 += red[k][tx];
+    atomicAdd(&db[c0 + tx], s2);
+  }
+}
+
+// Weight gradient on TMA-fed tiles: dW[m][n] += sum over this CTA's pixels q
+// of X[q + off(tap)][ci] dY[q][n], m = tap Cin + ci.  X comes from its three
+// x-shifted, y-padded channel-major copies [3][nimg][Cin][H+2][W] and dY from
+// its channel-major copy [nimg][N][H][W], so for a chunk of 64 pixels of one
+// image row every (tap, channel block) of the A tile and the whole B tile are
+// rectangular boxes, starting on 64-pixel boundaries, that TMA loads,
+// pixel-contiguous (K-major), in the 128-byte swizzle layout.  A tile of 128 rows takes 128/CB boxes of
+// CB = min(Cin, 128) channels (one tap each).  Ring, roles, bounded waits and
+// the timeout path as in k_conv_tma; the FP32 result is added to dW with
+// atomics (the pixel range of a launch is split over blockIdx.y).
+template <int BN, int S>
+__global__ void __launch_bounds__(128) k_wgrad_tma(const __grid_constant__ CUtensorMap tmX,
+                                                   const __grid_constant__ CUtensorMap tmD, int H, int W, int nimg,
+                                                   int Cin, int pix_per_cta, float* __restrict__ dW,
+                                                   int* __restrict__ err) {
+  constexpr int ABYTES = 128 * 128, BBYTES = BN * 128, STAGE = ABYTES + BBYTES;
+  static_assert(STAGE % 1024 == 0, "1024-byte aligned stages");
+  extern __shared__ __align__(1024) unsigned char smraw[];
+  __shared__ __align__(8) uint64_t full[S], empty[S], done;
+  __shared__ uint32_t tslot;
+  __shared__ int s_loaded;
+  unsigned char* sm = smraw + ((1024 - (tc::smem_u32(smraw) & 1023)) & 1023);
+  const int tid = threadIdx.x, warp = tid >> 5;
+  const int npix = nimg * H * W, M = 9 * Cin;
+  const int m0 = blockIdx.x * 128;
+  const int q0 = blockIdx.y * pix_per_cta, q1 = min(npix, q0 + pix_per_cta);
+  const int nck = q1 > q0 ? (q1 - q0) / 64 : 0;
+  const int CB = Cin < 128 ? Cin : 128;
+  constexpr uint32_t NCOL = BN < 32 ? 32 : BN;
+  if (warp == 0) tc::tmem_alloc(&tslot, NCOL);
+  if (tid == 0) {
+    for (int i = 0; i < S; ++i) {
+      tc::mbar_init(&full[i]);
+      tc::mbar_init(&empty[i]);
+    }
+    tc::mbar_init(&done);
+    s_loaded = 0;
+  }
+  tc::fence_before();
+  __syncthreads();
+  tc::fence_after();
+  const uint32_t taddr = tslot;
+  const uint32_t idesc = tc::idesc_bf16(128, BN);
+  bool ok = true;
+  if (tid == 0) {
+    // A boxes of this M tile: rows [r, r + CB) hold tap m / Cin, channels from m % Cin
+    int i = 0;
+    for (; i < nck && ok; ++i) {
+      const int st = i % S;
+      if (i >= S) ok = tc::mbar_wait(&empty[st], ((i - S) / S) & 1, err);
+      if (!ok) break;
+      const int q = q0 + 64 * i;
+      const int row = q / W, x0 = q - row * W, b = row / H, y = row - b * H;
+      unsigned char* sA = sm + st * STAGE;
+      int nbox = 0;
+      for (int r = 0; r < 128 && m0 + r < M; r += CB) ++nbox;
+      tc::mbar_arrive_expect_tx(&full[st], (uint32_t)(nbox * CB * 128 + BBYTES));
+      for (int r = 0; r < 128 && m0 + r < M; r += CB) {
+        const int m = m0 + r, tap = m / Cin, ci = m - tap * Cin;
+        tc::tma_load_5d(sA + r * 128, &tmX, &full[st], x0, y + tap / 3, ci, b, tap % 3);
+      }
+      tc::tma_load_4d(sA + ABYTES, &tmD, &full[st], x0, y, 0, b);
+    }
+    s_loaded = i;
+  } else if (tid == 32) {
+    for (int i = 0; i < nck && ok; ++i) {
+      const int st = i % S;
+      ok = tc::mbar_wait(&full[st], (i / S) & 1, err);
+      if (!ok) break;
+      tc::fence_after();
+      const uint32_t a0 = tc::smem_u32(sm + st * STAGE);
+#pragma unroll
+      for (int j = 0; j < 4; ++j) {
+        const uint64_t ad = tc::smem_desc_sw128(a0 + 32 * j);
+        const uint64_t bd = tc::smem_desc_sw128(a0 + ABYTES + 32 * j);
+        tc::mma(taddr, ad, bd, idesc, (i > 0 || j > 0) ? 1u : 0u);
+      }
+      tc::commit(&empty[st]);
+    }
+    tc::commit(&done);
+  }
+  __syncthreads();
+  ok = tc::mbar_wait(&done, 0, err) && ok;
+  if (tid == 0 && ld_err_nonzero(err)) {
+    const int loaded = s_loaded;
+    for (int i = loaded - S < 0 ? 0 : loaded - S; i < loaded; ++i) tc::mbar_wait(&full[i % S], (i / S) & 1, err);
+  }
+  tc::fence_after();
+  if (__syncthreads_and(ok) && nck > 0) {
+    const int m = m0 + 32 * warp + (tid & 31);
+    constexpr int NC = BN < 32 ? 16 : 32;
+#pragma unroll 1
+    for (int c0 = 0; c0 < BN; c0 += NC) {
+      float v[32];
+      const uint32_t ta = taddr + ((uint32_t)(32 * warp) << 16) + c0;
+      if (NC == 16) tc::tmem_ld16(ta, v);
+      else tc::tmem_ld32(ta, v);
+      if (m < M)
+#pragma unroll
+        for (int j = 0; j < NC; j += 4)
+          atomicAdd(reinterpret_cast<float4*>(&dW[(size_t)m * BN + c0 + j]), make_float4(v[j], v[j + 1], v[j + 2], v[j + 3]));
+    }
+  }
+  tc::fence_before();
+  __syncthreads();
+  if (warp == 0) tc::tmem_dealloc(taddr, NCOL);
+}
+
 // Periodic padding: out[b][y][x][c] = in[b][(y-1) mod H][(x-1) mod W][c] on
 // the (H+2) x (W+2) stack, 16-byte vectors (C a multiple of 8).
 __global__ void k_pad(const bf16* __restrict__ in, bf16* __restrict__ out, int H, int W, int C, int nimg) {
@@ -899,6 +1056,8 @@ class Net {
   }();
   bf16* padbuf = nullptr;  // periodically padded input of k_conv_tma
   size_t padbuf_n = 0;
+  bf16* xsbuf = nullptr;   // three shifted channel-major input copies (k_wgrad_tma)
+  bf16* dchw = nullptr;    // channel-major output gradient (k_wgrad_tma)
   std::vector<void*> allocs;
   // activations (forward) per level and gradient scratch
   Tensor x0;
@@ -1023,6 +1182,8 @@ class Net {
     for (int l = 0; l < levels; ++l)
       padbuf_n = std::max(padbuf_n, (size_t)bcap * ((H >> l) + 2) * ((W >> l) + 2) * (size_t)(base << (l + 1)));
     padbuf = dalloc<bf16>(padbuf_n);
+    xsbuf = dalloc<bf16>(3 * padbuf_n);
+    dchw = dalloc<bf16>(padbuf_n);
     out_f = dalloc<float>((size_t)H * W * 2 * bcap);
     feat_psi = dalloc<double2>((size_t)H * W);
     feat_pos = dalloc<double>(2 * kMaxVortices);
@@ -1167,7 +1328,66 @@ class Net {
     k_conv<BN><<<grid, 128, smem, st>>>(in.d, in.h, in.w, nb, in.c, w, bias, cout, relu, ob, ldo, of, nout, err);
   }
   // dW GEMM (and, with db, the bias gradient of the nb real channels).
+  // The TMA-fed weight gradient when enabled and the shape allows it: rows of
+  // 64k pixels, Cin dividing 128 or a multiple of it, at most 256 output
+  // channels.  On GB300 the k_wgrad launches took 56% of a 512^2 training
+  // step (batches of 8) at 30-60 TFLOP/s.
+  bool wgrad_tma(const Tensor& in, const bf16* dy, int coutp, float* out, float* db, int nbias) {
+    const int Hh = in.h, Ww = in.w, C = in.c;
+    if (!tma_ok_ || Ww % 64 != 0 || C % 16 != 0 || (128 % C != 0 && C % 128 != 0) || coutp % 16 != 0 ||
+        coutp > 256)
+      return false;
+    if ((size_t)nb * C * (Hh + 2) * Ww > padbuf_n || (size_t)nb * coutp * Hh * Ww > padbuf_n) return false;
+    static EncodeTiled enc = encode_tiled_fn();
+    if (!enc) return false;
+    const int CB = C < 128 ? C : 128;
+    CUtensorMap tx, td;
+    const cuuint64_t gX[5] = {(cuuint64_t)Ww, (cuuint64_t)Hh + 2, (cuuint64_t)C, (cuuint64_t)nb, 3};
+    const cuuint64_t sX[4] = {(cuuint64_t)Ww * 2, (cuuint64_t)(Hh + 2) * Ww * 2, (cuuint64_t)C * (Hh + 2) * Ww * 2,
+                              (cuuint64_t)nb * C * (Hh + 2) * Ww * 2};
+    const cuuint32_t bX[5] = {64, 1, (cuuint32_t)CB, 1, 1};
+    const cuuint64_t gD[4] = {(cuuint64_t)Ww, (cuuint64_t)Hh, (cuuint64_t)coutp, (cuuint64_t)nb};
+    const cuuint64_t sD[3] = {(cuuint64_t)Ww * 2, (cuuint64_t)Hh * Ww * 2, (cuuint64_t)coutp * Hh * Ww * 2};
+    const cuuint32_t bD[4] = {64, 1, (cuuint32_t)coutp, 1};
+    const cuuint32_t e5[5] = {1, 1, 1, 1, 1};
+    if (enc(&tx, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 5, xsbuf, gX, sX, bX, e5, CU_TENSOR_MAP_INTERLEAVE_NONE,
+            CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+            CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS ||
+        enc(&td, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 4, dchw, gD, sD, bD, e5, CU_TENSOR_MAP_INTERLEAVE_NONE,
+            CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+            CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
+      return false;
+    k_chw<true><<<dim3(Ww / 32, (C + 31) / 32, nb * (Hh + 2)), 256, 0, st>>>(in.d, xsbuf, Hh, Ww, C, nb, nullptr, 0);
+    k_chw<false><<<dim3(Ww / 32, (coutp + 31) / 32, nb * Hh), 256, 0, st>>>(dy, dchw, Hh, Ww, coutp, nb, db, nbias);
+    const int npix = nb * Hh * Ww, M = 9 * C;
+    const int mt = (M + 127) / 128;
+    int ppc = 8192;
+    while ((npix + ppc - 1) / ppc * mt < 8 * 152 && ppc > 256) ppc /= 2;
+    cudaMemsetAsync(out, 0, sizeof(float) * (size_t)M * coutp, st);
+    const dim3 grid(mt, (npix + ppc - 1) / ppc);
+    switch (coutp) {
+      case 16: launch_wgrad_tma<16, 4>(grid, tx, td, in, ppc, out); break;
+      case 32: launch_wgrad_tma<32, 4>(grid, tx, td, in, ppc, out); break;
+      case 64: launch_wgrad_tma<64, 4>(grid, tx, td, in, ppc, out); break;
+      case 128: launch_wgrad_tma<128, 4>(grid, tx, td, in, ppc, out); break;
+      case 256: launch_wgrad_tma<256, 3>(grid, tx, td, in, ppc, out); break;
+      default: return false;
+    }
+    return true;
+  }
+  template <int BN, int S>
+  void launch_wgrad_tma(dim3 grid, const CUtensorMap& tx, const CUtensorMap& td, const Tensor& in, int ppc,
+                        float* out) {
+    const size_t smem = (size_t)S * (128 * 128 + BN * 128) + 1024;
+    static bool attr = false;
+    if (!attr) {
+      cudaFuncSetAttribute(k_wgrad_tma<BN, S>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+      attr = true;
+    }
+    k_wgrad_tma<BN, S><<<grid, 128, smem, st>>>(tx, td, in.h, in.w, nb, in.c, ppc, out, err);
+  }
   void wgrad(const Tensor& in, const bf16* dy, int coutp, float* out, float* db, int nbias) {
+    if (wgrad_tma(in, dy, coutp, out, db, nbias)) return;
     const int npix = nb * in.h * in.w, M = 9 * in.c;
     const int mt = (M + 127) / 128;
     int ppc = 8192;
