@@ -871,10 +871,11 @@ __global__ void k_pool_bwd(const bf16* __restrict__ dout, bf16* __restrict__ din
   }
 }
 __global__ void k_up(const bf16* __restrict__ in, bf16* __restrict__ out, int H, int W, int C) {
-  // out is H x W, in is H/2 x W/2
-  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < H * W * C; i += gridDim.x * blockDim.x) {
-    const int c = i % C, p = i / C, y = p / W, x = p % W;
-    out[i] = in[((size_t)(y / 2) * (W / 2) + x / 2) * C + c];
+  // out is H x W, in is H/2 x W/2; 8 channels per thread step
+  const int cv = C / 8;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < H * W * cv; i += gridDim.x * blockDim.x) {
+    const int c = i % cv, p = i / cv, y = p / W, x = p % W;
+    reinterpret_cast<uint4*>(out)[i] = reinterpret_cast<const uint4*>(in)[((size_t)(y / 2) * (W / 2) + x / 2) * cv + c];
   }
 }
 __global__ void k_up_bwd(const bf16* __restrict__ dout, bf16* __restrict__ din, int H, int W, int C) {
@@ -888,14 +889,33 @@ __global__ void k_up_bwd(const bf16* __restrict__ dout, bf16* __restrict__ din, 
     din[i] = __float2bfloat16(s);
   }
 }
+// The elementwise kernels below take 8 BF16 values (16 bytes) per thread
+// step; n is a multiple of 8 (channels are padded to 16).
 __global__ void k_add(const bf16* __restrict__ a, const bf16* __restrict__ b, bf16* __restrict__ o, size_t n) {
-  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
-    o[i] = __float2bfloat16(__bfloat162float(a[i]) + __bfloat162float(b[i]));
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n / 8; i += (size_t)gridDim.x * blockDim.x) {
+    uint4 qa = reinterpret_cast<const uint4*>(a)[i], qb = reinterpret_cast<const uint4*>(b)[i], qo;
+    const __nv_bfloat162* ea = reinterpret_cast<const __nv_bfloat162*>(&qa);
+    const __nv_bfloat162* eb = reinterpret_cast<const __nv_bfloat162*>(&qb);
+    __nv_bfloat162* eo = reinterpret_cast<__nv_bfloat162*>(&qo);
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      const float2 fa = __bfloat1622float2(ea[k]), fb = __bfloat1622float2(eb[k]);
+      eo[k] = __floats2bfloat162_rn(fa.x + fb.x, fa.y + fb.y);
+    }
+    reinterpret_cast<uint4*>(o)[i] = qo;
+  }
 }
 // d_pre = d_post * (y > 0)
 __global__ void k_relu_bwd(const bf16* __restrict__ y, const bf16* __restrict__ d, bf16* __restrict__ o, size_t n) {
-  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
-    o[i] = __bfloat162float(y[i]) > 0.f ? d[i] : __float2bfloat16(0.f);
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n / 8; i += (size_t)gridDim.x * blockDim.x) {
+    uint4 qy = reinterpret_cast<const uint4*>(y)[i], qd = reinterpret_cast<const uint4*>(d)[i], qo;
+    const bf16* ey = reinterpret_cast<const bf16*>(&qy);
+    const bf16* ed = reinterpret_cast<const bf16*>(&qd);
+    bf16* eo = reinterpret_cast<bf16*>(&qo);
+#pragma unroll
+    for (int k = 0; k < 8; ++k) eo[k] = __bfloat162float(ey[k]) > 0.f ? ed[k] : __float2bfloat16(0.f);
+    reinterpret_cast<uint4*>(o)[i] = qo;
+  }
 }
 // MSE loss (mean over the images, pixels and outputs) on the head output
 // (FP32 [p][nout], p over the stacked images) against planar targets
@@ -1442,10 +1462,10 @@ class Net {
     }
     const Tensor* dec = &s[levels - 1];
     for (int l = levels - 2; l >= 0; --l) {
-      k_up<<<blocks(N(u[l])), 256, 0, st>>>(dec->d, u[l].d, nb * u[l].h, u[l].w, u[l].c);
+      k_up<<<blocks(N(u[l]) / 8), 256, 0, st>>>(dec->d, u[l].d, nb * u[l].h, u[l].w, u[l].c);
       const Conv& c1 = convs[ci++];
       conv(u[l], c1.wb, c1.coutp, c1.cout, param + c1.boff, 1, c[l].d, nullptr, 0);
-      k_add<<<blocks(N(e[l])), 256, 0, st>>>(c[l].d, s[l].d, e[l].d, N(e[l]));
+      k_add<<<blocks(N(e[l]) / 8), 256, 0, st>>>(c[l].d, s[l].d, e[l].d, N(e[l]));
       const Conv& c2 = convs[ci++];
       conv(e[l], c2.wb, c2.coutp, c2.cout, param + c2.boff, 1, d[l].d, nullptr, 0);
       dec = &d[l];
@@ -1460,7 +1480,7 @@ class Net {
     const size_t nout = (size_t)nb * in.h * in.w * cv.coutp;
     const bf16* dpre = dpost;
     if (cv.relu) {
-      k_relu_bwd<<<blocks(nout), 256, 0, st>>>(out, dpost, dpre_scratch, nout);
+      k_relu_bwd<<<blocks(nout / 8), 256, 0, st>>>(out, dpost, dpre_scratch, nout);
       dpre = dpre_scratch;
     }
     wgrad(in, dpre, cv.coutp, wscratch, grad + cv.boff, cv.cout);
@@ -1507,7 +1527,7 @@ class Net {
         // d s[l] = pool_bwd(d p[l]) + d e[l] (the skip, stashed in g3[l]);
         // d p[l] sits in g2[l], so the result goes to g1[l]
         k_pool_bwd<<<blocks(N(s[l])), 256, 0, st>>>(gcur, g1[l].d, nb * s[l].h, s[l].w, s[l].c);
-        k_add<<<blocks(N(s[l])), 256, 0, st>>>(g1[l].d, g3[l].d, g1[l].d, N(s[l]));
+        k_add<<<blocks(N(s[l]) / 8), 256, 0, st>>>(g1[l].d, g3[l].d, g1[l].d, N(s[l]));
         ds = g1[l].d;
       }
       const int cs = 2 * l + 1, ca = 2 * l;
