@@ -324,10 +324,10 @@ __global__ void __launch_bounds__(128) k_conv_tma(const __grid_constant__ CUtens
   if (warp == 0) tc::tmem_dealloc(taddr, NCOL);
 }
 
-// Channel-major copies for the TMA-fed weight gradient.  A block moves a
-// 64-pixel x 64-channel tile of one image row through shared memory with
-// 16-byte loads (8 channels of a pixel) and 16-byte stores (8 pixels of a
-// channel).  W must be a multiple of 64 and C of 8.
+// Channel-major copies for the TMA-fed weight gradient.  A block moves
+// 64-pixel x 64-channel tiles of 8 consecutive image rows through shared
+// memory with 16-byte loads (8 channels of a pixel) and 16-byte stores (8
+// pixels of a channel).  W must be a multiple of 64 and C of 8.
 // SHIFT = false: NHWC [nimg][H][W][C] -> [nimg][C][H][W]; with db, also
 // db[c] += sum over the pixels of in[.][c] for c < nbias (the bias gradient).
 // SHIFT = true: the three x-shifted, y-padded copies
@@ -339,28 +339,34 @@ __global__ void __launch_bounds__(256) k_chw(const bf16* __restrict__ in, bf16* 
                                              int nimg, float* __restrict__ db, int nbias) {
   constexpr int NX = SHIFT ? 66 : 64;   // pixels x0 - 1 .. x0 + 64 when shifted
   constexpr int SP = 72;                // row pitch (bf16) of the channel-major tile
+  constexpr int ROWS = 8;               // image rows per block (one bias atomic per channel and block)
   __shared__ __align__(16) bf16 t[64][SP];
   const int Hp = SHIFT ? H + 2 : H;
   const int x0 = blockIdx.x * 64, c0 = blockIdx.y * 64;
-  const int b = blockIdx.z / Hp, yp = blockIdx.z - b * Hp;
-  const int ys = SHIFT ? (yp == 0 ? H - 1 : (yp == H + 1 ? 0 : yp - 1)) : yp;
   const int nc = min(64, C - c0);  // channels of this tile (a multiple of 8)
-  for (int v = threadIdx.x; v < NX * 8; v += blockDim.x) {
-    const int i = v >> 3, g = v & 7;
-    if (8 * g >= nc) continue;
-    int xs = SHIFT ? x0 - 1 + i : x0 + i;
-    xs = xs < 0 ? xs + W : (xs >= W ? xs - W : xs);
-    const uint4 q = *reinterpret_cast<const uint4*>(in + (((size_t)b * H + ys) * W + xs) * C + c0 + 8 * g);
-    const bf16* e = reinterpret_cast<const bf16*>(&q);
-#pragma unroll
-    for (int k = 0; k < 8; ++k) t[8 * g + k][i] = e[k];
-  }
-  __syncthreads();
   const size_t plane = (size_t)nimg * C * Hp * W;
-  for (int v = threadIdx.x; v < 64 * 8; v += blockDim.x) {
-    const int c = v >> 3, pg = v & 7;
-    float sum = 0.f;
-    if (c < nc) {
+  float sum[2] = {0.f, 0.f};
+  const int r1 = min((int)(blockIdx.z + 1) * ROWS, nimg * Hp);
+  for (int row = blockIdx.z * ROWS; row < r1; ++row) {
+    const int b = row / Hp, yp = row - b * Hp;
+    const int ys = SHIFT ? (yp == 0 ? H - 1 : (yp == H + 1 ? 0 : yp - 1)) : yp;
+    __syncthreads();  // the previous row's tile has been read
+    for (int v = threadIdx.x; v < NX * 8; v += blockDim.x) {
+      const int i = v >> 3, g = v & 7;
+      if (8 * g >= nc) continue;
+      int xs = SHIFT ? x0 - 1 + i : x0 + i;
+      xs = xs < 0 ? xs + W : (xs >= W ? xs - W : xs);
+      const uint4 q = *reinterpret_cast<const uint4*>(in + (((size_t)b * H + ys) * W + xs) * C + c0 + 8 * g);
+      const bf16* e = reinterpret_cast<const bf16*>(&q);
+#pragma unroll
+      for (int k = 0; k < 8; ++k) t[8 * g + k][i] = e[k];
+    }
+    __syncthreads();
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {
+      const int v = threadIdx.x + 256 * h;
+      const int c = v >> 3, pg = v & 7;
+      if (c >= nc) continue;
 #pragma unroll
       for (int dx = 0; dx < (SHIFT ? 3 : 1); ++dx) {
         uint4 q;
@@ -369,16 +375,21 @@ __global__ void __launch_bounds__(256) k_chw(const bf16* __restrict__ in, bf16* 
         for (int k = 0; k < 8; ++k) e[k] = t[c][8 * pg + k + dx];
         if (!SHIFT)
 #pragma unroll
-          for (int k = 0; k < 8; ++k) sum += __bfloat162float(e[k]);
+          for (int k = 0; k < 8; ++k) sum[h] += __bfloat162float(e[k]);
         *reinterpret_cast<uint4*>(out + dx * plane + (((size_t)b * C + c0 + c) * Hp + yp) * W + x0 + 8 * pg) = q;
       }
     }
-    if (!SHIFT && db) {
+  }
+  if (!SHIFT && db) {
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {
       // the 8 threads of channel c are consecutive lanes
-      sum += __shfl_xor_sync(0xffffffffu, sum, 1);
-      sum += __shfl_xor_sync(0xffffffffu, sum, 2);
-      sum += __shfl_xor_sync(0xffffffffu, sum, 4);
-      if (pg == 0 && c < nc && c0 + c < nbias) atomicAdd(&db[c0 + c], sum);
+      float x = sum[h];
+      x += __shfl_xor_sync(0xffffffffu, x, 1);
+      x += __shfl_xor_sync(0xffffffffu, x, 2);
+      x += __shfl_xor_sync(0xffffffffu, x, 4);
+      const int v = threadIdx.x + 256 * h, c = v >> 3;
+      if ((v & 7) == 0 && c < nc && c0 + c < nbias) atomicAdd(&db[c0 + c], x);
     }
   }
 }
@@ -1387,8 +1398,10 @@ class Net {
             CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
             CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
       return false;
-    k_chw<true><<<dim3(Ww / 64, (C + 63) / 64, nb * (Hh + 2)), 256, 0, st>>>(in.d, xsbuf, Hh, Ww, C, nb, nullptr, 0);
-    k_chw<false><<<dim3(Ww / 64, (coutp + 63) / 64, nb * Hh), 256, 0, st>>>(dy, dchw, Hh, Ww, coutp, nb, db, nbias);
+    k_chw<true><<<dim3(Ww / 64, (C + 63) / 64, (nb * (Hh + 2) + 7) / 8), 256, 0, st>>>(in.d, xsbuf, Hh, Ww, C, nb,
+                                                                                      nullptr, 0);
+    k_chw<false><<<dim3(Ww / 64, (coutp + 63) / 64, (nb * Hh + 7) / 8), 256, 0, st>>>(dy, dchw, Hh, Ww, coutp, nb, db,
+                                                                                     nbias);
     const int npix = nb * Hh * Ww, M = 9 * C;
     const int mt = (M + 127) / 128;
     int ppc = 8192;
