@@ -69,3 +69,24 @@ def test_ensemble_fp32_config_shape_sample_vs_oracle():
             o.set_psi(psis[m], otoc=True)
             o.gpe_rk4(100)
             assert rel(e.get_psi(m), o.get_psi()) < 1e-5
+
+
+@pytest.mark.parametrize("prec", [vk.VK_PREC_FP64, vk.VK_PREC_FP32])
+def test_persistent_stage_kernel_equals_pass_kernels(prec, monkeypatch):
+    """VK_FUSED=1 makes the ensemble step with kb_stage (one cooperative launch
+    per RK4 stage over every member, bounded grid barriers), VK_FUSED=0 with
+    the four pass kernels: the same device bodies on the same tiles' columns
+    and rows, so the members agree bit for bit."""
+    sizes = [128, 256, 512, 256]
+    ps, psis = _members(sizes, prec)
+    out = {}
+    for flag in ("1", "0"):
+        monkeypatch.setenv("VK_FUSED", flag)
+        with vk.Ensemble(ps) as e:
+            assert ("-> persistent" if flag == "1" else "-> pass kernels") in e.report
+            for m, psi in enumerate(psis):
+                e.set_psi(m, psi)
+            e.gpe_rk4(6)
+            out[flag] = [e.get_psi(m) for m in range(len(sizes))]
+    for a, b in zip(out["1"], out["0"]):
+        assert np.array_equal(a, b)
