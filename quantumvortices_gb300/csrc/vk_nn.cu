@@ -1309,17 +1309,20 @@ class Net {
     else go(std::integral_constant<int, 16>());
     return true;
   }
-  static constexpr int kTmaStages = 4;
+  // Ring depth: 3 stages for 128-channel tiles (two CTAs per SM, so one
+  // CTA's epilogue overlaps the other's MMAs), 4 for narrower ones.
+  template <int BN> static constexpr int tma_stages() { return BN >= 128 ? 3 : 4; }
   template <int BN, int CK>
   void launch_tma(dim3 grid, const CUtensorMap& ta, const CUtensorMap& tb, const Tensor& in, const float* bias,
                   int cout, int relu, bf16* ob, int ldo, float* of, int nout) {
-    const size_t smem = (size_t)kTmaStages * (128 * CK * 2 + BN * CK * 2) + 1024;
+    constexpr int S = tma_stages<BN>();
+    const size_t smem = (size_t)S * (128 * CK * 2 + BN * CK * 2) + 1024;
     static bool attr = false;
     if (!attr) {
-      cudaFuncSetAttribute(k_conv_tma<BN, kTmaStages, CK>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+      cudaFuncSetAttribute(k_conv_tma<BN, S, CK>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
       attr = true;
     }
-    k_conv_tma<BN, kTmaStages, CK><<<grid, 128, smem, st>>>(ta, tb, in.h, in.w, nb, in.c, bias, cout, relu, ob, ldo,
+    k_conv_tma<BN, S, CK><<<grid, 128, smem, st>>>(ta, tb, in.h, in.w, nb, in.c, bias, cout, relu, ob, ldo,
                                                              of, nout, err);
   }
   // The row-block kernel for narrow layers when the shape allows it.
@@ -1412,7 +1415,7 @@ class Net {
       case 16: launch_wgrad_tma<16, 4>(grid, tx, td, in, ppc, out); break;
       case 32: launch_wgrad_tma<32, 4>(grid, tx, td, in, ppc, out); break;
       case 64: launch_wgrad_tma<64, 4>(grid, tx, td, in, ppc, out); break;
-      case 128: launch_wgrad_tma<128, 4>(grid, tx, td, in, ppc, out); break;
+      case 128: launch_wgrad_tma<128, 3>(grid, tx, td, in, ppc, out); break;  // two CTAs per SM
       case 256: launch_wgrad_tma<256, 3>(grid, tx, td, in, ppc, out); break;
       default: return false;
     }
