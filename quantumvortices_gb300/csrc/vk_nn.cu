@@ -1309,9 +1309,9 @@ class Net {
     else go(std::integral_constant<int, 16>());
     return true;
   }
-  // Ring depth: 3 stages for 128-channel tiles (two CTAs per SM, so one
-  // CTA's epilogue overlaps the other's MMAs), 4 for narrower ones.
-  template <int BN> static constexpr int tma_stages() { return BN >= 128 ? 3 : 4; }
+  // Ring depth: 3 stages for tiles of 64 or more channels (two or three CTAs
+  // per SM, so one CTA's epilogue overlaps another's MMAs), 4 for narrower.
+  template <int BN> static constexpr int tma_stages() { return BN >= 64 ? 3 : 4; }
   template <int BN, int CK>
   void launch_tma(dim3 grid, const CUtensorMap& ta, const CUtensorMap& tb, const Tensor& in, const float* bias,
                   int cout, int relu, bf16* ob, int ldo, float* of, int nout) {
