@@ -413,6 +413,10 @@ def grid4096_bench(torch, steps=5):
         e1.record(ext)
         torch.cuda.synchronize()
         out[nm] = n * n * steps / (e0.elapsed_time(e1) * 1e-3)
+        s.timing_begin()
+        s.gpe_rk4(1)
+        per = s.timing_end()
+        out[nm + "_kernel_ms"] = {k: round(v[0] / v[1], 5) for k, v in per.items()}
         s.set_psi_vortices(1024, 11, xi0, min_sep=4 * xi0)
         s.gpe_rk4(100)
         psis[nm] = s.get_psi()
