@@ -23,6 +23,12 @@
 #include <mutex>
 #include <unordered_set>
 #include "vk_fft.cuh"
+#ifdef __CUDACC__
+#include "vk_bulk.cuh"
+#define VK_HAVE_BULK 1
+#else
+#define VK_HAVE_BULK 0  // host builds of the pass bodies: element-wise loads only
+#endif
 
 namespace vk {
 
@@ -48,8 +54,9 @@ inline void ensure_smem_attr(const void* fn, size_t dyn_bytes) {
 // half-height paired transforms radix-8 stages on the same threads.  The
 // FP32 x passes at L = 1024 use one warp per row (NT = 32 R) and the
 // warp-per-row transform of vk_fft.cuh; the FP64 y passes at L = 1024 run
-// four warps per row (8 points per thread); the choice of geometry and of
-// the transform per pass follows timings on GB300.
+// four warps per row (8 points per thread); at L = 4096 the FP32 passes cap
+// their registers for two (x) and three (y) CTAs per SM; the choice of
+// geometry and of the transform per pass follows timings on GB300.
 // MINB is the CTAs per SM the register budget is sized for.
 template <typename T, int L> struct GeoX;
 template <typename T, int L> struct GeoY;
@@ -67,14 +74,28 @@ VK_GEO(GeoY, double, 128, 2, 8) VK_GEO(GeoY, double, 256, 1, 8) VK_GEO(GeoY, dou
 VK_GEOE(GeoY, double, 1024, 1, 5, 8) VK_GEO(GeoY, double, 2048, 1, 4) VK_GEO(GeoY, double, 4096, 1, 2)
 VK_GEO(GeoX, float, 16, 16, 4) VK_GEO(GeoX, float, 32, 16, 4) VK_GEO(GeoX, float, 64, 16, 4)
 VK_GEO(GeoX, float, 128, 8, 4) VK_GEO(GeoX, float, 256, 4, 4) VK_GEO(GeoX, float, 512, 2, 8)
-VK_GEOE(GeoX, float, 1024, 4, 2, 32) VK_GEO(GeoX, float, 2048, 2, 2) VK_GEO(GeoX, float, 4096, 2, 1)
+VK_GEOE(GeoX, float, 1024, 4, 2, 32) VK_GEO(GeoX, float, 2048, 2, 2) VK_GEO(GeoX, float, 4096, 2, 2)
 VK_GEO(GeoY, float, 16, 16, 4) VK_GEO(GeoY, float, 32, 8, 8) VK_GEO(GeoY, float, 64, 4, 8)
 VK_GEO(GeoY, float, 128, 2, 8) VK_GEO(GeoY, float, 256, 1, 8) VK_GEO(GeoY, float, 512, 1, 8)
-VK_GEO(GeoY, float, 1024, 1, 8) VK_GEO(GeoY, float, 2048, 1, 4) VK_GEO(GeoY, float, 4096, 1, 2)
+VK_GEO(GeoY, float, 1024, 1, 8) VK_GEO(GeoY, float, 2048, 1, 4) VK_GEO(GeoY, float, 4096, 1, 3)
 #undef VK_GEO
 #undef VK_GEOE
 
 __device__ __forceinline__ int kwn(int i, int n) { return i < n / 2 ? i : i - n; }
+
+// Programmatic dependent launch.  The RK4 pass kernels (k_x1, k_y1, k_x2,
+// k_y2_rk4, k_xinv) may be launched with programmatic stream serialization:
+// their CTAs can then be scheduled while the previous kernel's last CTAs
+// run.  Each waits for the previous kernel to complete (its writes visible)
+// before it touches any field, so the ordering of the passes is that of a
+// plain stream; with an ordinary launch the wait returns at once.  Once all
+// of its own CTAs are running, a pass lets the next one be scheduled.
+__device__ __forceinline__ void pdl_enter() {
+#if defined(__CUDA_ARCH__)
+  asm volatile("griddepcontrol.wait;" ::: "memory");
+  asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+#endif
+}
 
 // Row index of logical row l when only |kx| <= K rows are processed.
 __device__ __forceinline__ int pruned_row(int l, int K, int n) { return l <= K ? l : n - (2 * K + 1 - l); }
@@ -107,6 +128,25 @@ __device__ __forceinline__ void stage_rows(cplx<T>* __restrict__ s, F fetch) {
   }
 }
 
+#if VK_HAVE_BULK
+// FP64 row tiles by bulk copies (vk_bulk.cuh): rows r < nr of the tile come
+// from row_of(r) (L contiguous values), rows nr <= r < NR are zeroed.  Every
+// thread must call it; false: a wait ran out, the caller must return.
+template <int L, int NR, int NT, int LP, class RowOf>
+__device__ __forceinline__ bool bulk_rows(double2* __restrict__ s, RowOf row_of, int nr, int* err,
+                                          unsigned long long limit) {
+  __shared__ uint64_t bar;
+  bulk_begin(&bar, (uint32_t)(nr * L * sizeof(double2)));
+#pragma unroll 1
+  for (int r = 0; r < NR; ++r) {
+    if (r < nr) bulk_row_range<NT>(s + r * LP, row_of(r), 0, L, &bar);
+    else
+      for (int k = threadIdx.x; k < L; k += NT) s[r * LP + pidx(k)] = make_double2(0.0, 0.0);
+  }
+  return bulk_wait(&bar, err, limit);
+}
+#endif
+
 // Scalars shared by the passes (by value in the launch).
 struct StepConsts {
   int nx, ny;        // grid
@@ -136,6 +176,10 @@ struct StepConsts {
   const double* omega_dev;
   double sgle_amp, sqrt_dt, ktrunc2;
   int selftrunc;
+  // Bulk row loads (FP64): the error word a CTA sets when its bounded wait
+  // for the row's copies runs out, and the poll limit.
+  int* async_err;
+  unsigned long long async_limit;
 };
 
 // Counter-based uniform [0,1) of the forcing phases (SplitMix64 finaliser of
@@ -270,6 +314,7 @@ template <typename T, int L, bool PRUNE>
 __global__ void __launch_bounds__(GeoX<T, L>::NT, GeoX<T, L>::MINB) k_xinv(const cplx<T>* __restrict__ src, cplx<T>* __restrict__ dst,
                                                      const cplx<T>* __restrict__ tw, T scale, int K) {
   extern __shared__ __align__(16) unsigned char smraw[];
+  pdl_enter();
   xinv_body<T, L, GeoX<T, L>, PRUNE>(src, dst, tw, scale, K, blockIdx.x, reinterpret_cast<cplx<T>*>(smraw));
 }
 
@@ -357,7 +402,9 @@ __device__ __forceinline__ void x1_body(const cplx<T>* __restrict__ Ta, cplx<T>*
 // twiddle table, and is unpacked with
 //   E(k) = (Z(k) + conj Z(L/2-k))/2,  O(k) = -i (Z(k) - conj Z(L/2-k))/2,
 //   rho^(k) = E(k) + W_L^k O(k),  k in [0, K] (K < L/2).
-template <typename T, int L, class G, bool FROM_T, bool PRUNE, bool SPREAD = false>
+//   BULK (FP64): the row arrives by bulk copies (vk_bulk.cuh) instead of
+//   element-wise loads; the pruned band K < k < L-K is zeroed in shared memory.
+template <typename T, int L, class G, bool FROM_T, bool PRUNE, bool SPREAD = false, bool BULK = false>
 __device__ __forceinline__ void x1_single_body(const cplx<T>* __restrict__ Ta, cplx<T>* __restrict__ psi,
                                                cplx<T>* __restrict__ Tb, const cplx<T>* __restrict__ tw,
                                                StepConsts c, const int y, cplx<T>* __restrict__ s) {
@@ -366,13 +413,29 @@ __device__ __forceinline__ void x1_single_body(const cplx<T>* __restrict__ Ta, c
   constexpr bool SP = SPREAD && H / G::NT >= 4;  // all threads in both transforms
   constexpr int NA = SP || G::NT < L / 16 ? G::NT : L / 16;  // threads of the L-point transform
   constexpr int NH = SP || G::NT < H / 8 ? G::NT : H / 8;    // threads of the L/2-point transform
+  static_assert(!BULK || (VK_HAVE_BULK && sizeof(T) == 8), "bulk row loads: FP64 device code");
   const int ny = c.ny, K = c.K;
+  if constexpr (BULK) {
+#if VK_HAVE_BULK
+    __shared__ uint64_t bar;
+    const int kin = FROM_T && PRUNE ? K + 1 : L;  // copied: [0, kin) and, pruned, [L-K, L)
+    bulk_begin(&bar, (uint32_t)((FROM_T && PRUNE ? 2 * K + 1 : L) * sizeof(C)));
+    const C* row = (FROM_T ? Ta : psi) + (size_t)y * L;
+    bulk_row_range<G::NT>(s, row, 0, kin, &bar);
+    if (FROM_T && PRUNE) {
+      bulk_row_range<G::NT>(s, row, L - K, L, &bar);
+      for (int k = kin + threadIdx.x; k < L - K; k += G::NT) s[pidx(k)] = mkc<T>(T(0), T(0));
+    }
+    if (!bulk_wait(&bar, c.async_err, c.async_limit)) return;
+#endif
+  }
   if (FROM_T) {
-    stage_rows<T, L, 1, G::NT, G::LP>(s, [&](int, int k) {
-      C v = mkc<T>(T(0), T(0));
-      if (!PRUNE || k <= K || k >= L - K) v = Ta[(size_t)y * L + k];
-      return v;
-    });
+    if constexpr (!BULK)
+      stage_rows<T, L, 1, G::NT, G::LP>(s, [&](int, int k) {
+        C v = mkc<T>(T(0), T(0));
+        if (!PRUNE || k <= K || k >= L - K) v = Ta[(size_t)y * L + k];
+        return v;
+      });
     __syncthreads();
     fft_rows<T, L, 1, NA, +1, G::NT>(s, tw);
     const T scale = T(c.scale);
@@ -381,7 +444,7 @@ __device__ __forceinline__ void x1_single_body(const cplx<T>* __restrict__ Ta, c
       s[pidx(x)] = v;
       psi[(size_t)y * L + x] = v;
     }
-  } else {
+  } else if constexpr (!BULK) {
     stage_rows<T, L, 1, G::NT, G::LP>(s, [&](int, int x) { return psi[(size_t)y * L + x]; });
   }
   __syncthreads();
@@ -409,33 +472,46 @@ __device__ __forceinline__ void x1_single_body(const cplx<T>* __restrict__ Ta, c
   }
 }
 
-template <typename T, int L, bool FROM_T, bool PRUNE>
+// BULK (FP64): the single-row CTAs load their row by bulk copies.
+template <typename T, int L, bool FROM_T, bool PRUNE, bool BULK = false>
 __global__ void __launch_bounds__(GeoX<T, L>::NT, GeoX<T, L>::MINB) k_x1(const cplx<T>* __restrict__ Ta, cplx<T>* __restrict__ psi,
                                                    cplx<T>* __restrict__ Tb, const cplx<T>* __restrict__ tw,
                                                    StepConsts c) {
   extern __shared__ __align__(16) unsigned char smraw[];
+  pdl_enter();
   const int npair = (int)gridDim.x - c.xsingle;
   if (L < 128 || (int)blockIdx.x < npair)
     x1_body<T, L, GeoX<T, L>, FROM_T, PRUNE>(Ta, psi, Tb, tw, c, blockIdx.x, reinterpret_cast<cplx<T>*>(smraw));
   else if constexpr (L >= 128)
-    x1_single_body<T, L, GeoX<T, L>, FROM_T, PRUNE>(Ta, psi, Tb, tw, c, GeoX<T, L>::R * npair + ((int)blockIdx.x - npair),
-                                                    reinterpret_cast<cplx<T>*>(smraw));
+    x1_single_body<T, L, GeoX<T, L>, FROM_T, PRUNE, false, BULK>(
+        Ta, psi, Tb, tw, c, GeoX<T, L>::R * npair + ((int)blockIdx.x - npair), reinterpret_cast<cplx<T>*>(smraw));
 }
 
 // ------------------------------------------------------------------------
 // Y1: rows kx in [0,K] of Tb: F_y, 2/3 mask, F^-1_y -> Tc[y][kx] (pitch pk).
 // ------------------------------------------------------------------------
-template <typename T, int L, class G>
+// BULK (FP64): the rows arrive by bulk copies (bulk_rows).
+template <typename T, int L, class G, bool BULK = false>
 __device__ __forceinline__ void y1_body(const cplx<T>* __restrict__ Tb, cplx<T>* __restrict__ Tc,
                                                    const cplx<T>* __restrict__ tw, StepConsts c, const int tile, cplx<T>* __restrict__ s) {
   typedef cplx<T> C;
+  static_assert(!BULK || (VK_HAVE_BULK && sizeof(T) == 8), "bulk row loads: FP64 device code");
   const int l0 = tile * G::R;
   const int K = c.K;
-  stage_rows<T, L, G::R, G::NT, G::LP>(s, [&](int r, int y) {
-    C v = mkc<T>(T(0), T(0));
-    if (l0 + r <= K) v = Tb[(size_t)(l0 + r) * L + y];
-    return v;
-  });
+  if constexpr (BULK) {
+#if VK_HAVE_BULK
+    const int nr = min(G::R, K + 1 - l0);
+    if (!bulk_rows<L, G::R, G::NT, G::LP>(s, [&](int r) { return Tb + (size_t)(l0 + r) * L; }, nr, c.async_err,
+                                         c.async_limit))
+      return;
+#endif
+  } else {
+    stage_rows<T, L, G::R, G::NT, G::LP>(s, [&](int r, int y) {
+      C v = mkc<T>(T(0), T(0));
+      if (l0 + r <= K) v = Tb[(size_t)(l0 + r) * L + y];
+      return v;
+    });
+  }
   __syncthreads();
   fft_rows<T, L, G::R, G::NT, -1>(s, tw);
   for (int e = threadIdx.x; e < G::R * L; e += G::NT) {
@@ -451,11 +527,12 @@ __device__ __forceinline__ void y1_body(const cplx<T>* __restrict__ Tb, cplx<T>*
   }
 }
 
-template <typename T, int L>
+template <typename T, int L, bool BULK = false>
 __global__ void __launch_bounds__(GeoY<T, L>::NT, GeoY<T, L>::MINB) k_y1(const cplx<T>* __restrict__ Tb, cplx<T>* __restrict__ Tc,
                                                    const cplx<T>* __restrict__ tw, StepConsts c) {
   extern __shared__ __align__(16) unsigned char smraw[];
-  y1_body<T, L, GeoY<T, L>>(Tb, Tc, tw, c, blockIdx.x, reinterpret_cast<cplx<T>*>(smraw));
+  pdl_enter();
+  y1_body<T, L, GeoY<T, L>, BULK>(Tb, Tc, tw, c, blockIdx.x, reinterpret_cast<cplx<T>*>(smraw));
 }
 
 // ------------------------------------------------------------------------
@@ -596,6 +673,7 @@ __global__ void __launch_bounds__(GeoX<T, L>::NT, GeoX<T, L>::MINB) k_x2(const c
                                                    const T* __restrict__ vpot, cplx<T>* __restrict__ Td,
                                                    const cplx<T>* __restrict__ tw, StepConsts c) {
   extern __shared__ __align__(16) unsigned char smraw[];
+  pdl_enter();
   const int npair = (int)gridDim.x - c.xsingle;
   if (L < 128 || (int)blockIdx.x < npair)
     x2_body<T, L, GeoX<T, L>, SIGN, PRUNE_OUT, POT>(Tc, psi, vpot, Td, tw, c, blockIdx.x, reinterpret_cast<cplx<T>*>(smraw));
@@ -674,20 +752,30 @@ __device__ __forceinline__ cplx<T> rk4_mode(const StepConsts& c, const Rk4Coef<T
 // FRC: the -DGPE_FRCDISP terms (a separate instantiation, so the plain
 // kernel carries none of their registers).
 // ------------------------------------------------------------------------
-template <typename T, int L, class G, int STAGE, bool FRC = false>
+template <typename T, int L, class G, int STAGE, bool FRC = false, bool BULK = false>
 __device__ __forceinline__ void y2_rk4_body(const cplx<T>* __restrict__ Td, cplx<T>* __restrict__ kpsi,
                                                        cplx<T>* __restrict__ str1, cplx<T>* __restrict__ str2,
                                                        cplx<T>* __restrict__ Ta, const cplx<T>* __restrict__ tw,
                                                        StepConsts c, const int tile, cplx<T>* __restrict__ s) {
   typedef cplx<T> C;
+  static_assert(!BULK || (VK_HAVE_BULK && sizeof(T) == 8), "bulk row loads: FP64 device code");
   const int l0 = tile * G::R;
   const int K = c.K, nx = c.nx;
   const int nrow = 2 * K + 1;
-  stage_rows<T, L, G::R, G::NT, G::LP>(s, [&](int r, int y) {
-    C v = mkc<T>(T(0), T(0));
-    if (l0 + r < nrow) v = Td[(size_t)pruned_row(l0 + r, K, nx) * L + y];
-    return v;
-  });
+  if constexpr (BULK) {
+#if VK_HAVE_BULK
+    const int nr = min(G::R, nrow - l0);
+    if (!bulk_rows<L, G::R, G::NT, G::LP>(
+            s, [&](int r) { return Td + (size_t)pruned_row(l0 + r, K, nx) * L; }, nr, c.async_err, c.async_limit))
+      return;
+#endif
+  } else {
+    stage_rows<T, L, G::R, G::NT, G::LP>(s, [&](int r, int y) {
+      C v = mkc<T>(T(0), T(0));
+      if (l0 + r < nrow) v = Td[(size_t)pruned_row(l0 + r, K, nx) * L + y];
+      return v;
+    });
+  }
   __syncthreads();
   fft_rows<T, L, G::R, G::NT, -1>(s, tw);
   const Rk4Coef<T> q = rk4_coef<T, STAGE>(c);
@@ -733,13 +821,15 @@ __device__ __forceinline__ void y2_rk4_body(const cplx<T>* __restrict__ Td, cplx
   }
 }
 
-template <typename T, int L, int STAGE, bool FRC = false>
+template <typename T, int L, int STAGE, bool FRC = false, bool BULK = false>
 __global__ void __launch_bounds__(GeoY<T, L>::NT, GeoY<T, L>::MINB) k_y2_rk4(const cplx<T>* __restrict__ Td, cplx<T>* __restrict__ kpsi,
                                                        cplx<T>* __restrict__ str1, cplx<T>* __restrict__ str2,
                                                        cplx<T>* __restrict__ Ta, const cplx<T>* __restrict__ tw,
                                                        StepConsts c) {
   extern __shared__ __align__(16) unsigned char smraw[];
-  y2_rk4_body<T, L, GeoY<T, L>, STAGE, FRC>(Td, kpsi, str1, str2, Ta, tw, c, blockIdx.x, reinterpret_cast<cplx<T>*>(smraw));
+  pdl_enter();
+  y2_rk4_body<T, L, GeoY<T, L>, STAGE, FRC, BULK>(Td, kpsi, str1, str2, Ta, tw, c, blockIdx.x,
+                                                  reinterpret_cast<cplx<T>*>(smraw));
 }
 
 // ------------------------------------------------------------------------

@@ -173,6 +173,26 @@ class Solver : public SolverBase {
     if (std::is_same<T, double>::value && nx_ == 1024 && !(xs_env && xs_env[0] == '0')) c_.xsingle = ny_;
     // VK_XSPLIT=1: single rows in every x pass with nx >= 128 (timing comparisons)
     if (xs_env && xs_env[0] == '1' && nx_ >= 128) c_.xsingle = ny_;
+    // Pass kernels by programmatic dependent launch (VK_PDL=0: plain launches).
+    {
+      const char* e = std::getenv("VK_PDL");
+      pdl_ = !(e && e[0] == '0');
+    }
+    // FP64: the y passes (y1, RK4 y2) and the single-row CTAs of k_x1 load
+    // their rows by bulk copies (cp.async.bulk on an mbarrier, bounded
+    // waits); VK_BULK=0 loads element-wise.
+    bulk_ = false;
+    if (std::is_same<T, double>::value) {
+      const char* b = std::getenv("VK_BULK");
+      bulk_ = !(b && b[0] == '0');
+    }
+    if (bulk_) {
+      const char* lim = std::getenv("VK_SPIN_LIMIT");
+      VK_CUDA_TRY(cudaMalloc(&async_err_, sizeof(int)));
+      VK_CUDA_TRY(cudaMemset(async_err_, 0, sizeof(int)));
+      c_.async_err = async_err_;
+      c_.async_limit = lim ? std::strtoull(lim, nullptr, 10) : (1ull << 24);
+    }
     {
       int frc = init_fused();
       if (frc) return frc;
@@ -668,6 +688,31 @@ class Solver : public SolverBase {
     }
     if (timing_) record_event(tag);
   }
+  // The pass kernels k_x1, k_y1, k_x2 and k_y2_rk4 (each starts with
+  // pdl_enter) with programmatic stream serialization, so that a pass's CTAs
+  // are scheduled while the previous pass drains; pdl_ off (VK_PDL=0) or
+  // timing on: a plain launch.
+  template <typename... KA, typename... A>
+  void launch_pass(const char* tag, void (*kern)(KA...), int grid, int block, size_t smem, A... args) {
+    if (!pdl_ || timing_) return launch_raw(tag, kern, grid, block, smem, args...);
+    ensure_smem_attr((const void*)kern, smem);
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(grid);
+    cfg.blockDim = dim3(block);
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = st_;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    at[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    const cudaError_t le = cudaLaunchKernelEx(&cfg, kern, args...);
+    ++launches_;
+    if (le != cudaSuccess && launch_err_ == cudaSuccess) {
+      launch_err_ = le;
+      launch_err_tag_ = tag;
+    }
+  }
   // Cooperative launch (all CTAs co-resident; capturable in a graph).
   template <typename... KA, typename... A>
   void launch_coop(const char* tag, void (*kern)(KA...), int grid, int block, size_t smem, A... args) {
@@ -925,16 +970,30 @@ class Solver : public SolverBase {
       typedef GeoX<T, L> G;
       const size_t sm = sizeof(C) * G::R * G::LP;
       const int grid = x_grid(G::R);
-      if (!from_t) launch_raw("k_x1", k_x1<T, L, false, false>, grid, G::NT, sm, (const C*)Ta_, psi_, Tb_, (const C*)twx_, c_);
-      else if (prune) launch_raw("k_x1", k_x1<T, L, true, true>, grid, G::NT, sm, (const C*)Ta_, psi_, Tb_, (const C*)twx_, c_);
-      else launch_raw("k_x1", k_x1<T, L, true, false>, grid, G::NT, sm, (const C*)Ta_, psi_, Tb_, (const C*)twx_, c_);
+      auto go = [&](auto bulk_c) {
+        constexpr bool B = decltype(bulk_c)::value;
+        if (!from_t) launch_pass("k_x1", k_x1<T, L, false, false, B>, grid, G::NT, sm, (const C*)Ta_, psi_, Tb_, (const C*)twx_, c_);
+        else if (prune) launch_pass("k_x1", k_x1<T, L, true, true, B>, grid, G::NT, sm, (const C*)Ta_, psi_, Tb_, (const C*)twx_, c_);
+        else launch_pass("k_x1", k_x1<T, L, true, false, B>, grid, G::NT, sm, (const C*)Ta_, psi_, Tb_, (const C*)twx_, c_);
+      };
+      if constexpr (std::is_same<T, double>::value && L >= 128) {
+        if (bulk_ && c_.xsingle > 0) return go(std::true_type());
+      }
+      go(std::false_type());
     });
   }
   void y1() {
     with_len(ny_, [&](auto lc) {
       constexpr int L = decltype(lc)::value;
       typedef GeoY<T, L> G;
-      launch_raw("k_y1", k_y1<T, L>, (K_ + 1 + G::R - 1) / G::R, G::NT, sizeof(C) * G::R * G::LP, (const C*)Tb_, Tc_,
+      if constexpr (std::is_same<T, double>::value) {
+        if (bulk_) {
+          launch_pass("k_y1", k_y1<T, L, true>, (K_ + 1 + G::R - 1) / G::R, G::NT, sizeof(C) * G::R * G::LP,
+                     (const C*)Tb_, Tc_, (const C*)twy_, c_);
+          return;
+        }
+      }
+      launch_pass("k_y1", k_y1<T, L>, (K_ + 1 + G::R - 1) / G::R, G::NT, sizeof(C) * G::R * G::LP, (const C*)Tb_, Tc_,
                  (const C*)twy_, c_);
     });
   }
@@ -944,8 +1003,8 @@ class Solver : public SolverBase {
       typedef GeoX<T, L> G;
       const size_t sm = sizeof(C) * G::R * G::LP;
       const int grid = x_grid(G::R);
-      if (sign > 0) launch_raw("k_x2", k_x2<T, L, +1, true, false>, grid, G::NT, sm, (const C*)Tc_, (const C*)psi_, (const T*)nullptr, Td_, (const C*)twx_, c_);
-      else launch_raw("k_x2", k_x2<T, L, -1, false, false>, grid, G::NT, sm, (const C*)Tc_, (const C*)psi_, (const T*)nullptr, Td_, (const C*)twx_, c_);
+      if (sign > 0) launch_pass("k_x2", k_x2<T, L, +1, true, false>, grid, G::NT, sm, (const C*)Tc_, (const C*)psi_, (const T*)nullptr, Td_, (const C*)twx_, c_);
+      else launch_pass("k_x2", k_x2<T, L, -1, false, false>, grid, G::NT, sm, (const C*)Tc_, (const C*)psi_, (const T*)nullptr, Td_, (const C*)twx_, c_);
       (void)prune_out;
     });
   }
@@ -955,17 +1014,23 @@ class Solver : public SolverBase {
       typedef GeoY<T, L> G;
       const int grid = (2 * K_ + 1 + G::R - 1) / G::R;
       const size_t sm = sizeof(C) * G::R * G::LP;
-      auto go = [&](auto frc_c) {
-        constexpr bool F = decltype(frc_c)::value;
+      auto go = [&](auto frc_c, auto bulk_c) {
+        constexpr bool F = decltype(frc_c)::value, B = decltype(bulk_c)::value;
         switch (stage) {
-          case 1: launch_raw("k_y2_rk4", k_y2_rk4<T, L, 1, F>, grid, G::NT, sm, (const C*)Td_, kpsi_, str1_, str2_, Ta_, (const C*)twy_, c_); break;
-          case 2: launch_raw("k_y2_rk4", k_y2_rk4<T, L, 2, F>, grid, G::NT, sm, (const C*)Td_, kpsi_, str1_, str2_, Ta_, (const C*)twy_, c_); break;
-          case 3: launch_raw("k_y2_rk4", k_y2_rk4<T, L, 3, F>, grid, G::NT, sm, (const C*)Td_, kpsi_, str1_, str2_, Ta_, (const C*)twy_, c_); break;
-          default: launch_raw("k_y2_rk4", k_y2_rk4<T, L, 4, F>, grid, G::NT, sm, (const C*)Td_, kpsi_, str1_, str2_, Ta_, (const C*)twy_, c_); break;
+          case 1: launch_pass("k_y2_rk4", k_y2_rk4<T, L, 1, F, B>, grid, G::NT, sm, (const C*)Td_, kpsi_, str1_, str2_, Ta_, (const C*)twy_, c_); break;
+          case 2: launch_pass("k_y2_rk4", k_y2_rk4<T, L, 2, F, B>, grid, G::NT, sm, (const C*)Td_, kpsi_, str1_, str2_, Ta_, (const C*)twy_, c_); break;
+          case 3: launch_pass("k_y2_rk4", k_y2_rk4<T, L, 3, F, B>, grid, G::NT, sm, (const C*)Td_, kpsi_, str1_, str2_, Ta_, (const C*)twy_, c_); break;
+          default: launch_pass("k_y2_rk4", k_y2_rk4<T, L, 4, F, B>, grid, G::NT, sm, (const C*)Td_, kpsi_, str1_, str2_, Ta_, (const C*)twy_, c_); break;
         }
       };
-      if (c_.frc) go(std::true_type());
-      else go(std::false_type());
+      auto go_b = [&](auto frc_c) {
+        if constexpr (std::is_same<T, double>::value) {
+          if (bulk_) return go(frc_c, std::true_type());
+        }
+        go(frc_c, std::false_type());
+      };
+      if (c_.frc) go_b(std::true_type());
+      else go_b(std::false_type());
     });
   }
   void y2_argle(bool resid) {
@@ -1007,7 +1072,23 @@ class Solver : public SolverBase {
     int rc = check_launch();
     if (rc) return rc;
     VK_CUDA_TRY(cudaStreamSynchronize(st_));
-    return barrier_check();
+    rc = barrier_check();
+    return rc ? rc : async_check();
+  }
+  // A CTA whose wait for its bulk row loads ran out set the error word:
+  // report it once, reset it and invalidate the field.
+  int async_check() {
+    if (!async_err_) return VK_OK;
+    int h = 0;
+    VK_CUDA_TRY(cudaMemcpyAsync(&h, async_err_, sizeof(int), cudaMemcpyDeviceToHost, st_));
+    VK_CUDA_TRY(cudaStreamSynchronize(st_));
+    if (h == 0) return VK_OK;
+    VK_CUDA_TRY(cudaMemsetAsync(async_err_, 0, sizeof(int), st_));
+    VK_CUDA_TRY(cudaStreamSynchronize(st_));
+    set_error("vk_gpe_rk4: a CTA of a row pass gave up waiting for its bulk row loads (the field is not valid; "
+              "set it again)");
+    have_psi_ = false;
+    return VK_E_CUDA;
   }
 
   int upload(const double* host, C* dev) {
@@ -1063,6 +1144,8 @@ class Solver : public SolverBase {
     if (part_) cudaFree(part_);
     if (sums_) cudaFree(sums_);
     if (bar_) cudaFree(bar_);
+    if (async_err_) cudaFree(async_err_);
+    async_err_ = nullptr;
     if (rngc_) cudaFree(rngc_);
     rngc_ = nullptr;
     if (Tg_) cudaFree(Tg_);
@@ -1133,6 +1216,9 @@ class Solver : public SolverBase {
   std::vector<const char*> ev_tag_;
   Diagnostics<T> diag_;
   GridBarrier* bar_ = nullptr;            // persistent stage kernel: barrier state
+  bool bulk_ = false;                     // FP64 bulk row loads
+  bool pdl_ = true;                       // pass kernels by programmatic dependent launch
+  int* async_err_ = nullptr;              // their error word
   int fused_grid_ = 0;                    //   its CTAs (0: the four pass kernels)
   size_t fused_smem_ = 0;
   unsigned long long spin_limit_ = 1ull << 24;
