@@ -83,20 +83,6 @@ VK_GEO(GeoY, float, 1024, 1, 8) VK_GEO(GeoY, float, 2048, 1, 4) VK_GEO(GeoY, flo
 
 __device__ __forceinline__ int kwn(int i, int n) { return i < n / 2 ? i : i - n; }
 
-// Programmatic dependent launch.  The RK4 pass kernels (k_x1, k_y1, k_x2,
-// k_y2_rk4, k_xinv) may be launched with programmatic stream serialization:
-// their CTAs can then be scheduled while the previous kernel's last CTAs
-// run.  Each waits for the previous kernel to complete (its writes visible)
-// before it touches any field, so the ordering of the passes is that of a
-// plain stream; with an ordinary launch the wait returns at once.  Once all
-// of its own CTAs are running, a pass lets the next one be scheduled.
-__device__ __forceinline__ void pdl_enter() {
-#if defined(__CUDA_ARCH__)
-  asm volatile("griddepcontrol.wait;" ::: "memory");
-  asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
-#endif
-}
-
 // Row index of logical row l when only |kx| <= K rows are processed.
 __device__ __forceinline__ int pruned_row(int l, int K, int n) { return l <= K ? l : n - (2 * K + 1 - l); }
 
@@ -314,7 +300,6 @@ template <typename T, int L, bool PRUNE>
 __global__ void __launch_bounds__(GeoX<T, L>::NT, GeoX<T, L>::MINB) k_xinv(const cplx<T>* __restrict__ src, cplx<T>* __restrict__ dst,
                                                      const cplx<T>* __restrict__ tw, T scale, int K) {
   extern __shared__ __align__(16) unsigned char smraw[];
-  pdl_enter();
   xinv_body<T, L, GeoX<T, L>, PRUNE>(src, dst, tw, scale, K, blockIdx.x, reinterpret_cast<cplx<T>*>(smraw));
 }
 
@@ -478,7 +463,6 @@ __global__ void __launch_bounds__(GeoX<T, L>::NT, GeoX<T, L>::MINB) k_x1(const c
                                                    cplx<T>* __restrict__ Tb, const cplx<T>* __restrict__ tw,
                                                    StepConsts c) {
   extern __shared__ __align__(16) unsigned char smraw[];
-  pdl_enter();
   const int npair = (int)gridDim.x - c.xsingle;
   if (L < 128 || (int)blockIdx.x < npair)
     x1_body<T, L, GeoX<T, L>, FROM_T, PRUNE>(Ta, psi, Tb, tw, c, blockIdx.x, reinterpret_cast<cplx<T>*>(smraw));
@@ -531,7 +515,6 @@ template <typename T, int L, bool BULK = false>
 __global__ void __launch_bounds__(GeoY<T, L>::NT, GeoY<T, L>::MINB) k_y1(const cplx<T>* __restrict__ Tb, cplx<T>* __restrict__ Tc,
                                                    const cplx<T>* __restrict__ tw, StepConsts c) {
   extern __shared__ __align__(16) unsigned char smraw[];
-  pdl_enter();
   y1_body<T, L, GeoY<T, L>, BULK>(Tb, Tc, tw, c, blockIdx.x, reinterpret_cast<cplx<T>*>(smraw));
 }
 
@@ -673,7 +656,6 @@ __global__ void __launch_bounds__(GeoX<T, L>::NT, GeoX<T, L>::MINB) k_x2(const c
                                                    const T* __restrict__ vpot, cplx<T>* __restrict__ Td,
                                                    const cplx<T>* __restrict__ tw, StepConsts c) {
   extern __shared__ __align__(16) unsigned char smraw[];
-  pdl_enter();
   const int npair = (int)gridDim.x - c.xsingle;
   if (L < 128 || (int)blockIdx.x < npair)
     x2_body<T, L, GeoX<T, L>, SIGN, PRUNE_OUT, POT>(Tc, psi, vpot, Td, tw, c, blockIdx.x, reinterpret_cast<cplx<T>*>(smraw));
@@ -827,7 +809,6 @@ __global__ void __launch_bounds__(GeoY<T, L>::NT, GeoY<T, L>::MINB) k_y2_rk4(con
                                                        cplx<T>* __restrict__ Ta, const cplx<T>* __restrict__ tw,
                                                        StepConsts c) {
   extern __shared__ __align__(16) unsigned char smraw[];
-  pdl_enter();
   y2_rk4_body<T, L, GeoY<T, L>, STAGE, FRC, BULK>(Td, kpsi, str1, str2, Ta, tw, c, blockIdx.x,
                                                   reinterpret_cast<cplx<T>*>(smraw));
 }

@@ -173,11 +173,6 @@ class Solver : public SolverBase {
     if (std::is_same<T, double>::value && nx_ == 1024 && !(xs_env && xs_env[0] == '0')) c_.xsingle = ny_;
     // VK_XSPLIT=1: single rows in every x pass with nx >= 128 (timing comparisons)
     if (xs_env && xs_env[0] == '1' && nx_ >= 128) c_.xsingle = ny_;
-    // Pass kernels by programmatic dependent launch (VK_PDL=0: plain launches).
-    {
-      const char* e = std::getenv("VK_PDL");
-      pdl_ = !(e && e[0] == '0');
-    }
     // FP64: the y passes (y1, RK4 y2) and the single-row CTAs of k_x1 load
     // their rows by bulk copies (cp.async.bulk on an mbarrier, bounded
     // waits); VK_BULK=0 loads element-wise.
@@ -688,31 +683,6 @@ class Solver : public SolverBase {
     }
     if (timing_) record_event(tag);
   }
-  // The pass kernels k_x1, k_y1, k_x2 and k_y2_rk4 (each starts with
-  // pdl_enter) with programmatic stream serialization, so that a pass's CTAs
-  // are scheduled while the previous pass drains; pdl_ off (VK_PDL=0) or
-  // timing on: a plain launch.
-  template <typename... KA, typename... A>
-  void launch_pass(const char* tag, void (*kern)(KA...), int grid, int block, size_t smem, A... args) {
-    if (!pdl_ || timing_) return launch_raw(tag, kern, grid, block, smem, args...);
-    ensure_smem_attr((const void*)kern, smem);
-    cudaLaunchConfig_t cfg = {};
-    cfg.gridDim = dim3(grid);
-    cfg.blockDim = dim3(block);
-    cfg.dynamicSmemBytes = smem;
-    cfg.stream = st_;
-    cudaLaunchAttribute at[1];
-    at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
-    at[0].val.programmaticStreamSerializationAllowed = 1;
-    cfg.attrs = at;
-    cfg.numAttrs = 1;
-    const cudaError_t le = cudaLaunchKernelEx(&cfg, kern, args...);
-    ++launches_;
-    if (le != cudaSuccess && launch_err_ == cudaSuccess) {
-      launch_err_ = le;
-      launch_err_tag_ = tag;
-    }
-  }
   // Cooperative launch (all CTAs co-resident; capturable in a graph).
   template <typename... KA, typename... A>
   void launch_coop(const char* tag, void (*kern)(KA...), int grid, int block, size_t smem, A... args) {
@@ -972,9 +942,9 @@ class Solver : public SolverBase {
       const int grid = x_grid(G::R);
       auto go = [&](auto bulk_c) {
         constexpr bool B = decltype(bulk_c)::value;
-        if (!from_t) launch_pass("k_x1", k_x1<T, L, false, false, B>, grid, G::NT, sm, (const C*)Ta_, psi_, Tb_, (const C*)twx_, c_);
-        else if (prune) launch_pass("k_x1", k_x1<T, L, true, true, B>, grid, G::NT, sm, (const C*)Ta_, psi_, Tb_, (const C*)twx_, c_);
-        else launch_pass("k_x1", k_x1<T, L, true, false, B>, grid, G::NT, sm, (const C*)Ta_, psi_, Tb_, (const C*)twx_, c_);
+        if (!from_t) launch_raw("k_x1", k_x1<T, L, false, false, B>, grid, G::NT, sm, (const C*)Ta_, psi_, Tb_, (const C*)twx_, c_);
+        else if (prune) launch_raw("k_x1", k_x1<T, L, true, true, B>, grid, G::NT, sm, (const C*)Ta_, psi_, Tb_, (const C*)twx_, c_);
+        else launch_raw("k_x1", k_x1<T, L, true, false, B>, grid, G::NT, sm, (const C*)Ta_, psi_, Tb_, (const C*)twx_, c_);
       };
       if constexpr (std::is_same<T, double>::value && L >= 128) {
         if (bulk_ && c_.xsingle > 0) return go(std::true_type());
@@ -988,12 +958,12 @@ class Solver : public SolverBase {
       typedef GeoY<T, L> G;
       if constexpr (std::is_same<T, double>::value) {
         if (bulk_) {
-          launch_pass("k_y1", k_y1<T, L, true>, (K_ + 1 + G::R - 1) / G::R, G::NT, sizeof(C) * G::R * G::LP,
+          launch_raw("k_y1", k_y1<T, L, true>, (K_ + 1 + G::R - 1) / G::R, G::NT, sizeof(C) * G::R * G::LP,
                      (const C*)Tb_, Tc_, (const C*)twy_, c_);
           return;
         }
       }
-      launch_pass("k_y1", k_y1<T, L>, (K_ + 1 + G::R - 1) / G::R, G::NT, sizeof(C) * G::R * G::LP, (const C*)Tb_, Tc_,
+      launch_raw("k_y1", k_y1<T, L>, (K_ + 1 + G::R - 1) / G::R, G::NT, sizeof(C) * G::R * G::LP, (const C*)Tb_, Tc_,
                  (const C*)twy_, c_);
     });
   }
@@ -1003,8 +973,8 @@ class Solver : public SolverBase {
       typedef GeoX<T, L> G;
       const size_t sm = sizeof(C) * G::R * G::LP;
       const int grid = x_grid(G::R);
-      if (sign > 0) launch_pass("k_x2", k_x2<T, L, +1, true, false>, grid, G::NT, sm, (const C*)Tc_, (const C*)psi_, (const T*)nullptr, Td_, (const C*)twx_, c_);
-      else launch_pass("k_x2", k_x2<T, L, -1, false, false>, grid, G::NT, sm, (const C*)Tc_, (const C*)psi_, (const T*)nullptr, Td_, (const C*)twx_, c_);
+      if (sign > 0) launch_raw("k_x2", k_x2<T, L, +1, true, false>, grid, G::NT, sm, (const C*)Tc_, (const C*)psi_, (const T*)nullptr, Td_, (const C*)twx_, c_);
+      else launch_raw("k_x2", k_x2<T, L, -1, false, false>, grid, G::NT, sm, (const C*)Tc_, (const C*)psi_, (const T*)nullptr, Td_, (const C*)twx_, c_);
       (void)prune_out;
     });
   }
@@ -1017,10 +987,10 @@ class Solver : public SolverBase {
       auto go = [&](auto frc_c, auto bulk_c) {
         constexpr bool F = decltype(frc_c)::value, B = decltype(bulk_c)::value;
         switch (stage) {
-          case 1: launch_pass("k_y2_rk4", k_y2_rk4<T, L, 1, F, B>, grid, G::NT, sm, (const C*)Td_, kpsi_, str1_, str2_, Ta_, (const C*)twy_, c_); break;
-          case 2: launch_pass("k_y2_rk4", k_y2_rk4<T, L, 2, F, B>, grid, G::NT, sm, (const C*)Td_, kpsi_, str1_, str2_, Ta_, (const C*)twy_, c_); break;
-          case 3: launch_pass("k_y2_rk4", k_y2_rk4<T, L, 3, F, B>, grid, G::NT, sm, (const C*)Td_, kpsi_, str1_, str2_, Ta_, (const C*)twy_, c_); break;
-          default: launch_pass("k_y2_rk4", k_y2_rk4<T, L, 4, F, B>, grid, G::NT, sm, (const C*)Td_, kpsi_, str1_, str2_, Ta_, (const C*)twy_, c_); break;
+          case 1: launch_raw("k_y2_rk4", k_y2_rk4<T, L, 1, F, B>, grid, G::NT, sm, (const C*)Td_, kpsi_, str1_, str2_, Ta_, (const C*)twy_, c_); break;
+          case 2: launch_raw("k_y2_rk4", k_y2_rk4<T, L, 2, F, B>, grid, G::NT, sm, (const C*)Td_, kpsi_, str1_, str2_, Ta_, (const C*)twy_, c_); break;
+          case 3: launch_raw("k_y2_rk4", k_y2_rk4<T, L, 3, F, B>, grid, G::NT, sm, (const C*)Td_, kpsi_, str1_, str2_, Ta_, (const C*)twy_, c_); break;
+          default: launch_raw("k_y2_rk4", k_y2_rk4<T, L, 4, F, B>, grid, G::NT, sm, (const C*)Td_, kpsi_, str1_, str2_, Ta_, (const C*)twy_, c_); break;
         }
       };
       auto go_b = [&](auto frc_c) {
@@ -1216,12 +1186,11 @@ class Solver : public SolverBase {
   std::vector<const char*> ev_tag_;
   Diagnostics<T> diag_;
   GridBarrier* bar_ = nullptr;            // persistent stage kernel: barrier state
-  bool bulk_ = false;                     // FP64 bulk row loads
-  bool pdl_ = true;                       // pass kernels by programmatic dependent launch
-  int* async_err_ = nullptr;              // their error word
   int fused_grid_ = 0;                    //   its CTAs (0: the four pass kernels)
   size_t fused_smem_ = 0;
   unsigned long long spin_limit_ = 1ull << 24;
+  bool bulk_ = false;                     // FP64 bulk row loads
+  int* async_err_ = nullptr;              // their error word
 };
 
 }  // namespace VK_SOLVER_NS
