@@ -35,8 +35,8 @@ PEAKS_FILE = os.path.join(ROOT, "MEASURED_PEAKS.json")
 FALLBACK_HBM_GBS = 6800.0
 # DRAM bytes per launch (dram__bytes_read.sum + dram__bytes_write.sum) of the
 # FP64 1024^2 passes, recorded from one earlier ncu capture of this workload
-# (not measured by this script: ncu is not run here)
-RECORDED_DRAM_BYTES_1024_FP64 = {"k_x1": 11421184 + 0, "k_x2": 22499328 + 3072}
+# with the bulk row loads (not measured by this script: ncu is not run here)
+RECORDED_DRAM_BYTES_1024_FP64 = {"k_x1": 11421952 + 0, "k_x2": 22499328 + 3072, "k_y2_rk4": 44822784 + 64768, "k_y1": 5660416 + 256}
 
 
 def parse():

@@ -162,7 +162,7 @@ def test_feature_kernel_matches_numpy():
 def test_tma_conv_matches_cp_async_conv(h, base, levels, narrow):
     """Layers whose input has 64k channels run on the TMA-fed kernel
     (VK_CONV_TMA=1: periodic padding, TMA tiles in the 128-byte swizzle
-    layout, 4-stage mbarrier ring), and with VK_CONV_TMA_NARROW=1 the 16- and
+    layout, 3- or 4-stage mbarrier ring), and with VK_CONV_TMA_NARROW=1 the 16- and
     32-channel layers too (32- and 64-byte swizzle); the K order is that of
     the cp.async kernels, so forward outputs and gradients agree to FP32
     rounding (a batch of 2)."""
