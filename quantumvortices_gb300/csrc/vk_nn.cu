@@ -324,102 +324,72 @@ __global__ void __launch_bounds__(128) k_conv_tma(const __grid_constant__ CUtens
   if (warp == 0) tc::tmem_dealloc(taddr, NCOL);
 }
 
-// Channel-major copies for the TMA-fed weight gradient, by 8 x 8 register
-// transposes (no shared memory).  A thread owns 8 consecutive pixels of one
-// image row (10 when shifted) and 8 channels: it loads 16 bytes per pixel,
-// transposes the block with byte permutes, and stores 16 bytes (8 pixels)
-// per channel.  Threads run over (pixel block, channel group) pairs with the
-// group fastest, so a warp's loads cover whole pixels and its stores whole
-// 16-byte pixel runs of each channel plane; blockIdx.y takes `rows` image
-// rows.  W and C must be multiples of 8.
+// Channel-major copies for the TMA-fed weight gradient.  A block moves
+// 64-pixel x 64-channel tiles of 8 consecutive image rows through shared
+// memory with 16-byte loads (8 channels of a pixel) and 16-byte stores (8
+// pixels of a channel).  W must be a multiple of 64 and C of 8.
 // SHIFT = false: NHWC [nimg][H][W][C] -> [nimg][C][H][W]; with db, also
-//   db[c] += sum over the pixels of the copied values (c < nbias; the bias
-//   gradient).  RELU: in is the gradient after the activation and y the
-//   layer's output; the copied values are d_pre = d_post (y > 0), written in
-//   NHWC to pre as well (the data-gradient input).
+// db[c] += sum over the pixels of in[.][c] for c < nbias (the bias gradient).
 // SHIFT = true: the three x-shifted, y-padded copies
-//   out[dx][nimg][C][H+2][W] = in[.][(y - 1) mod H][(x + dx - 1) mod W][.],
-//   dx = 0, 1, 2, so that every tap of a 64-pixel row chunk starts on a
-//   64-pixel boundary (TMA wants the innermost coordinate on a 16-byte
-//   boundary).
-__device__ __forceinline__ uint32_t u4w(const uint4& q, int p) {
-  return p == 0 ? q.x : (p == 1 ? q.y : (p == 2 ? q.z : q.w));
-}
-__device__ __forceinline__ uint32_t relu_mask2(uint32_t d, uint32_t y) {
-  // two BF16 lanes: keep d where y > 0 (positive, nonzero: sign bit clear and not +0)
-  const uint32_t lo = ((y & 0x8000u) == 0 && (y & 0x7fffu) != 0) ? 0x0000ffffu : 0u;
-  const uint32_t hi = ((y & 0x80000000u) == 0 && (y & 0x7fff0000u) != 0) ? 0xffff0000u : 0u;
-  return d & (lo | hi);
-}
-template <bool SHIFT, bool RELU>
-__global__ void __launch_bounds__(256) k_chw(const bf16* __restrict__ in, const bf16* __restrict__ y,
-                                             bf16* __restrict__ pre, bf16* __restrict__ out, int H, int W, int C,
-                                             int nimg, int rows, float* __restrict__ db, int nbias) {
-  constexpr int NP = SHIFT ? 10 : 8;  // pixels 8 pb - 1 .. 8 pb + 8 when shifted
-  const int G = C >> 3;
-  const int q = blockIdx.x * blockDim.x + threadIdx.x;
-  const bool act = q < (W >> 3) * G;
-  const int g = act ? q % G : 0, pb = act ? q / G : 0;
+// out[dx][nimg][C][H+2][W] = in[.][(y - 1) mod H][(x + dx - 1) mod W][.],
+// dx = 0, 1, 2, so that every tap of a 64-pixel row chunk starts on a 64-pixel
+// boundary (TMA wants the innermost coordinate on a 16-byte boundary).
+template <bool SHIFT>
+__global__ void __launch_bounds__(256) k_chw(const bf16* __restrict__ in, bf16* __restrict__ out, int H, int W, int C,
+                                             int nimg, float* __restrict__ db, int nbias) {
+  constexpr int NX = SHIFT ? 66 : 64;   // pixels x0 - 1 .. x0 + 64 when shifted
+  constexpr int SP = 72;                // row pitch (bf16) of the channel-major tile
+  constexpr int ROWS = 8;               // image rows per block (one bias atomic per channel and block)
+  __shared__ __align__(16) bf16 t[64][SP];
   const int Hp = SHIFT ? H + 2 : H;
+  const int x0 = blockIdx.x * 64, c0 = blockIdx.y * 64;
+  const int nc = min(64, C - c0);  // channels of this tile (a multiple of 8)
   const size_t plane = (size_t)nimg * C * Hp * W;
-  float sum[8];
-#pragma unroll
-  for (int c = 0; c < 8; ++c) sum[c] = 0.f;
-  const int r1 = min((int)(blockIdx.y + 1) * rows, nimg * Hp);
-  for (int row = blockIdx.y * rows; act && row < r1; ++row) {
+  float sum[2] = {0.f, 0.f};
+  const int r1 = min((int)(blockIdx.z + 1) * ROWS, nimg * Hp);
+  for (int row = blockIdx.z * ROWS; row < r1; ++row) {
     const int b = row / Hp, yp = row - b * Hp;
     const int ys = SHIFT ? (yp == 0 ? H - 1 : (yp == H + 1 ? 0 : yp - 1)) : yp;
-    const size_t rbase = ((size_t)b * H + ys) * W;
-    uint4 v[NP];
+    __syncthreads();  // the previous row's tile has been read
+    for (int v = threadIdx.x; v < NX * 8; v += blockDim.x) {
+      const int i = v >> 3, g = v & 7;
+      if (8 * g >= nc) continue;
+      int xs = SHIFT ? x0 - 1 + i : x0 + i;
+      xs = xs < 0 ? xs + W : (xs >= W ? xs - W : xs);
+      const uint4 q = *reinterpret_cast<const uint4*>(in + (((size_t)b * H + ys) * W + xs) * C + c0 + 8 * g);
+      const bf16* e = reinterpret_cast<const bf16*>(&q);
 #pragma unroll
-    for (int j = 0; j < NP; ++j) {
-      int x = 8 * pb + j - (SHIFT ? 1 : 0);
-      if (SHIFT) x = x < 0 ? x + W : (x >= W ? x - W : x);
-      v[j] = *reinterpret_cast<const uint4*>(in + (rbase + x) * C + 8 * g);
+      for (int k = 0; k < 8; ++k) t[8 * g + k][i] = e[k];
     }
-    if (RELU) {
-      uint4 m[8];
+    __syncthreads();
 #pragma unroll
-      for (int j = 0; j < 8; ++j) m[j] = *reinterpret_cast<const uint4*>(y + (rbase + 8 * pb + j) * C + 8 * g);
+    for (int h = 0; h < 2; ++h) {
+      const int v = threadIdx.x + 256 * h;
+      const int c = v >> 3, pg = v & 7;
+      if (c >= nc) continue;
 #pragma unroll
-      for (int j = 0; j < 8; ++j) {
-        v[j] = make_uint4(relu_mask2(v[j].x, m[j].x), relu_mask2(v[j].y, m[j].y), relu_mask2(v[j].z, m[j].z),
-                          relu_mask2(v[j].w, m[j].w));
-        *reinterpret_cast<uint4*>(pre + (rbase + 8 * pb + j) * C + 8 * g) = v[j];
-      }
-    }
+      for (int dx = 0; dx < (SHIFT ? 3 : 1); ++dx) {
+        uint4 q;
+        bf16* e = reinterpret_cast<bf16*>(&q);
 #pragma unroll
-    for (int dx = 0; dx < (SHIFT ? 3 : 1); ++dx) {
+        for (int k = 0; k < 8; ++k) e[k] = t[c][8 * pg + k + dx];
+        if (!SHIFT)
 #pragma unroll
-      for (int p = 0; p < 4; ++p) {  // channels 2p (low halves) and 2p + 1 (high halves)
-        uint32_t lo[4], hi[4];
-#pragma unroll
-        for (int k = 0; k < 4; ++k) {  // output pixels 2k, 2k + 1 = source v[2k + dx], v[2k + 1 + dx]
-          const uint32_t a = u4w(v[2 * k + dx], p), c = u4w(v[2 * k + 1 + dx], p);
-          lo[k] = __byte_perm(a, c, 0x5410);
-          hi[k] = __byte_perm(a, c, 0x7632);
-        }
-        bf16* o = out + dx * plane + (((size_t)b * C + 8 * g + 2 * p) * Hp + yp) * W + 8 * pb;
-        *reinterpret_cast<uint4*>(o) = make_uint4(lo[0], lo[1], lo[2], lo[3]);
-        *reinterpret_cast<uint4*>(o + (size_t)Hp * W) = make_uint4(hi[0], hi[1], hi[2], hi[3]);
-        if (!SHIFT) {
-#pragma unroll
-          for (int k = 0; k < 4; ++k) {
-            sum[2 * p] += __uint_as_float(lo[k] << 16) + __uint_as_float(lo[k] & 0xffff0000u);
-            sum[2 * p + 1] += __uint_as_float(hi[k] << 16) + __uint_as_float(hi[k] & 0xffff0000u);
-          }
-        }
+          for (int k = 0; k < 8; ++k) sum[h] += __bfloat162float(e[k]);
+        *reinterpret_cast<uint4*>(out + dx * plane + (((size_t)b * C + c0 + c) * Hp + yp) * W + x0 + 8 * pg) = q;
       }
     }
   }
   if (!SHIFT && db) {
-    // lanes with the same channel group are G apart (G < 32) or alone
-    const int lane = threadIdx.x & 31;
 #pragma unroll
-    for (int c = 0; c < 8; ++c) {
-      float x = sum[c];
-      for (int sft = G; sft < 32; sft <<= 1) x += __shfl_xor_sync(0xffffffffu, x, sft);
-      if (act && lane < G && 8 * g + c < nbias) atomicAdd(&db[8 * g + c], x);
+    for (int h = 0; h < 2; ++h) {
+      // the 8 threads of channel c are consecutive lanes
+      float x = sum[h];
+      x += __shfl_xor_sync(0xffffffffu, x, 1);
+      x += __shfl_xor_sync(0xffffffffu, x, 2);
+      x += __shfl_xor_sync(0xffffffffu, x, 4);
+      const int v = threadIdx.x + 256 * h, c = v >> 3;
+      if ((v & 7) == 0 && c < nc && c0 + c < nbias) atomicAdd(&db[c0 + c], x);
     }
   }
 }
@@ -1406,11 +1376,7 @@ class Net {
   // 64k pixels, Cin dividing 128 or a multiple of it, at most 256 output
   // channels.  On GB300 the k_wgrad launches took 56% of a 512^2 training
   // step (batches of 8) at 30-60 TFLOP/s.
-  // relu_y (optional): dy is the gradient after the activation and relu_y
-  // the layer output; the weight gradient then uses d_pre = dy (relu_y > 0),
-  // which is also written to pre (NHWC) for the data gradient.
-  bool wgrad_tma(const Tensor& in, const bf16* dy, int coutp, float* out, float* db, int nbias,
-                 const bf16* relu_y = nullptr, bf16* pre = nullptr) {
+  bool wgrad_tma(const Tensor& in, const bf16* dy, int coutp, float* out, float* db, int nbias) {
     const int Hh = in.h, Ww = in.w, C = in.c;
     if (!tma_ok_ || Ww % 64 != 0 || C % 16 != 0 || (128 % C != 0 && C % 128 != 0) || coutp % 16 != 0 ||
         coutp > 256)
@@ -1435,9 +1401,10 @@ class Net {
             CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
             CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
       return false;
-    chw<true>(in.d, nullptr, nullptr, xsbuf, Hh, Ww, C, nullptr, 0);
-    if (relu_y) chw<false, true>(dy, relu_y, pre, dchw, Hh, Ww, coutp, db, nbias);
-    else chw<false>(dy, nullptr, nullptr, dchw, Hh, Ww, coutp, db, nbias);
+    k_chw<true><<<dim3(Ww / 64, (C + 63) / 64, (nb * (Hh + 2) + 7) / 8), 256, 0, st>>>(in.d, xsbuf, Hh, Ww, C, nb,
+                                                                                      nullptr, 0);
+    k_chw<false><<<dim3(Ww / 64, (coutp + 63) / 64, (nb * Hh + 7) / 8), 256, 0, st>>>(dy, dchw, Hh, Ww, coutp, nb, db,
+                                                                                     nbias);
     const int npix = nb * Hh * Ww, M = 9 * C;
     const int mt = (M + 127) / 128;
     int ppc = 8192;
@@ -1464,16 +1431,6 @@ class Net {
       attr = true;
     }
     k_wgrad_tma<BN, S><<<grid, 128, smem, st>>>(tx, td, in.h, in.w, nb, in.c, ppc, out, err);
-  }
-  // k_chw launch: (pixel block, channel group) pairs over x, image rows over
-  // y, about four CTAs per SM.
-  template <bool SHIFT, bool RELU = false>
-  void chw(const bf16* src, const bf16* y, bf16* pre, bf16* dst, int Hh, int Ww, int C, float* db, int nbias) {
-    const int gx = ((Ww / 8) * (C / 8) + 255) / 256;
-    const int nrows = nb * (SHIFT ? Hh + 2 : Hh);
-    const int rows = std::max(1, std::min(8, nrows * gx / (4 * 152)));
-    k_chw<SHIFT, RELU><<<dim3(gx, (nrows + rows - 1) / rows), 256, 0, st>>>(src, y, pre, dst, Hh, Ww, C, nb, rows, db,
-                                                                            nbias);
   }
   void wgrad(const Tensor& in, const bf16* dy, int coutp, float* out, float* db, int nbias) {
     if (wgrad_tma(in, dy, coutp, out, db, nbias)) return;
@@ -1538,14 +1495,11 @@ class Net {
   void conv_bwd(const Conv& cv, const Tensor& in, const bf16* out, const bf16* dpost, bf16* dpre_scratch, bf16* din) {
     const size_t nout = (size_t)nb * in.h * in.w * cv.coutp;
     const bf16* dpre = dpost;
-    bool done = false;
     if (cv.relu) {
-      // the TMA weight gradient takes the ReLU mask in its channel-major copy
-      done = wgrad_tma(in, dpost, cv.coutp, wscratch, grad + cv.boff, cv.cout, out, dpre_scratch);
-      if (!done) k_relu_bwd<<<blocks(nout / 8), 256, 0, st>>>(out, dpost, dpre_scratch, nout);
+      k_relu_bwd<<<blocks(nout / 8), 256, 0, st>>>(out, dpost, dpre_scratch, nout);
       dpre = dpre_scratch;
     }
-    if (!done) wgrad(in, dpre, cv.coutp, wscratch, grad + cv.boff, cv.cout);
+    wgrad(in, dpre, cv.coutp, wscratch, grad + cv.boff, cv.cout);
     k_wgrad_scatter<<<blocks((size_t)cv.cout * 9 * cv.cin), 256, 0, st>>>(wscratch, cv.cout, cv.cin, cv.coutp,
                                                                           cv.cinp, grad + cv.woff);
     if (din) {
