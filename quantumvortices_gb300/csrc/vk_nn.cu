@@ -338,7 +338,13 @@ template <bool SHIFT>
 __global__ void __launch_bounds__(256) k_chw(const bf16* __restrict__ in, bf16* __restrict__ out, int H, int W, int C,
                                              int nimg, float* __restrict__ db, int nbias) {
   constexpr int NX = SHIFT ? 66 : 64;   // pixels x0 - 1 .. x0 + 64 when shifted
-  constexpr int SP = 72;                // row pitch (bf16) of the channel-major tile
+  // Row pitch (bf16) of the channel-major tile: 66 = 33 words, so channel
+  // row r starts at bank r mod 32.  The scattered stores of the load phase
+  // (lanes: 4 pixels x 8 channel groups, rows 8 g + k) then fall on 4 bank
+  // groups (2-way), and the 8-pixel reads of the store phase (lanes: 4
+  // channels x 8 pixel groups) on 32 distinct banks; a pitch of 72 (36
+  // words) put all 8 channel groups on one bank.
+  constexpr int SP = 66;
   constexpr int ROWS = 8;               // image rows per block (one bias atomic per channel and block)
   __shared__ __align__(16) bf16 t[64][SP];
   const int Hp = SHIFT ? H + 2 : H;
