@@ -990,8 +990,11 @@ __global__ void k_planar2(const float* __restrict__ in, float* __restrict__ out,
     out[(size_t)b * 2 * npix + npix + q] = in[2 * p + 1];
   }
 }
+// hyper = {lr, 1 - b1^t, 1 - b2^t} in device memory, so that a captured
+// training step replays with the current step's values.
 __global__ void k_adam(float* __restrict__ p, const float* __restrict__ g, float* __restrict__ m, float* __restrict__ v,
-                       size_t n, float lr, float b1, float b2, float c1, float c2, float eps) {
+                       size_t n, const float* __restrict__ hyper, float b1, float b2, float eps) {
+  const float lr = hyper[0], c1 = hyper[1], c2 = hyper[2];
   for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
     const float gi = g[i];
     const float mi = b1 * m[i] + (1.f - b1) * gi, vi = b2 * v[i] + (1.f - b2) * gi * gi;
@@ -1081,6 +1084,18 @@ class Net {
   float* out_f = nullptr;     // head output [p][2]
   int64_t steps = 0;
   int nb = 1, bcap = 1;       // images in the current batch, batch capacity
+  // One CUDA graph per training step (forward, backward, Adam), captured at
+  // the second step of a batch size and replayed after it: the step's inputs
+  // are copied into fixed buffers first, and Adam reads lr and its bias
+  // corrections from device memory.  VK_NN_GRAPH=0: plain launches.
+  float *in_stage = nullptr, *tgt_stage = nullptr, *hyper = nullptr;
+  float hyper_h[3] = {0.f, 0.f, 0.f};
+  cudaGraphExec_t tgraph = nullptr;
+  int tgraph_nb = 0;
+  bool graph_ok_ = [] {
+    const char* e = std::getenv("VK_NN_GRAPH");
+    return !(e && e[0] == '0');
+  }();
   static constexpr int kMaxVortices = 4096;  // vk_nn_features
   double2* feat_psi = nullptr;
   double* feat_pos = nullptr;
@@ -1114,6 +1129,7 @@ class Net {
   Tensor dhead;
 
   ~Net() {
+    if (tgraph) cudaGraphExecDestroy(tgraph);
     for (auto* q : allocs) cudaFree(q);
     if (st) cudaStreamDestroy(st);
   }
@@ -1232,6 +1248,9 @@ class Net {
     xsbuf = dalloc<bf16>(3 * padbuf_n);
     dchw = dalloc<bf16>(padbuf_n);
     out_f = dalloc<float>((size_t)H * W * 2 * bcap);
+    in_stage = dalloc<float>((size_t)H * W * 3 * bcap);
+    tgt_stage = dalloc<float>((size_t)H * W * 2 * bcap);
+    hyper = dalloc<float>(3);
     feat_psi = dalloc<double2>((size_t)H * W);
     feat_pos = dalloc<double>(2 * kMaxVortices);
     feat_gx = dalloc<float>((size_t)kMaxVortices * W);
@@ -1563,12 +1582,63 @@ class Net {
     }
   }
 
-  void adam(float lr) {
+  static constexpr float kB1 = 0.9f, kB2 = 0.999f;
+  // Adam's step number, lr and bias corrections into device memory (before
+  // the step's kernels, outside any graph).
+  void adam_hyper(float lr) {
     ++steps;
-    const float b1 = 0.9f, b2 = 0.999f;
-    const float c1 = 1.f - std::pow(b1, (float)steps), c2 = 1.f - std::pow(b2, (float)steps);
-    k_adam<<<blocks(nparam), 256, 0, st>>>(param, grad, adam_m, adam_v, nparam, lr, b1, b2, c1, c2, 1e-8f);
+    hyper_h[0] = lr;
+    hyper_h[1] = 1.f - std::pow(kB1, (float)steps);
+    hyper_h[2] = 1.f - std::pow(kB2, (float)steps);
+    cudaMemcpyAsync(hyper, hyper_h, sizeof(hyper_h), cudaMemcpyHostToDevice, st);
+  }
+  void adam() {
+    k_adam<<<blocks(nparam), 256, 0, st>>>(param, grad, adam_m, adam_v, nparam, hyper, kB1, kB2, 1e-8f);
     refresh_weights();
+  }
+  void step_kernels() {
+    forward(in_stage);
+    backward(tgt_stage);
+    adam();
+  }
+  // One training step on device inputs [nb][3][H][W] and targets
+  // [nb][2][H][W] (FP32, planar).  The first step of a batch size runs
+  // plain launches (it also sets the kernels' attributes); the second is
+  // captured into a graph, which the later steps replay.  A capture that
+  // fails falls back to plain launches for good.
+  void train_step(const float* in_dev, const float* tgt_dev, float lr) {
+    const size_t npix = (size_t)H * W;
+    cudaMemcpyAsync(in_stage, in_dev, sizeof(float) * 3 * npix * nb, cudaMemcpyDeviceToDevice, st);
+    cudaMemcpyAsync(tgt_stage, tgt_dev, sizeof(float) * 2 * npix * nb, cudaMemcpyDeviceToDevice, st);
+    adam_hyper(lr);
+    if (graph_ok_ && tgraph && tgraph_nb == nb) {
+      cudaGraphLaunch(tgraph, st);
+      return;
+    }
+    if (graph_ok_ && tgraph_nb == -nb) {  // second step of this batch size: capture
+      if (tgraph) cudaGraphExecDestroy(tgraph);
+      tgraph = nullptr;
+      cudaGraph_t g = nullptr;
+      if (cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal) == cudaSuccess) {
+        step_kernels();
+        if (cudaStreamEndCapture(st, &g) == cudaSuccess && g && cudaGraphInstantiate(&tgraph, g, 0) == cudaSuccess) {
+          tgraph_nb = nb;
+        } else {
+          tgraph = nullptr;
+          graph_ok_ = false;
+        }
+        if (g) cudaGraphDestroy(g);
+      } else {
+        graph_ok_ = false;
+      }
+      cudaGetLastError();
+      if (tgraph) {
+        cudaGraphLaunch(tgraph, st);
+        return;
+      }
+    }
+    step_kernels();
+    if (graph_ok_ && tgraph_nb != nb) tgraph_nb = -nb;
   }
 
   int check() {
@@ -1721,9 +1791,7 @@ extern "C" int vk_nn_loss_grad(void* net, const float* in_dev, const float* targ
 extern "C" int vk_nn_train_step(void* net, const float* in_dev, const float* target_dev, float lr, double* loss_out) {
   Net* x = as_net(net);
   if (!x || !in_dev || !target_dev) { set_error("vk_nn_train_step: null argument"); return VK_E_INVALID; }
-  x->forward(in_dev);
-  x->backward(target_dev);
-  x->adam(lr);
+  x->train_step(in_dev, target_dev, lr);
   if (loss_out) cudaMemcpyAsync(loss_out, x->loss, sizeof(double), cudaMemcpyDeviceToHost, x->st);
   return x->check();
 }
