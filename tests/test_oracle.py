@@ -2,8 +2,9 @@
 
 Parity with the reference binary is unpinned (no Fortran/FFTW here and no
 reference tests), so the oracle is pinned by: numpy's FFT, exact
-known answers of the equation, and an independent numpy restatement of one
-RK4 step, one ARGLE step and the diagnostics.
+known answers of the equation (plane waves under RK4 and ARGLE, uniform
+states, linear dispersion, particles in a uniform state), and an independent
+numpy restatement of one RK4 step, one ARGLE step and the diagnostics.
 """
 import math
 
@@ -60,6 +61,67 @@ def test_plane_wave_rk4_known_answer(k):
     o.gpe_rk4(7)
     a = _plane_wave_rk4(p.alpha, p.gstrength, p.omega_chem, p.dt, k[0] ** 2 + k[1] ** 2, 7)
     assert np.abs(o.get_psi() - a * psi0).max() < 1e-13
+
+
+@pytest.mark.parametrize("k", [(2, 1), (0, -6)])
+def test_plane_wave_argle_known_answer(k):
+    """ARGLE on a plane wave A e^{ik.x} (src/gpe.f90:5-224): |psi|^2 is uniform,
+    so P_G rho = |A|^2 and N^ = -g |A|^2 psi^, and each step is the scalar
+    recurrence A <- A (1 + dt (Omega - g |A|^2)) / (1 + alpha k^2 dt); the
+    residual is |A_new - A_old| / (dt |A_old|) of the last step."""
+    n = 32
+    p = vk.params_for(n, dt=1e-3)
+    o = Oracle.from_vk_params(p)
+    X, Y = _grid(n)
+    a0 = 0.7 + 0.2j
+    psi0 = a0 * np.exp(1j * (k[0] * X + k[1] * Y))
+    o.set_psi(psi0, otoc=False)
+    r = o.argle(9)
+    a, k2 = a0, k[0] ** 2 + k[1] ** 2
+    for _ in range(9):
+        prev = a
+        a = a * (1 + p.dt * (p.omega_chem - p.gstrength * abs(a) ** 2)) / (1 + p.alpha * k2 * p.dt)
+    kp = o.get_kpsi()  # [kx][ky], unnormalised
+    expect = np.zeros((n, n), complex)
+    expect[k[0] % n, k[1] % n] = a * n * n
+    assert np.abs(kp - expect).max() < 1e-12 * n * n
+    assert abs(r - abs(a - prev) / (p.dt * abs(prev))) < 1e-9 * r
+
+
+def _uniform_with_particles(pos, f0):
+    n = 64
+    dx = 2 * math.pi / n
+    d = 2.0 * math.sqrt(2.0) * dx
+    p = vk.params_for(n, dt=1e-3, n_particles=len(pos), ppotd=2.0, ppotv0=10.0, gp_mass_part=5.0 * math.pi * d * d)
+    o = Oracle.from_vk_params(p)
+    o.set_psi(np.ones((n, n), complex), otoc=False)
+    o.particles_set(np.asarray(pos, float), np.zeros((len(pos), 2)), np.asarray(f0, float))
+    return o, p
+
+
+def test_particle_in_uniform_condensate_feels_only_its_external_force():
+    """grad rho = 0 in a uniform state, so the fluid force of
+    translate_particle_potential (src/gpe_particle.f90:219-324) vanishes and a
+    single particle (no repulsion) feels exactly f0ext."""
+    o, _ = _uniform_with_particles([[1.3, 4.1]], [[0.05, -0.02]])
+    assert np.abs(o.particle_forces() - np.array([[0.05, -0.02]])).max() < 1e-13
+
+
+def test_two_particle_repulsion_known_answer():
+    """Two particles in a uniform state: the forces are the short-range
+    repulsion of src/gpe_particle.f90:378-427 alone, equal and opposite, with
+    the closed form -384 dE pi^12 r0^12 / L^12 sin(dq) / (-3 + cos dqx + cos dqy)^7
+    (dE the single-precision literal 0.062, r0 = 4 xi, L = 2 pi)."""
+    q = np.array([[1.0, 2.0], [1.9, 1.4]])
+    o, p = _uniform_with_particles(q, np.zeros((2, 2)))
+    f = o.particle_forces()
+    de = float(np.float32(0.062))
+    rf = 384.0 * de * math.pi ** 12 * (4.0 * p.xi) ** 12 / (2 * math.pi) ** 12
+    dq = q[0] - q[1]
+    den = (-3 + math.cos(dq[0]) + math.cos(dq[1])) ** 7
+    f01 = -rf * np.sin(dq) / den
+    assert np.abs(f[0] + f[1]).max() < 1e-12 * np.abs(f01).max()
+    assert np.abs(f[0] - f01).max() < 1e-12 * np.abs(f01).max()
 
 
 def test_uniform_state_stationary():
