@@ -88,6 +88,30 @@ def test_plane_wave_argle_known_answer(k):
     assert abs(r - abs(a - prev) / (p.dt * abs(prev))) < 1e-9 * r
 
 
+def test_plane_wave_diagnostics_known_answer():
+    """diagnostics_gpe (src/diagnostics.f90:4-571) of A e^{ik.x}: the box
+    averages are exact, so norm = |A|^2 L^2, mom = 2 alpha |A|^2 k,
+    Egrad = 2 alpha^2 |A|^2 k^2, Echem = 2 alpha Omega |A|^2,
+    Eint = alpha g |A|^4 (P_G keeps the uniform density), Etot = Egrad + Eint,
+    and the |kpsi|^2 spectrum holds |A|^2 in the shell nint(|k|) alone."""
+    n = 32
+    p = vk.params_for(n, dt=1e-3)
+    o = Oracle.from_vk_params(p)
+    X, Y = _grid(n)
+    a0, k = 0.8 - 0.3j, (3, -4)
+    o.set_psi(a0 * np.exp(1j * (k[0] * X + k[1] * Y)), otoc=False)
+    sc, spec = o.diagnostics()
+    al, g, om, a2 = p.alpha, p.gstrength, p.omega_chem, abs(a0) ** 2
+    k2 = k[0] ** 2 + k[1] ** 2
+    want = {0: 2 * al * a2 * k[0], 1: 2 * al * a2 * k[1], 2: 2 * al * al * a2 * k2, 3: 2 * al * om * a2,
+            4: al * g * a2 * a2, 5: 2 * al * al * a2 * k2 + al * g * a2 * a2, 6: a2 * (2 * math.pi) ** 2}
+    for i, w in want.items():
+        assert abs(sc[i] - w) <= 1e-12 * max(1.0, abs(w)), i
+    shell = np.zeros(spec.shape[1])
+    shell[int(round(math.sqrt(k2)))] = a2
+    assert np.abs(spec[5] - shell).max() <= 1e-12
+
+
 def _uniform_with_particles(pos, f0):
     n = 64
     dx = 2 * math.pi / n
