@@ -1,4 +1,5 @@
-"""Exact known answers on the GPU path (FP64), independent of the oracle.
+"""Exact known answers and exact properties of the GPU path (FP64),
+independent of the oracle.
 
 A plane wave A e^{ik.x} keeps a uniform density, so P_G |psi|^2 = |A|^2 and
 the passes reduce to scalar maps of the amplitude:
@@ -8,7 +9,10 @@ the passes reduce to scalar maps of the amplitude:
 * diagnostics_gpe (src/diagnostics.f90:4-571): norm = |A|^2 L^2, mom = 2 alpha |A|^2 k,
   Egrad = 2 alpha^2 |A|^2 k^2, Echem = 2 alpha Omega |A|^2, Eint = alpha g |A|^4, and the
   |kpsi|^2 spectrum holds |A|^2 in the shell nint(|k|) alone.
-Bounds: 1e-12 (FP64 rounding of a few hundred transforms of an O(1) field).
+With g = Omega = 0 every mode follows the RK4 polynomial R(z)^n of its
+linear rotation, and at 1024^2 the step commutes with a shift by whole grid
+points.  Bounds: 1e-12 (FP64 rounding of a few hundred transforms of an O(1)
+field).
 """
 import math
 
@@ -83,3 +87,46 @@ def test_plane_wave_diagnostics():
     shell = np.zeros(d.spec.shape[1])
     shell[int(round(math.sqrt(k2)))] = a2
     assert np.abs(d.spec[5] - shell).max() <= 1e-12
+
+
+def test_linear_dispersion_without_interaction():
+    """g = Omega = 0: every mode evolves by the RK4 polynomial of
+    z = -i alpha k^2 dt, psi^(t_n) = R(z)^n psi^(0), R = 1 + z + z^2/2 + z^3/6 + z^4/24."""
+    n = 64
+    p = vk.params_for(n, dt=2e-3, otoc=False)
+    p.gstrength = 0.0
+    p.omega_chem = 0.0
+    x = np.arange(n) * 2 * np.pi / n
+    X, Y = np.meshgrid(x, x)
+    rng = np.random.default_rng(5)
+    psi0 = np.zeros((n, n), complex)
+    for kx, ky in [(1, 2), (-3, 4), (5, -1), (0, 7)]:
+        psi0 += (rng.standard_normal() + 1j * rng.standard_normal()) * np.exp(1j * (kx * X + ky * Y))
+    with vk.GPESolver(p) as s:
+        s.set_psi(psi0)
+        s.gpe_rk4(6)
+        got = s.get_psi()
+    kk = np.fft.fftfreq(n, 1.0 / n)
+    KX, KY = np.meshgrid(kk, kk)
+    z = -1j * p.alpha * (KX ** 2 + KY ** 2) * p.dt
+    R = 1 + z + z * z / 2 + z ** 3 / 6 + z ** 4 / 24
+    want = np.fft.ifft2(np.fft.fft2(psi0) * R ** 6)
+    assert np.abs(got - want).max() < 1e-12 * np.abs(want).max()
+
+
+def test_translation_equivariance_at_1024():
+    """The step commutes with a shift by whole grid points (all the physics is
+    in Fourier multipliers and pointwise products): 1024^2 FP64, 64 vortices,
+    5 RK4 steps from psi and from psi rolled by (37, -101)."""
+    n = 1024
+    p = vk.params_for(n, dt=5e-4)
+    psi0, _ = vk.ic_vortices(n, n, 64, seed=9, min_sep=4 * math.sqrt(2) * 2 * math.pi / n)
+    shift = (37, -101)
+    out = []
+    for psi in (psi0, np.roll(psi0, shift, axis=(0, 1))):
+        with vk.GPESolver(p) as s:
+            s.set_psi(np.ascontiguousarray(psi))
+            s.gpe_rk4(5)
+            out.append(s.get_psi())
+    a, b = np.roll(out[0], shift, axis=(0, 1)), out[1]
+    assert np.linalg.norm(a - b) / np.linalg.norm(b) < 1e-12
