@@ -11,8 +11,8 @@ the passes reduce to scalar maps of the amplitude:
   |kpsi|^2 spectrum holds |A|^2 in the shell nint(|k|) alone.
 With g = Omega = 0 every mode follows the RK4 polynomial R(z)^n of its
 linear rotation, and at 1024^2 the step commutes with a shift by whole grid
-points.  Bounds: 1e-12 (FP64 rounding of a few hundred transforms of an O(1)
-field).
+points and with a quarter turn.  Bounds: 1e-12 (FP64 rounding of a few
+hundred transforms of an O(1) field); the FP32 plane wave to 1e-5.
 """
 import math
 
@@ -130,3 +130,44 @@ def test_translation_equivariance_at_1024():
             out.append(s.get_psi())
     a, b = np.roll(out[0], shift, axis=(0, 1)), out[1]
     assert np.linalg.norm(a - b) / np.linalg.norm(b) < 1e-12
+
+
+def test_rotation_equivariance_at_1024():
+    """A quarter turn of the grid commutes with the step: the kinetic operator
+    and the 2/3 disk are isotropic, and the quarter turn swaps the x passes
+    (real-row transforms) with the y passes (complex, transposed layout), so
+    the two sides run different kernels on the same physics."""
+    n = 1024
+    p = vk.params_for(n, dt=5e-4)
+    psi0, _ = vk.ic_vortices(n, n, 64, seed=12, min_sep=4 * math.sqrt(2) * 2 * math.pi / n)
+    out = []
+    for psi in (psi0, np.rot90(psi0)):
+        with vk.GPESolver(p) as s:
+            s.set_psi(np.ascontiguousarray(psi))
+            s.gpe_rk4(5)
+            out.append(s.get_psi())
+    a, b = np.rot90(out[0]), out[1]
+    assert np.linalg.norm(a - b) / np.linalg.norm(b) < 1e-12
+
+
+def test_plane_wave_rk4_fp32():
+    """The FP32 path (background density moved out of the transforms) on the
+    plane wave: the scalar RK4 map to FP32 accuracy (1e-5 relative)."""
+    n = 256
+    p = vk.params_for(n, dt=5e-4, precision=vk.VK_PREC_FP32, otoc=False)
+    psi0 = _plane_wave(n)
+    with vk.GPESolver(p) as s:
+        s.set_psi(psi0)
+        s.gpe_rk4(10)
+        got = s.get_psi()
+    k2 = K[0] ** 2 + K[1] ** 2
+    f = lambda a: -1j * (p.alpha * k2 - p.omega_chem + p.gstrength * abs(a) ** 2) * a
+    a, dt = A0, p.dt
+    for _ in range(10):
+        k1 = f(a)
+        k2_ = f(a + dt / 2 * k1)
+        k3 = f(a + dt / 2 * k2_)
+        k4 = f(a + dt * k3)
+        a = a + dt / 6 * (k1 + 2 * k2_ + 2 * k3 + k4)
+    want = psi0 * (a / A0)
+    assert np.abs(got - want).max() < 1e-5 * np.abs(want).max()
