@@ -135,3 +135,24 @@ def test_particles_fp32_bulk():
     opos, _, _ = o.particles_get()
     assert np.abs(pos - opos).max() < 1e-6
     s.close()
+
+
+def test_two_particle_repulsion_closed_form():
+    """Two particles in a uniform fluid (grad rho = 0: no fluid force) feel
+    the short-range repulsion of src/gpe_particle.f90:378-427 alone:
+    -384 dE pi^12 r0^12 / L^12 sin(dq) / (-3 + cos dqx + cos dqy)^7, with the
+    single-precision literal dE = 0.062, r0 = 4 xi and L = 2 pi."""
+    n = 64
+    p = _params(n, 2)
+    s = vk.GPESolver(p)
+    s.set_psi(np.ones((n, n), complex))
+    q = np.array([[1.0, 2.0], [1.9, 1.4]])
+    s.particles_set(q, np.zeros((2, 2)), np.zeros((2, 2)))
+    s.diagnostics_gpe()
+    _, _, frc = s.particles_get()
+    s.close()
+    rf = 384.0 * float(np.float32(0.062)) * math.pi ** 12 * (4.0 * p.xi) ** 12 / (2 * math.pi) ** 12
+    dq = q[0] - q[1]
+    f01 = -rf * np.sin(dq) / (-3 + math.cos(dq[0]) + math.cos(dq[1])) ** 7
+    assert np.abs(frc[0] - f01).max() <= 1e-12 * np.abs(f01).max()
+    assert np.abs(frc[1] + f01).max() <= 1e-12 * np.abs(f01).max()
